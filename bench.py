@@ -1,0 +1,357 @@
+"""Benchmark of the Gerstner water-surface path on GB300.
+
+Metric: Gerstner terms/s = sum over patches of (vertices x waves) per second,
+at <= 1e-5 relative displacement error vs FP64 (the error bound is enforced by
+tests/; this file only times).  Workload: the batched configuration — 256
+independent patches, grid side log-uniform in [64, 1024], 8..64 waves each,
+t U[0, 1e3] s, with the 512^2 noise heightmap layer — as one persistent
+launch.  A step = the three launches of one wt_gerstner_displace call
+(validate/sort, FP64 phase constants, persistent forward).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  Under torchrun each rank runs its own
+256-patch workload (seed 2 + rank; weak scaling, no collective on the data
+path) and the step time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import __graft_entry__  # noqa: E402
+
+METRIC = "Gerstner terms/s (verts x waves) at <=1e-5 rel err vs FP64; batched persistent launch"
+UNIT = "terms/s"
+PROFILE_TRAFFIC = ROOT / "profiles" / "forward_config3_ncu.md"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--patches", type=int, default=256)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
+    ap.add_argument("--no-extras", action="store_true", help="skip the unbatched / single-patch side runs")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) != 7:
+                continue
+            try:
+                rows.append((float(parts[0]), float(parts[1]), float(parts[2]), parts[3:]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        # samples under load: power well above idle
+        pmax = max(r[2] for r in rows)
+        load = [r for r in rows if r[2] >= 0.5 * pmax] or rows
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in load for i, v in enumerate(r[3]) if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(r[0] for r in load), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(load), "power_w_max": pmax}
+
+
+def traffic_from_profile():
+    """DRAM bytes per forward launch from the committed ncu summary, if any."""
+    if not PROFILE_TRAFFIC.exists():
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", PROFILE_TRAFFIC.read_text())
+    return float(m.group(1)) if m else None
+
+
+def cpu_sample(w, target_s: float, threads: int):
+    """Runs the oracle's FP32 restatement of the reference shader (5 surface
+    evaluations per vertex, central-difference normals) over the first rows
+    of every patch, rows chosen so the run lasts about target_s."""
+    from oracle import oracle as O
+    import types
+    hmp = None
+    tex = None
+    if w.heightmap is not None:
+        tex = O.noise_f64(w.heightmap.terms, w.heightmap.width, w.heightmap.height).astype(np.float32)
+        hmp = types.SimpleNamespace(sample_scale=w.heightmap.sample_scale, disp_scale=w.heightmap.disp_scale,
+                                    wrap=w.heightmap.wrap)
+    t0 = time.perf_counter()
+    O.cpu_baseline(w.patches, w.waves, tex, hmp, row_limit=1, threads=threads)
+    probe = time.perf_counter() - t0
+    rows = max(1, min(int(target_s / max(probe, 1e-3)), int(w.patches["rows"].max())))
+    t0 = time.perf_counter()
+    nv, _, _ = O.cpu_baseline(w.patches, w.waves, tex, hmp, row_limit=rows, threads=threads)
+    dt = time.perf_counter() - t0
+    terms = int(sum(min(rows, int(p["rows"])) * int(p["cols"]) * int(p["wave_count"]) for p in w.patches))
+    return terms / dt, dt, rows, terms
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT))
+    from oracle import build as ob
+    ob.build_oracle()
+    wt = __graft_entry__.load_package()
+    from wave_tool_gb300 import workloads
+    w = workloads.config3(n_patches=args.patches, seed=2)
+    threads = os.cpu_count() or 1
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps))
+    rates, dts = [], []
+    for i in range(args.warmup + args.steps):
+        r, dt, rows, terms = cpu_sample(w, per_step, threads)
+        if i >= args.warmup:
+            rates.append(r)
+            dts.append(dt)
+    value = statistics.median(rates)
+    sample = f"first {rows} rows of each of the {args.patches} patches ({terms} terms) per step"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(dts),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w.name, "patches": args.patches, "terms": w.n_terms,
+                   "implementation": "FP32 restatement of water-grid.vert (5 evaluations/vertex, FD normals), "
+                                     "POSIX threads on all host cores"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    del wt
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    wt = __graft_entry__.load_package()
+    wt.lib()
+    from wave_tool_gb300 import workloads
+
+    w = workloads.config3(n_patches=args.patches, seed=2 + rank)
+    hm = wt.heightmap_from(w.heightmap)
+    surf = wt.Surface(w.patches, w.waves, hm)
+    flags = wt.WT_OUT_DISPLACEMENT
+    pos, nrm = surf.alloc_outputs(flags)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    def step():
+        surf.displace(pos, nrm, flags=flags)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    st, bad = surf.status()
+    if st != 0:
+        raise RuntimeError(f"device validation failed: {st} at patch {bad}")
+
+    fma_s, sin_s = wt.measure_peaks()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        barrier()
+        t_wall = time.perf_counter()
+        for e0, e1 in ev:
+            flush.zero_()  # evict L2 between steps (outside the timed events)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+        barrier()
+        t_wall = time.perf_counter() - t_wall
+    ms = [e0.elapsed_time(e1) for e0, e1 in ev]
+    ms_step = sum(ms) / len(ms)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_step], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    terms = w.n_terms
+    value = terms * world / (ms_step * 1e-3)
+
+    # end to end through the C ABI from pinned host buffers
+    hp = torch.from_numpy(np.ascontiguousarray(w.patches).view(np.uint8).reshape(-1)).pin_memory()
+    hw = torch.from_numpy(np.ascontiguousarray(w.waves).view(np.uint8).reshape(-1)).pin_memory()
+    htex = hm.texels.cpu().pin_memory()
+    hpos = torch.empty(pos.shape, dtype=pos.dtype, pin_memory=True)
+    hnrm = torch.empty(nrm.shape, dtype=nrm.dtype, pin_memory=True)
+    h2d = hp.numel() + hw.numel() + htex.numel() * 4
+    d2h = hpos.numel() * 4 + hnrm.numel() * 4
+
+    def e2e_step():
+        surf.patches.copy_(hp, non_blocking=True)
+        surf.waves.copy_(hw, non_blocking=True)
+        hm.texels.copy_(htex, non_blocking=True)
+        surf.displace(pos, nrm, flags=flags)
+        hpos.copy_(pos, non_blocking=True)
+        hnrm.copy_(nrm, non_blocking=True)
+
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = terms * world / (e2e_ms * 1e-3)
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        # 256 plain launches (one wt_gerstner_displace per patch)
+        for _ in range(2):
+            surf.displace(pos, nrm, flags=flags, unbatched=True)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n_plain = 3
+        a.record(stream)
+        for _ in range(n_plain):
+            surf.displace(pos, nrm, flags=flags, unbatched=True)
+        b.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = a.elapsed_time(b) / n_plain
+        extras["unbatched_256_launches"] = {"ms_per_step": plain_ms, "value": terms / (plain_ms * 1e-3),
+                                            "batched_speedup": plain_ms / ms_step}
+        # the single 1024^2 / 32-wave / noise patch
+        w2 = workloads.config2()
+        s2 = wt.Surface(w2.patches, w2.waves, wt.heightmap_from(w2.heightmap))
+        p2, n2 = s2.alloc_outputs(flags)
+        for _ in range(5):
+            s2.displace(p2, n2, flags=flags)
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(20)]
+        for x, y in evs:
+            flush.zero_()
+            x.record(stream)
+            s2.displace(p2, n2, flags=flags)
+            y.record(stream)
+        torch.cuda.synchronize()
+        ms2 = statistics.median(x.elapsed_time(y) for x, y in evs)
+        extras["single_patch_1024sq_32waves_noise"] = {"ms_per_step": ms2, "value": w2.n_terms / (ms2 * 1e-3)}
+
+    cpu = None
+    if rank == 0:
+        r, dt, rows, cterms = cpu_sample(w, args.cpu_seconds, os.cpu_count() or 1)
+        cpu = {"value": r, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"first {rows} rows of each of the {args.patches} patches ({cterms} terms, {dt:.1f} s); "
+                         "FP32 restatement of water-grid.vert, 5 evaluations/vertex"}
+
+    if rank == 0:
+        clocks = clk.summary()
+        peak_fma_terms = fma_s / 10.0   # 10 FMA of algorithmic work per term
+        peak_mufu_terms = sin_s / 2.0   # sin + cos per term on the MUFU pipe
+        achieved = value / world
+        verts = int(np.sum(w.patches["cols"].astype(np.int64) * w.patches["rows"]))
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (SplitMix64 seed 2 + rank)",
+            "config": {"workload": w.name, "patches": args.patches, "vertices": verts, "terms_per_step": terms,
+                       "waves_per_patch": "8..64", "grid_side": "64..1024 log-uniform", "heightmap": "512^2 noise",
+                       "outputs": "float4 displacement + float4 normal", "phase": "FP64-reduced",
+                       "l2": "256 MiB buffer zeroed between timed steps (outside the per-step events)",
+                       "parallelism": f"weak x{world} (each GPU its own 256 patches)"},
+            "roofline": {"bound": "fma", "achieved": achieved / 1e9, "peak": peak_fma_terms / 1e9,
+                         "unit": "Gterms/s", "frac": achieved / peak_fma_terms,
+                         "traffic": traffic_from_profile(),
+                         "peak_source": "measured in this run by wt_measure_peaks (FP32 FMA probe)/10",
+                         "mufu_leg_peak": peak_mufu_terms / 1e9,
+                         "survey_min_peak": min(peak_fma_terms, peak_mufu_terms) / 1e9,
+                         "hbm_gbs": 32.0 * verts / (ms_step * 1e-3) / 1e9,
+                         "note": "achieved = terms per step / step time (prep launches included)"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "ms_per_step": e2e_ms},
+            "gpu_launches": 3 * args.steps,
+            "clocks": clocks,
+            "wall_s_timed_region": t_wall,
+            "extras": extras,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,245 @@
+/*
+ * wt.h — C ABI of the GB300-native Gerstner water-surface path.
+ *
+ * This header replaces the water-grid hot path of wave-tool: the host side in
+ * src/render-engine.cpp:1045-1115 (uniform upload + glDrawElements) and the
+ * per-vertex work in assets/shaders/water-grid.vert:74-194 (Gerstner sum,
+ * heightmap displacement, vertical bounce, normals), plus the projected-grid
+ * index buffer built in src/program.cpp:686-717.
+ *
+ * Conventions
+ *  - Plain C: no C++ types, no exceptions, no CUDA headers needed.
+ *    `wt_stream` is ABI-identical to cudaStream_t (pass one directly; NULL is
+ *    the legacy default stream).
+ *  - Every entry point returns a wt_status; wt_last_error() gives a message
+ *    for the last failure on the calling thread.
+ *  - The caller owns all device memory. Entry points that need scratch take a
+ *    caller-provided device `workspace` sized by the matching *_workspace_size
+ *    query; nothing allocates inside a launch call, so launch calls can be
+ *    captured into a CUDA graph.
+ *  - Launch calls are asynchronous on `stream`. Host-side validation errors are
+ *    returned immediately; device-side validation of the patch table (which
+ *    lives in device memory) is recorded in the workspace and read back with
+ *    wt_workspace_status().
+ */
+#ifndef WT_H
+#define WT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* wt_stream; /* same type as cudaStream_t */
+
+typedef enum wt_status {
+    WT_OK = 0,
+    WT_ERR_INVALID_ARG = 1,  /* bad pointer, size, alignment or parameter */
+    WT_ERR_CUDA = 2,         /* a CUDA runtime call failed (see wt_last_error) */
+    WT_ERR_TIMEOUT = 3,      /* a bounded device-side wait gave up */
+    WT_ERR_NOMEM = 4,        /* workspace smaller than the size query asked for */
+    WT_ERR_UNSUPPORTED = 5   /* a parameter combination this build does not handle */
+} wt_status;
+
+/* One Gerstner wave.  Replaces `struct GerstnerWave`
+ * (src/render-engine.h:130-167) and the per-wave uniforms
+ * (assets/shaders/water-grid.vert:45-51, src/render-engine.cpp:1067-1081).
+ *
+ *   theta = k * dot(D, xz) + speed * k * t + phase,   k = 2*pi / wavelength
+ *   P    += A * (D.x * Q * cos(theta), sin(theta), D.z * Q * cos(theta))
+ *
+ * `steepness_q` is the per-wave Q_i the shader consumes (the reference divides
+ * its user steepness by k*A*count on the host, render-engine.cpp:1073; use
+ * wt_wave_from_reference to apply that).  `speed * k` is the reference's
+ * phaseConstant_phi; `phase` is an extra constant offset (0 reproduces the
+ * reference).  wavelength = +inf means k = 0.  32 bytes, two float4 loads. */
+typedef struct wt_wave {
+    float amplitude;   /* A >= 0, metres */
+    float wavelength;  /* lambda > 0 (or +inf), metres */
+    float dir_x;       /* D, a unit xz direction */
+    float dir_z;
+    float steepness_q; /* Q_i */
+    float speed;       /* crest speed, m/s (omega = speed * k) */
+    float phase;       /* constant phase offset, radians */
+    float _pad;        /* must be 0 */
+} wt_wave;
+
+/* One projected-grid patch: a cols x rows vertex grid bilinearly spanning four
+ * world-space corners on the y = 0 plane (water-grid.vert:37-38,59-60,87-91).
+ * Vertex (row, col) has u = col/(cols-1), v = row/(rows-1); row 0 is the
+ * BL-BR edge, matching gl_VertexID = row*cols + col (water-grid.vert:115-125).
+ * Its outputs live at vertex index out_offset + row*cols + col. 72 bytes. */
+typedef struct wt_patch {
+    float bl[2];          /* world (x, z) of the bottom-left corner  (u=0, v=0) */
+    float br[2];          /* bottom-right (u=1, v=0) */
+    float tl[2];          /* top-left     (u=0, v=1) */
+    float tr[2];          /* top-right    (u=1, v=1) */
+    uint32_t cols;        /* vertices along u, >= 2 (the reference's gridLength) */
+    uint32_t rows;        /* vertices along v, >= 2 */
+    uint32_t wave_offset; /* first wave of this patch in the wave array */
+    uint32_t wave_count;  /* number of waves (0 allowed) */
+    double time_s;        /* wave animation time, seconds (waveAnimationTimeInSeconds) */
+    float y_offset;       /* vertical bounce displacement added to y (render-engine.cpp:299-300) */
+    uint32_t flags;       /* reserved, must be 0 */
+    uint64_t out_offset;  /* first output vertex of this patch */
+} wt_patch;
+
+enum { WT_WRAP_REPEAT = 0, WT_WRAP_MIRRORED_REPEAT = 1 };
+
+/* The heightmap-noise layer (water-grid.vert:93-111; sampler state
+ * src/texture.cpp:54-71).  Sampled at the Gerstner-displaced position with
+ * GL_LINEAR semantics (texel centres at i + 0.5) at texture coordinates
+ * sample_scale * (x', -z'); adds disp_scale * 2 * (r - 0.5) to y.
+ * `texels` is device memory, R32F, width*height values, texel (i, j) at
+ * texels[j*width + i], j = 0 is the t = 0 row.  The struct itself is a host
+ * struct passed by pointer. */
+typedef struct wt_heightmap {
+    const float* texels;
+    uint32_t width;
+    uint32_t height;
+    float sample_scale;   /* heightmapSampleScale */
+    float disp_scale;     /* heightmapDisplacementScale */
+    uint32_t wrap;        /* WT_WRAP_* */
+    uint32_t _pad;
+} wt_heightmap;
+
+/* Flags of wt_gerstner_displace / wt_gerstner_adjoint. */
+enum {
+    WT_OUT_WORLD = 0,           /* pos_out = displaced world position, w = 1 */
+    WT_OUT_DISPLACEMENT = 1,    /* pos_out = displaced - undisplaced grid position, w = 0 */
+    WT_LAYOUT_FLOAT4 = 0,       /* 16-byte stride per vertex (x, y, z, w) */
+    WT_LAYOUT_VEC3 = 2,         /* 12-byte tightly packed vec3 (the reference VAO layout,
+                                   render-engine.cpp:1175-1191) */
+    WT_PHASE_FP64 = 0,          /* per-wave phase reduced mod 2*pi in FP64 (default) */
+    WT_PHASE_FP32_NAIVE = 4     /* the reference's FP32 phase w*dot(D,xz) + phi*t, for
+                                   precision studies (water-grid.vert:78) */
+};
+
+/* Per-wave gradient of a loss.  d_direction is with respect to the angle of D
+ * (D = (cos a, sin a)); d_dir_x / d_dir_z are the raw component gradients. */
+typedef struct wt_wave_grad {
+    float d_amplitude;
+    float d_wavelength;
+    float d_direction;
+    float d_steepness_q;
+    float d_phase;
+    float d_speed;
+    float d_dir_x;
+    float d_dir_z;
+} wt_wave_grad;
+
+/* One term of the tileable noise heightmap:
+ *   h(i, j) += amplitude * sin(2*pi*(kx*i + ky*j)/size + phase). */
+typedef struct wt_noise_term {
+    int32_t kx;
+    int32_t ky;
+    float amplitude;
+    float phase;
+} wt_noise_term;
+
+/* ---- queries ------------------------------------------------------------ */
+
+const char* wt_version(void);
+/* Message for the last failing call on this thread ("" if none). */
+const char* wt_last_error(void);
+
+/* Workspace for wt_gerstner_displace over `n_patches` patches whose
+ * wave_count values sum to `total_wave_slots`. */
+wt_status wt_displace_workspace_size(uint32_t n_patches, uint64_t total_wave_slots,
+                                     size_t* bytes);
+
+/* Workspace for wt_gerstner_adjoint.  Takes a HOST copy of the patch table
+ * (the per-tile gradient partials depend on every patch's size). */
+wt_status wt_adjoint_workspace_size(const wt_patch* host_patches, uint32_t n_patches,
+                                    size_t* bytes);
+
+/* Reads back (synchronising `stream`) the device-side validation word that the
+ * last launch with this workspace wrote: WT_OK, or WT_ERR_INVALID_ARG with
+ * the first offending patch index in *bad_patch (may be NULL). */
+wt_status wt_workspace_status(const void* workspace, wt_stream stream, uint32_t* bad_patch);
+
+/* ---- the hot path ------------------------------------------------------- */
+
+/* Gerstner displacement + analytic normals (+ heightmap noise, + bounce) for
+ * every vertex of every patch, in one persistent launch.
+ * Replaces water-grid.vert:114-194 driven by render-engine.cpp:1045-1115.
+ *   patches, waves : device arrays
+ *   hm             : host struct (NULL = no heightmap layer)
+ *   pos_out        : device, out_capacity vertices, layout per flags
+ *   nrm_out        : device or NULL; unit normal oriented +y (w = 0)
+ * Normals are the exact normal of the displaced surface,
+ * normalize(dP/dz x dP/dx), not the reference's central differences. */
+wt_status wt_gerstner_displace(const wt_patch* patches, uint32_t n_patches,
+                               const wt_wave* waves, uint32_t n_waves,
+                               const wt_heightmap* hm,
+                               float* pos_out, float* nrm_out, uint64_t out_capacity,
+                               uint32_t flags, void* workspace, size_t workspace_bytes,
+                               wt_stream stream);
+
+/* The same work issued as one launch pair per patch (no batching).  Exists to
+ * measure the batched launch against; results are identical. */
+wt_status wt_gerstner_displace_unbatched(const wt_patch* host_patches,
+                                         const wt_patch* patches, uint32_t n_patches,
+                                         const wt_wave* waves, uint32_t n_waves,
+                                         const wt_heightmap* hm,
+                                         float* pos_out, float* nrm_out,
+                                         uint64_t out_capacity, uint32_t flags,
+                                         void* workspace, size_t workspace_bytes,
+                                         wt_stream stream);
+
+/* Vector-Jacobian product of wt_gerstner_displace: given dL/dpos (float4 per
+ * vertex, w ignored) and dL/dnrm (float4 per vertex or NULL), writes dL/dwave
+ * for every wave (device array of n_waves).  Deterministic: per-tile partial
+ * sums are reduced in a fixed order.  No reference counterpart (the reference
+ * has no derivatives); the forward it differentiates is water-grid.vert:74-111. */
+wt_status wt_gerstner_adjoint(const wt_patch* patches, uint32_t n_patches,
+                              const wt_wave* waves, uint32_t n_waves,
+                              const wt_heightmap* hm,
+                              const float* d_pos, const float* d_nrm, uint64_t out_capacity,
+                              uint32_t flags, wt_wave_grad* grad_out,
+                              void* workspace, size_t workspace_bytes, wt_stream stream);
+
+/* The projected-grid triangle list: for each cell (row, col) the triangles
+ * (r,c),(r+1,c+1),(r+1,c) and (r,c),(r,c+1),(r+1,c+1), vertex (r,c) =
+ * base_vertex + r*cols + c.  6*(cols-1)*(rows-1) uint32 into idx_out (device).
+ * Bit-exact with src/program.cpp:686-717 (there cols = rows = 513, base 0). */
+wt_status wt_grid_indices(uint32_t cols, uint32_t rows, uint32_t base_vertex,
+                          uint32_t* idx_out, wt_stream stream);
+
+/* Tileable noise heightmap: sum of integer-wavenumber sinusoids over a
+ * width x height texel grid, then normalised to [0, 1] (min -> 0, max -> 1)
+ * so the reference's 2*(r - 0.5) mapping (water-grid.vert:106-111) holds.
+ * terms: device array.  Needs 16 bytes of workspace.  No reference
+ * counterpart: the reference loads a fixed PNG (render-engine.cpp:1308-1322). */
+wt_status wt_noise_synth(const wt_noise_term* terms, uint32_t n_terms,
+                         uint32_t width, uint32_t height, float* texels_out,
+                         void* workspace, size_t workspace_bytes, wt_stream stream);
+
+/* ---- reference parameter conversion (host only) ------------------------- */
+
+/* Converts one reference GerstnerWave (render-engine.h:137-141) into a
+ * wt_wave, applying the steepness normalisation of render-engine.cpp:1073
+ * (Q_i = Q / (w*A*count), 0 when w*A == 0) in the reference's FP32 order.
+ * wavelength = 2*pi/w, speed = phi/w, phase = 0.  A reference wave with w = 0
+ * and A*phi != 0 (a spatially uniform bob) has no wt_wave form and gives
+ * WT_ERR_UNSUPPORTED. */
+wt_status wt_wave_from_reference(float amplitude_A, float frequency_w,
+                                 float phase_constant_phi, float steepness_Q,
+                                 float dir_x, float dir_z, uint32_t wave_count,
+                                 wt_wave* out);
+
+/* ---- measurement helpers ------------------------------------------------ */
+
+/* Measures this GPU's FP32 FMA rate (FMA/s) and MUFU sine rate (sin/s) with
+ * dependent-chain microkernels on `stream`.  scratch: device, >= 4 MiB.
+ * Synchronises the stream.  Used for the roofline denominator. */
+wt_status wt_measure_peaks(void* scratch, size_t scratch_bytes, double* fma_per_s,
+                           double* sin_per_s, wt_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WT_H */

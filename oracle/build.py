@@ -1,0 +1,75 @@
+"""Build recipe of the CPU oracle (test infrastructure only).
+
+``build_oracle()`` compiles the C restatement (gerstner_f64.c,
+reference_mode.c, indices_noise.c) into ``oracle/_build/liboracle.so``.
+``build_ref()`` compiles the reference's own vertex shader
+(``assets/shaders/water-grid.vert`` under the reference checkout) as C++ over
+``glsl_shim.hpp`` into ``oracle/_ref/libwgvert_ref.so``; it needs the
+reference checkout and is skipped without it.
+
+Both use -ffp-contract=off so that FP32 results do not depend on whether the
+host compiler fuses multiply-adds (x86_64 and aarch64 give the same bits).
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+REF_OUT = HERE / "_ref"
+SOURCES = ["gerstner_f64.c", "reference_mode.c", "indices_noise.c"]
+LIB = BUILD / "liboracle.so"
+REF_LIB = REF_OUT / "libwgvert_ref.so"
+CFLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-std=c11", "-Wall"]
+
+
+def reference_dir() -> Path:
+    return Path(os.environ.get("WT_REFERENCE_DIR", "/root/reference"))
+
+
+def _stale(out: Path, deps) -> bool:
+    if not out.exists():
+        return True
+    t = out.stat().st_mtime
+    return any(Path(d).stat().st_mtime > t for d in deps)
+
+
+def build_oracle(force: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    deps = [HERE / s for s in SOURCES] + [HERE / "wt_oracle.h", HERE.parent / "include" / "wt.h"]
+    if force or _stale(LIB, deps):
+        cmd = ["gcc", *CFLAGS, "-shared", "-o", str(LIB), *[str(HERE / s) for s in SOURCES],
+               "-lm", "-lpthread"]
+        subprocess.run(cmd, check=True)
+    return LIB
+
+
+def build_ref(force: bool = False) -> Path | None:
+    """Compile the reference shader where it lies; None if it is absent."""
+    src = reference_dir() / "assets" / "shaders" / "water-grid.vert"
+    if not src.exists():
+        return None
+    REF_OUT.mkdir(exist_ok=True)
+    deps = [src, HERE / "glsl_shim.hpp", HERE / "ref_driver.inc", HERE / "wt_oracle.h"]
+    if not (force or _stale(REF_LIB, deps)):
+        return REF_LIB
+    text = src.read_text()
+    first, _, body = text.partition("\n")
+    if not first.startswith("#version"):
+        raise RuntimeError(f"unexpected first line in {src}: {first!r}")
+    # The GLSL '#version' line is the only line that is not C++; it is dropped
+    # and the rest is compiled unchanged between the shim and the driver.
+    tu = ('#include "glsl_shim.hpp"\n'
+          f'#line 2 "{src}"\n' + body +
+          '\n#include "ref_driver.inc"\n')
+    cmd = ["g++", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+           "-std=gnu++17", "-w", "-I", str(HERE), "-x", "c++", "-", "-o", str(REF_LIB)]
+    subprocess.run(cmd, input=tu.encode(), check=True)
+    return REF_LIB
+
+
+if __name__ == "__main__":
+    print(build_oracle(force=True))
+    print(build_ref(force=True))

@@ -1,0 +1,228 @@
+"""ctypes binding of the CPU oracle.  TEST INFRASTRUCTURE ONLY.
+
+Loaded by tests/, by the smoke check and by the CPU-baseline leg of bench.py,
+only as the checker / the timed CPU restatement.  The product under
+wave-tool_gb300/ never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_ref = None
+
+
+class Heightmap(C.Structure):
+    _fields_ = [("texels", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("sample_scale", C.c_float), ("disp_scale", C.c_float), ("wrap", C.c_uint32),
+                ("_pad", C.c_uint32)]
+
+
+class RefWave(C.Structure):
+    _fields_ = [(n, C.c_float) for n in
+                ("amplitude_A", "frequency_w", "phaseConstant_phi", "steepness_Q_i", "dir_x", "dir_z")]
+
+
+class RefUniforms(C.Structure):
+    _fields_ = [("bottom_left", C.c_float * 4), ("bottom_right", C.c_float * 4),
+                ("top_left", C.c_float * 4), ("top_right", C.c_float * 4),
+                ("camera_position", C.c_float * 3), ("grid_length", C.c_uint32),
+                ("wave_count", C.c_uint32), ("waves", C.POINTER(RefWave)),
+                ("phase_offset", C.POINTER(C.c_float)), ("hm", Heightmap),
+                ("vertical_bounce", C.c_float), ("time_s", C.c_float),
+                ("view_only_yaw", C.c_float * 16), ("view_projection", C.c_float * 16)]
+
+
+class RefOutputs(C.Structure):
+    _fields_ = [(n, C.POINTER(C.c_float)) for n in
+                ("position", "clip", "ndc0", "view", "normal", "normal_yaw", "colour")]
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _fptr(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if not path.exists():
+            _build.build_oracle()
+        _lib = C.CDLL(str(path))
+        vp = C.c_void_p
+        _lib.wto_displace_f64.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp, vp, vp, vp]
+        _lib.wto_adjoint_f64.argtypes = [vp, vp, vp, vp, vp, vp]
+        _lib.wto_reference_vertex.argtypes = [C.POINTER(RefUniforms), C.c_uint32, C.c_uint32,
+                                              C.POINTER(RefOutputs)]
+        for f in (_lib.wto_cpu_reference, _lib.wto_cpu_analytic):
+            f.argtypes = [vp, C.c_uint32, vp, vp, C.c_uint32, C.c_int, vp, vp]
+            f.restype = C.c_uint64
+        _lib.wto_grid_indices.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, vp]
+        _lib.wto_noise_f64.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, vp]
+        _lib.wto_wave_to_reference.argtypes = [vp, C.POINTER(RefWave)]
+    return _lib
+
+
+def ref_lib():
+    """The reference shader compiled from its own source, or None when the
+    reference checkout is not on this machine."""
+    global _ref
+    if _ref is None:
+        path = _build.REF_LIB
+        if not path.exists():
+            if _build.build_ref() is None:
+                return None
+        _ref = C.CDLL(str(path))
+        _ref.wtref_vertex.argtypes = [C.POINTER(RefUniforms), C.c_uint32, C.c_uint32,
+                                      C.POINTER(RefOutputs)]
+        _ref.wtref_vertex.restype = C.c_int
+    return _ref
+
+
+def make_hm(texels: np.ndarray | None, sample_scale=0.0, disp_scale=0.0, wrap=0) -> Heightmap:
+    h = Heightmap()
+    if texels is None:
+        h.texels = None
+        h.width = h.height = 1
+    else:
+        assert texels.dtype == np.float32 and texels.flags.c_contiguous
+        h.texels = texels.ctypes.data
+        h.height, h.width = texels.shape
+    h.sample_scale, h.disp_scale, h.wrap = sample_scale, disp_scale, wrap
+    return h
+
+
+def displace_f64(patches, waves, texels=None, hm_params=None, rows=None):
+    """FP64 truth over every patch.  Returns (pos, disp, nrm, edge) arrays with
+    one row per output vertex (placed at each patch's out_offset)."""
+    L = lib()
+    n_out = int(max(int(p["out_offset"]) + int(p["cols"]) * int(p["rows"]) for p in patches))
+    pos = np.zeros((n_out, 3)); disp = np.zeros((n_out, 3)); nrm = np.zeros((n_out, 3))
+    edge = np.full(n_out, np.inf)
+    hm = None
+    if texels is not None:
+        hm = make_hm(texels, hm_params.sample_scale, hm_params.disp_scale, hm_params.wrap)
+    for p in patches:
+        o = int(p["out_offset"]); nv = int(p["cols"]) * int(p["rows"])
+        r1 = int(p["rows"]) if rows is None else min(int(p["rows"]), rows)
+        pp = np.array(p).copy()
+        L.wto_displace_f64(_ptr(pp), _ptr(waves), C.byref(hm) if hm else None, 0, r1,
+                           _ptr(pos[o:o + nv]), _ptr(disp[o:o + nv]), _ptr(nrm[o:o + nv]),
+                           _ptr(edge[o:o + nv]))
+    return pos, disp, nrm, edge
+
+
+def adjoint_f64(patches, waves, gpos, gnrm=None, texels=None, hm_params=None):
+    L = lib()
+    grad = np.zeros((len(waves), 8))
+    hm = None
+    if texels is not None:
+        hm = make_hm(texels, hm_params.sample_scale, hm_params.disp_scale, hm_params.wrap)
+    gpos = np.ascontiguousarray(gpos, dtype=np.float32)
+    gnrm = None if gnrm is None else np.ascontiguousarray(gnrm, dtype=np.float32)
+    for p in patches:
+        pp = np.array(p).copy()
+        L.wto_adjoint_f64(_ptr(pp), _ptr(waves), C.byref(hm) if hm else None, _ptr(gpos),
+                          _ptr(gnrm), _ptr(grad))
+    return grad
+
+
+def reference_uniforms(corners_xz, grid_length, ref_waves, time_s, texels=None, sample_scale=0.02,
+                       disp_scale=1.0, wrap=1, bounce=0.0, camera=(0.0, 4.0, 70.0),
+                       view_projection=None, view_yaw=None, phase_offset=None):
+    """A wto_ref_uniforms; corners_xz = (BL, BR, TL, TR) world xz, ref_waves a
+    list of (A, w, phi, Q_i, Dx, Dz).  Returns (uniforms, keepalive)."""
+    U = RefUniforms()
+    for name, (x, z) in zip(("bottom_left", "bottom_right", "top_left", "top_right"), corners_xz):
+        getattr(U, name)[:] = [x, 0.0, z, 1.0]
+    U.camera_position[:] = list(camera)
+    U.grid_length = grid_length
+    arr = (RefWave * max(1, len(ref_waves)))()
+    for i, w in enumerate(ref_waves):
+        arr[i] = RefWave(*[float(v) for v in w])
+    U.wave_count = len(ref_waves)
+    U.waves = arr
+    ph = None
+    if phase_offset is not None:
+        ph = np.ascontiguousarray(phase_offset, dtype=np.float32)
+        U.phase_offset = _fptr(ph)
+    U.hm = make_hm(texels, sample_scale, disp_scale, wrap)
+    U.vertical_bounce = bounce
+    U.time_s = time_s
+    eye = np.eye(4, dtype=np.float32).ravel(order="F")
+    U.view_projection[:] = list(eye if view_projection is None else np.asarray(view_projection, np.float32).ravel(order="F"))
+    U.view_only_yaw[:] = list(eye if view_yaw is None else np.asarray(view_yaw, np.float32).ravel(order="F"))
+    return U, (arr, ph, texels)
+
+
+def _outputs(n):
+    o = {k: np.zeros((n, d), np.float32) for k, d in
+         (("position", 4), ("clip", 4), ("ndc0", 2), ("view", 3), ("normal", 3), ("normal_yaw", 3), ("colour", 4))}
+    R = RefOutputs(*[_fptr(o[k]) for k in ("position", "clip", "ndc0", "view", "normal", "normal_yaw", "colour")])
+    return o, R
+
+
+def reference_vertex(U, id0, id1):
+    """The FP32 restatement (oracle/reference_mode.c)."""
+    o, R = _outputs(id1 - id0)
+    lib().wto_reference_vertex(C.byref(U), id0, id1, C.byref(R))
+    return o
+
+
+def reference_shader_vertex(U, id0, id1):
+    """The reference's own shader source compiled as C++ (oracle/_ref)."""
+    r = ref_lib()
+    if r is None:
+        return None
+    o, R = _outputs(id1 - id0)
+    R.position = None
+    rc = r.wtref_vertex(C.byref(U), id0, id1, C.byref(R))
+    if rc != 0:
+        raise ValueError("uniforms not expressible by the reference shader")
+    del o["position"]
+    return o
+
+
+def grid_indices(cols, rows, base=0):
+    out = np.zeros(6 * (cols - 1) * (rows - 1), np.uint32)
+    lib().wto_grid_indices(cols, rows, base, _ptr(out))
+    return out
+
+
+def noise_f64(terms, width, height):
+    out = np.zeros((height, width))
+    t = np.ascontiguousarray(terms)
+    lib().wto_noise_f64(_ptr(t), len(t), width, height, _ptr(out))
+    return out
+
+
+def wave_to_reference(wave):
+    r = RefWave()
+    w = np.array(wave).copy()
+    lib().wto_wave_to_reference(_ptr(w), C.byref(r))
+    return (r.amplitude_A, r.frequency_w, r.phaseConstant_phi, r.steepness_Q_i, r.dir_x, r.dir_z)
+
+
+def cpu_baseline(patches, waves, texels=None, hm_params=None, row_limit=1 << 30, threads=None,
+                 analytic=False):
+    """Runs the timed CPU restatement; returns (vertices, pos4, nrm4)."""
+    threads = threads or os.cpu_count() or 1
+    n_out = int(max(int(p["out_offset"]) + int(p["cols"]) * int(p["rows"]) for p in patches))
+    pos = np.zeros((n_out, 4), np.float32)
+    nrm = np.zeros((n_out, 4), np.float32)
+    hm = make_hm(texels, hm_params.sample_scale, hm_params.disp_scale, hm_params.wrap) if texels is not None else None
+    f = lib().wto_cpu_analytic if analytic else lib().wto_cpu_reference
+    pp = np.ascontiguousarray(patches)
+    nv = f(_ptr(pp), len(pp), _ptr(waves), C.byref(hm) if hm else None, row_limit, threads,
+           _ptr(pos), _ptr(nrm))
+    return int(nv), pos, nrm

@@ -1,0 +1,145 @@
+/*
+ * wt_oracle.h — CPU oracle of the Gerstner water-surface path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker that the CUDA path is
+ * compared against; it is never linked into, called by, or used as a fallback
+ * for the library under wave-tool_gb300/.  Only tests/, the smoke check and
+ * the CPU-baseline leg of bench.py load it.
+ *
+ * Two restatements of assets/shaders/water-grid.vert (the reference runs this
+ * path only as a GLSL vertex shader; it has no CPU implementation):
+ *
+ *  1. FP64 truth (gerstner_f64.c): the same wave sum in double precision, the
+ *     exact normal of the displaced surface, FP64 bilinear sampling of the
+ *     stored texels.  The CUDA kernels are held to it.
+ *  2. FP32 reference mode (reference_mode.c): a line-by-line FP32 restatement
+ *     of water-grid.vert:74-194 (five surface evaluations per vertex,
+ *     central-difference normals, camera-facing flip), pinned bit-exactly
+ *     against the reference shader source itself compiled as C++ (oracle/_ref,
+ *     built by oracle/build_ref.py) and against tests/golden fixtures.
+ *
+ * Plus the index buffer (src/program.cpp:686-717), the noise heightmap and a
+ * hand-derived FP64 adjoint.
+ */
+#ifndef WT_ORACLE_H
+#define WT_ORACLE_H
+
+#include <stdint.h>
+#include "../include/wt.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Heightmap as the oracle sees it: host texels, R channel in [0, 1]. */
+typedef struct wto_heightmap {
+    const float* texels;
+    uint32_t width, height;
+    float sample_scale, disp_scale;
+    uint32_t wrap;
+    uint32_t _pad;
+} wto_heightmap;
+
+/* ---- FP64 truth ---------------------------------------------------------- */
+
+/* Rows [row0, row1) of one patch.  Any output pointer may be NULL.  Arrays are
+ * indexed by the vertex's position inside the patch (row*cols + col):
+ *   pos  : 3 doubles, displaced world position (incl. heightmap + y_offset)
+ *   disp : 3 doubles, pos - undisplaced grid position (summed directly)
+ *   nrm  : 3 doubles, unit normal normalize(dP/dz x dP/dx)
+ *   edge : 1 double, distance (in texels) of the heightmap sample point from
+ *          the nearest texel-cell boundary (+inf without a heightmap); the
+ *          bilinear gradient jumps across those boundaries. */
+void wto_displace_f64(const wt_patch* p, const wt_wave* waves, const wto_heightmap* hm,
+                      uint32_t row0, uint32_t row1,
+                      double* pos, double* disp, double* nrm, double* edge);
+
+/* Undisplaced grid position (x, z) of vertex (row, col), water-grid.vert:87-91
+ * and :123-125 in FP64. */
+void wto_grid_xz_f64(const wt_patch* p, uint32_t row, uint32_t col, double* x, double* z);
+
+/* ---- FP64 adjoint -------------------------------------------------------- */
+
+/* Gradient of  L = sum_v <gpos_v, pos_v> + <gnrm_v, nrm_v>  with respect to the
+ * waves of one patch, accumulated (+=) into grad (8 doubles per wave, the
+ * wt_wave_grad field order) for waves [p->wave_offset, +wave_count).
+ * gpos: 4 floats per vertex (w ignored); gnrm: 4 floats per vertex or NULL.
+ * Indexed like the outputs (p->out_offset + row*cols + col). */
+void wto_adjoint_f64(const wt_patch* p, const wt_wave* waves, const wto_heightmap* hm,
+                     const float* gpos, const float* gnrm, double* grad);
+
+/* ---- FP32 reference mode ------------------------------------------------- */
+
+/* The shader's own uniform set (water-grid.vert:37-64). */
+typedef struct wto_ref_wave {
+    float amplitude_A, frequency_w, phaseConstant_phi, steepness_Q_i, dir_x, dir_z;
+} wto_ref_wave;
+
+typedef struct wto_ref_uniforms {
+    float bottom_left[4], bottom_right[4], top_left[4], top_right[4];
+    float camera_position[3];
+    uint32_t grid_length;
+    uint32_t wave_count;          /* <= number of entries in `waves` */
+    const wto_ref_wave* waves;
+    const float* phase_offset;    /* NULL, or one constant phase per wave (an
+                                     extension; NULL reproduces the shader) */
+    wto_heightmap hm;             /* hm.texels NULL: texture reads return 0 */
+    float vertical_bounce;
+    float time_s;
+    float view_only_yaw[16];      /* column-major, as glUniformMatrix4fv(GL_FALSE) */
+    float view_projection[16];
+} wto_ref_uniforms;
+
+/* Per-vertex outputs of water-grid.vert, any may be NULL:
+ *   position (4): world position after displacement (the `position` local)
+ *   clip (4): gl_Position;  ndc0 (2): xyPositionNDCSpaceHeight0
+ *   view (3): viewVecRaw;   normal (3): `normal` after the camera flip
+ *   normal_yaw (3): normalVecInViewSpaceOnlyYaw;  colour (4): heightmap_colour */
+typedef struct wto_ref_outputs {
+    float* position;
+    float* clip;
+    float* ndc0;
+    float* view;
+    float* normal;
+    float* normal_yaw;
+    float* colour;
+} wto_ref_outputs;
+
+/* Runs the vertex stage for gl_VertexID in [id0, id1); outputs of vertex id
+ * are written at index id - id0. */
+void wto_reference_vertex(const wto_ref_uniforms* u, uint32_t id0, uint32_t id1,
+                          const wto_ref_outputs* out);
+
+/* ---- CPU baseline (timed, multi-threaded) -------------------------------- */
+
+/* Runs the FP32 reference-mode vertex stage (5 surface evaluations per vertex,
+ * finite-difference normals) over rows [row0, row1) of every patch, with
+ * `threads` POSIX threads, writing float4 positions and normals at the
+ * patches' out_offset.  Returns the number of vertices processed. */
+uint64_t wto_cpu_reference(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
+                           const wto_heightmap* hm, uint32_t row_limit, int threads,
+                           float* pos4, float* nrm4);
+
+/* Same vertices, one FP32 surface evaluation per vertex with analytic normals. */
+uint64_t wto_cpu_analytic(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
+                          const wto_heightmap* hm, uint32_t row_limit, int threads,
+                          float* pos4, float* nrm4);
+
+/* Maps one wt_wave of a patch to the shader's uniforms: frequency_w =
+ * 2*pi/lambda, phaseConstant_phi = speed * frequency_w (FP32). */
+void wto_wave_to_reference(const wt_wave* w, wto_ref_wave* out);
+
+/* ---- index buffer, noise ------------------------------------------------- */
+
+/* src/program.cpp:686-717 generalised to cols x rows and a base vertex. */
+void wto_grid_indices(uint32_t cols, uint32_t rows, uint32_t base_vertex, uint32_t* out);
+
+/* FP64 noise heightmap normalised to [0, 1]. */
+void wto_noise_f64(const wt_noise_term* terms, uint32_t n_terms, uint32_t width,
+                   uint32_t height, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

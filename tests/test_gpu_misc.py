@@ -1,0 +1,109 @@
+"""GPU parity of the index buffer and the noise heightmap; device-side and
+host-side validation through the C ABI."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("cols,rows,base", [(513, 513, 0), (2, 2, 0), (3, 3, 7), (65, 17, 100), (1025, 3, 0),
+                                            (2048, 2048, 0)])
+def test_grid_indices_bit_exact(wt, oracle, gpu, cols, rows, base):
+    """src/program.cpp:686-717 (L = 513 there) bit for bit."""
+    got = wt.grid_indices(cols, rows, base).cpu().numpy().view(np.uint32)
+    assert np.array_equal(got, oracle.grid_indices(cols, rows, base))
+
+
+def test_grid_indices_large_grid_on_device(wt, gpu):
+    """A 4097^2 grid (100 M indices) checked against the closed form on the
+    device (too large for the CPU loop)."""
+    import torch
+    L = 4097
+    idx = wt.grid_indices(L, L).view(-1, 6).to(torch.int64)
+    r = torch.arange(L - 1, device="cuda").repeat_interleave(L - 1)
+    c = torch.arange(L - 1, device="cuda").repeat(L - 1)
+    base = r * L + c
+    exp = torch.stack([base, base + L + 1, base + L, base, base + 1, base + L + 1], 1)
+    assert torch.equal(idx, exp)
+
+
+def test_noise_matches_f64(wt, oracle, gpu):
+    from wave_tool_gb300 import workloads
+    for (w, h, n, k, seed) in ((512, 512, 64, 32, 1), (37, 21, 9, 5, 2), (1, 1, 3, 2, 3)):
+        terms = workloads.noise_terms(workloads.SplitMix64(seed), n=n, kmax=k)
+        got = wt.noise_synth(terms, w, h).cpu().numpy()
+        exp = oracle.noise_f64(terms, w, h)
+        if w * h > 1:
+            assert np.abs(got - exp).max() < 2e-5
+            assert got.min() == 0.0 and got.max() == 1.0
+
+
+def test_device_side_validation(wt, gpu):
+    """Invalid patches are skipped and reported with the first bad index."""
+    import torch
+    from wave_tool_gb300 import workloads
+    w = workloads.small_random(1, n_patches=4)
+    good = wt.Surface(w.patches, w.waves)
+    ref, _ = good.displace()
+    bad = w.patches.copy()
+    bad[2]["cols"] = 1                      # grid too small
+    bad[3]["wave_offset"] = len(w.waves)    # waves out of range
+    s = wt.Surface(bad, w.waves)
+    pos, nrm = s.alloc_outputs()
+    pos.fill_(-7.0)
+    s.displace(pos, nrm)
+    st, first = s.status()
+    assert st == wt.abi.WT_ERR_INVALID_ARG and first == 2
+    o0, n0 = int(bad[0]["out_offset"]), int(bad[0]["cols"] * bad[0]["rows"])
+    assert torch.equal(pos[o0:o0 + n0], ref[o0:o0 + n0])   # valid patches still ran
+    o2 = int(bad[2]["out_offset"])
+    assert float(pos[o2, 0]) == -7.0                        # invalid ones were not written
+    # NaN wave parameter
+    k = int(np.argmax(w.patches["wave_count"] > 0))
+    wv = w.waves.copy()
+    wv[int(w.patches[k]["wave_offset"])]["wavelength"] = np.nan
+    s2 = wt.Surface(w.patches, wv)
+    s2.displace()
+    st, first = s2.status()
+    assert st == wt.abi.WT_ERR_INVALID_ARG and first == k
+    # output capacity too small for the last patch
+    s3 = wt.Surface(w.patches, w.waves)
+    p3, n3 = s3.alloc_outputs()
+    s3.displace(p3[:-1], n3[:-1])
+    st, first = s3.status()
+    assert st == wt.abi.WT_ERR_INVALID_ARG and first == 3
+
+
+def test_workspace_too_small_for_wave_slots(wt, gpu):
+    import ctypes as C
+    from wave_tool_gb300 import workloads
+    w = workloads.small_random(2, n_patches=3, n_waves_range=(10, 20))
+    s = wt.Surface(w.patches, w.waves)
+    small = wt.empty_bytes(wt.displace_workspace_bytes(3, 1))
+    pos, nrm = s.alloc_outputs()
+    wt.check(wt.lib().wt_gerstner_displace(s.patches.data_ptr(), 3, s.waves.data_ptr(), len(w.waves), None,
+                                           pos.data_ptr(), nrm.data_ptr(), pos.shape[0], 0, small.data_ptr(),
+                                           small.numel(), wt.stream_handle()))
+    st, _ = wt.workspace_status(small)
+    assert st == wt.abi.WT_ERR_NOMEM
+    del C
+
+
+def test_host_side_validation(wt, gpu):
+    from wave_tool_gb300 import workloads
+    w = workloads.small_random(4, n_patches=2)
+    s = wt.Surface(w.patches, w.waves)
+    pos, nrm = s.alloc_outputs()
+    L = wt.lib()
+    ws = s.workspace
+    args = [s.patches.data_ptr(), 2, s.waves.data_ptr(), len(w.waves), None, pos.data_ptr(), nrm.data_ptr(),
+            pos.shape[0], 0, ws.data_ptr(), ws.numel(), wt.stream_handle()]
+    assert L.wt_gerstner_displace(*args) == 0
+    for i, v, code in ((0, None, 1), (5, pos.data_ptr() + 4, 1), (8, 0x100, 1), (10, 64, 4), (9, ws.data_ptr() + 16, 1),
+                       (7, 0, 1)):
+        a = list(args)
+        a[i] = v
+        assert L.wt_gerstner_displace(*a) == code, (i, v)
+        assert L.wt_last_error()

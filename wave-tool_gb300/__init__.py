@@ -1,0 +1,270 @@
+"""wave-tool GB300: the water-surface hot path of wave-tool as sm_103a CUDA
+behind a C ABI (include/wt.h), with this thin Python host layer on top.
+
+The reference computes this path in its GLSL vertex shader
+(assets/shaders/water-grid.vert:74-194) fed by RenderEngine::render
+(src/render-engine.cpp:1045-1115).  Here the same work is one persistent
+CUDA launch over many patches, called through ctypes on the in-tree
+``_build/libwt_gb300.so``.  PyTorch is used only for device memory and
+streams.  There is no CPU fallback: without the CUDA library every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from pathlib import Path
+
+import numpy as np
+
+from . import abi
+from .abi import (NOISE_TERM_DTYPE, PATCH_DTYPE, WAVE_DTYPE, WAVE_GRAD_DTYPE, WT_LAYOUT_FLOAT4,
+                  WT_LAYOUT_VEC3, WT_OUT_DISPLACEMENT, WT_OUT_WORLD, WT_PHASE_FP32_NAIVE, WT_PHASE_FP64,
+                  WT_WRAP_MIRRORED_REPEAT, WT_WRAP_REPEAT)
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libwt_gb300.so"
+
+# every symbol include/wt.h declares
+EXPORTED = [
+    "wt_version", "wt_last_error", "wt_displace_workspace_size", "wt_adjoint_workspace_size",
+    "wt_workspace_status", "wt_gerstner_displace", "wt_gerstner_displace_unbatched",
+    "wt_gerstner_adjoint", "wt_grid_indices", "wt_noise_synth", "wt_wave_from_reference",
+    "wt_measure_peaks",
+]
+
+
+class WtError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class CHeightmap(C.Structure):
+    _fields_ = [("texels", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("sample_scale", C.c_float), ("disp_scale", C.c_float), ("wrap", C.c_uint32),
+                ("_pad", C.c_uint32)]
+
+
+class CWave(C.Structure):
+    _fields_ = [(n, C.c_float) for n in WAVE_DTYPE.names]
+
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    from .build import build as _b
+    return _b(force=force)
+
+
+def lib():
+    """The CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"CUDA library {LIB_PATH} is missing: run build() first "
+                               "(there is no CPU fallback)")
+        L = C.CDLL(str(LIB_PATH))
+        vp, u32, u64, sz = C.c_void_p, C.c_uint32, C.c_uint64, C.c_size_t
+        L.wt_version.restype = C.c_char_p
+        L.wt_last_error.restype = C.c_char_p
+        L.wt_displace_workspace_size.argtypes = [u32, u64, C.POINTER(sz)]
+        L.wt_adjoint_workspace_size.argtypes = [vp, u32, C.POINTER(sz)]
+        L.wt_workspace_status.argtypes = [vp, vp, C.POINTER(u32)]
+        L.wt_gerstner_displace.argtypes = [vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, u64, u32, vp, sz, vp]
+        L.wt_gerstner_displace_unbatched.argtypes = [vp, vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, u64,
+                                                     u32, vp, sz, vp]
+        L.wt_gerstner_adjoint.argtypes = [vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, u64, u32, vp, vp,
+                                          sz, vp]
+        L.wt_grid_indices.argtypes = [u32, u32, u32, vp, vp]
+        L.wt_noise_synth.argtypes = [vp, u32, u32, u32, vp, vp, sz, vp]
+        L.wt_wave_from_reference.argtypes = [C.c_float] * 6 + [u32, C.POINTER(CWave)]
+        L.wt_measure_peaks.argtypes = [vp, sz, C.POINTER(C.c_double), C.POINTER(C.c_double), vp]
+        for name in EXPORTED:
+            if name not in ("wt_version", "wt_last_error"):
+                getattr(L, name).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def version() -> str:
+    return lib().wt_version().decode()
+
+
+def check(status: int) -> None:
+    if status != abi.WT_OK:
+        raise WtError(status, lib().wt_last_error().decode())
+
+
+# ---- torch plumbing ----------------------------------------------------------
+
+def _torch():
+    import torch
+    return torch
+
+
+def stream_handle(stream=None) -> int:
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def to_device(arr: np.ndarray, device="cuda"):
+    """Copy a (structured) numpy array to a device byte tensor."""
+    torch = _torch()
+    a = np.ascontiguousarray(arr)
+    return torch.from_numpy(a.view(np.uint8).reshape(-1).copy()).to(device)
+
+
+def empty_bytes(n: int, device="cuda"):
+    torch = _torch()
+    # 256-byte aligned by the caching allocator
+    return torch.empty(max(int(n), 1), dtype=torch.uint8, device=device)
+
+
+def _ptr(t) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+class DeviceHeightmap:
+    """A heightmap layer with texels in device memory (texels[j, i], j = t row)."""
+
+    def __init__(self, texels, sample_scale: float, disp_scale: float, wrap: int = WT_WRAP_REPEAT):
+        assert texels.is_cuda and texels.dtype == _torch().float32 and texels.dim() == 2
+        self.texels = texels.contiguous()
+        self.sample_scale = float(sample_scale)
+        self.disp_scale = float(disp_scale)
+        self.wrap = int(wrap)
+
+    def cstruct(self) -> CHeightmap:
+        h, w = self.texels.shape
+        return CHeightmap(self.texels.data_ptr(), w, h, self.sample_scale, self.disp_scale, self.wrap, 0)
+
+
+def displace_workspace_bytes(n_patches: int, total_wave_slots: int) -> int:
+    out = C.c_size_t()
+    check(lib().wt_displace_workspace_size(n_patches, total_wave_slots, C.byref(out)))
+    return out.value
+
+
+def adjoint_workspace_bytes(host_patches: np.ndarray) -> int:
+    out = C.c_size_t()
+    hp = np.ascontiguousarray(host_patches)
+    check(lib().wt_adjoint_workspace_size(hp.ctypes.data, len(hp), C.byref(out)))
+    return out.value
+
+
+def workspace_status(ws, stream=None) -> tuple[int, int]:
+    bad = C.c_uint32()
+    st = lib().wt_workspace_status(ws.data_ptr(), stream_handle(stream), C.byref(bad))
+    return st, bad.value
+
+
+class Surface:
+    """Device-resident patch table, waves and heightmap for the C ABI.
+
+    Mirrors the reference's per-frame inputs: `waves` are the GerstnerWave
+    uniforms (render-engine.cpp:1067-1081), `patches` the projected-grid
+    corners + gridLength + time (:1045-1108), `heightmap` the noise texture
+    (program.cpp:719, water-grid.vert:93-111)."""
+
+    def __init__(self, patches: np.ndarray, waves: np.ndarray, heightmap: DeviceHeightmap | None = None,
+                 device="cuda"):
+        assert patches.dtype == PATCH_DTYPE and waves.dtype == WAVE_DTYPE
+        self.host_patches = np.ascontiguousarray(patches)
+        self.host_waves = np.ascontiguousarray(waves)
+        self.patches = to_device(self.host_patches, device)
+        self.waves = to_device(self.host_waves, device)
+        self.heightmap = heightmap
+        self.n_patches = len(patches)
+        self.n_waves = len(waves)
+        self.n_vertices = int(max((int(p["out_offset"]) + int(p["cols"]) * int(p["rows"]) for p in patches),
+                                  default=0))
+        self.wave_slots = int(np.sum(patches["wave_count"].astype(np.uint64)))
+        self.workspace = empty_bytes(displace_workspace_bytes(self.n_patches, self.wave_slots), device)
+
+    def alloc_outputs(self, flags: int = 0, normals: bool = True):
+        torch = _torch()
+        w = 3 if flags & WT_LAYOUT_VEC3 else 4
+        pos = torch.empty((self.n_vertices, w), dtype=torch.float32, device=self.patches.device)
+        nrm = torch.empty_like(pos) if normals else None
+        return pos, nrm
+
+    def displace(self, pos=None, nrm=None, flags: int = 0, normals: bool = True, stream=None, unbatched=False):
+        if pos is None:
+            pos, nrm = self.alloc_outputs(flags, normals)
+        hm = self.heightmap.cstruct() if self.heightmap is not None else None
+        hmp = C.byref(hm) if hm is not None else None
+        cap = pos.shape[0]
+        if unbatched:
+            check(lib().wt_gerstner_displace_unbatched(
+                self.host_patches.ctypes.data, self.patches.data_ptr(), self.n_patches, self.waves.data_ptr(),
+                self.n_waves, hmp, pos.data_ptr(), _ptr(nrm), cap, flags, self.workspace.data_ptr(),
+                self.workspace.numel(), stream_handle(stream)))
+        else:
+            check(lib().wt_gerstner_displace(
+                self.patches.data_ptr(), self.n_patches, self.waves.data_ptr(), self.n_waves, hmp,
+                pos.data_ptr(), _ptr(nrm), cap, flags, self.workspace.data_ptr(), self.workspace.numel(),
+                stream_handle(stream)))
+        return pos, nrm
+
+    def status(self, stream=None):
+        return workspace_status(self.workspace, stream)
+
+
+def grid_indices(cols: int, rows: int, base_vertex: int = 0, stream=None):
+    torch = _torch()
+    out = torch.empty(6 * (cols - 1) * (rows - 1), dtype=torch.int32, device="cuda")
+    check(lib().wt_grid_indices(cols, rows, base_vertex, out.data_ptr(), stream_handle(stream)))
+    return out
+
+
+def noise_synth(terms: np.ndarray, width: int, height: int, stream=None):
+    torch = _torch()
+    assert terms.dtype == NOISE_TERM_DTYPE
+    t = to_device(terms)
+    out = torch.empty((height, width), dtype=torch.float32, device="cuda")
+    ws = empty_bytes(256)
+    check(lib().wt_noise_synth(t.data_ptr(), len(terms), width, height, out.data_ptr(), ws.data_ptr(),
+                               ws.numel(), stream_handle(stream)))
+    return out
+
+
+def wave_from_reference(amplitude_A, frequency_w, phase_constant_phi, steepness_Q, dir_x, dir_z,
+                        wave_count) -> np.ndarray:
+    w = CWave()
+    check(lib().wt_wave_from_reference(amplitude_A, frequency_w, phase_constant_phi, steepness_Q, dir_x, dir_z,
+                                       wave_count, C.byref(w)))
+    out = np.zeros(1, WAVE_DTYPE)
+    for n in WAVE_DTYPE.names:
+        out[n] = getattr(w, n)
+    return out
+
+
+def measure_peaks(stream=None) -> tuple[float, float]:
+    scratch = empty_bytes(4 << 20)
+    f, s = C.c_double(), C.c_double()
+    check(lib().wt_measure_peaks(scratch.data_ptr(), scratch.numel(), C.byref(f), C.byref(s),
+                                 stream_handle(stream)))
+    return f.value, s.value
+
+
+def heightmap_from(workload_hm, texels=None) -> DeviceHeightmap | None:
+    """Device heightmap of a workloads.Heightmap: synthesised on the GPU
+    unless texels are given."""
+    if workload_hm is None:
+        return None
+    if texels is None:
+        texels = noise_synth(workload_hm.terms, workload_hm.width, workload_hm.height)
+    return DeviceHeightmap(texels, workload_hm.sample_scale, workload_hm.disp_scale, workload_hm.wrap)
+
+
+__all__ = [
+    "abi", "build", "lib", "version", "check", "WtError", "Surface", "DeviceHeightmap", "grid_indices",
+    "noise_synth", "wave_from_reference", "measure_peaks", "displace_workspace_bytes",
+    "adjoint_workspace_bytes", "workspace_status", "heightmap_from", "PATCH_DTYPE", "WAVE_DTYPE",
+    "NOISE_TERM_DTYPE", "WAVE_GRAD_DTYPE", "WT_OUT_WORLD", "WT_OUT_DISPLACEMENT", "WT_LAYOUT_FLOAT4",
+    "WT_LAYOUT_VEC3", "WT_PHASE_FP64", "WT_PHASE_FP32_NAIVE", "WT_WRAP_REPEAT", "WT_WRAP_MIRRORED_REPEAT",
+    "EXPORTED", "math",
+]

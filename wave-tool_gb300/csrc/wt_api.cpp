@@ -1,0 +1,259 @@
+// wt_api.cpp — the C ABI of include/wt.h: argument validation, workspace
+// layout, launch orchestration, error reporting.
+//
+// Replaces the host side of the reference's water pass
+// (src/render-engine.cpp:1045-1115: uniform upload + glDrawElements) with
+// device-buffer launches; the per-frame host work of the reference (corner
+// projection, :797-1042) stays with the caller.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "wt_internal.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+wt_status fail(wt_status s, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+wt_status fail(wt_status s, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return s;
+}
+
+wt_status cuda_fail(cudaError_t e, const char* what) {
+    return fail(WT_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+
+// Forward launch tuning, chosen by the autotuner or the defaults.
+std::mutex g_tune_mu;
+wt::FwdConfig g_fwd_cfg = {8, 32, 8, 0};
+
+constexpr uint32_t kKnownFlags = WT_OUT_DISPLACEMENT | WT_LAYOUT_VEC3 | WT_PHASE_FP32_NAIVE;
+constexpr uint32_t kMaxPatches = 1u << 24;
+
+wt_status check_hm(const wt_heightmap* hm, wt::HmDev* out) {
+    std::memset(out, 0, sizeof(*out));
+    if (!hm) return WT_OK;
+    if (!hm->texels) return fail(WT_ERR_INVALID_ARG, "heightmap: texels is NULL");
+    if (!aligned(hm->texels, 4)) return fail(WT_ERR_INVALID_ARG, "heightmap: texels not 4-byte aligned");
+    if (hm->width < 1 || hm->height < 1 || hm->width > 32768 || hm->height > 32768)
+        return fail(WT_ERR_INVALID_ARG, "heightmap: size %ux%u outside [1, 32768]", hm->width, hm->height);
+    if (!std::isfinite(hm->sample_scale) || hm->sample_scale < 0.0f)
+        return fail(WT_ERR_INVALID_ARG, "heightmap: sample_scale must be finite and >= 0");
+    if (!std::isfinite(hm->disp_scale)) return fail(WT_ERR_INVALID_ARG, "heightmap: disp_scale not finite");
+    if (hm->wrap != WT_WRAP_REPEAT && hm->wrap != WT_WRAP_MIRRORED_REPEAT)
+        return fail(WT_ERR_INVALID_ARG, "heightmap: unknown wrap mode %u", hm->wrap);
+    if (hm->_pad != 0) return fail(WT_ERR_INVALID_ARG, "heightmap: _pad must be 0");
+    out->texels = hm->texels;
+    out->width = hm->width;
+    out->height = hm->height;
+    out->sample_scale = hm->sample_scale;
+    out->disp_scale = hm->disp_scale;
+    out->wrap = hm->wrap;
+    out->present = 1;
+    return WT_OK;
+}
+
+struct Prepared {
+    wt::HmDev hm;
+    wt::WsLayout L;
+};
+
+// Shared validation of the displace / adjoint entry points.
+wt_status check_common(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
+                       const wt_heightmap* hm, uint64_t out_capacity, uint32_t flags, void* ws,
+                       size_t ws_bytes, Prepared* P) {
+    if (n_patches > kMaxPatches) return fail(WT_ERR_INVALID_ARG, "n_patches %u > %u", n_patches, kMaxPatches);
+    if (!patches) return fail(WT_ERR_INVALID_ARG, "patches is NULL");
+    if (!aligned(patches, 8)) return fail(WT_ERR_INVALID_ARG, "patches not 8-byte aligned");
+    if (n_waves > 0 && !waves) return fail(WT_ERR_INVALID_ARG, "waves is NULL");
+    if (waves && !aligned(waves, 4)) return fail(WT_ERR_INVALID_ARG, "waves not 4-byte aligned");
+    if (flags & ~kKnownFlags) return fail(WT_ERR_INVALID_ARG, "unknown flags 0x%x", flags & ~kKnownFlags);
+    if (out_capacity == 0) return fail(WT_ERR_INVALID_ARG, "out_capacity is 0");
+    if (!ws) return fail(WT_ERR_INVALID_ARG, "workspace is NULL");
+    if (!aligned(ws, 256)) return fail(WT_ERR_INVALID_ARG, "workspace not 256-byte aligned");
+    wt_status st = check_hm(hm, &P->hm);
+    if (st != WT_OK) return st;
+    wt::WsLayout L0 = wt::ws_layout(n_patches, 0);
+    if (ws_bytes < L0.end)
+        return fail(WT_ERR_NOMEM, "workspace %zu bytes < %zu needed for %u patches", ws_bytes, L0.end, n_patches);
+    // every byte past the fixed part holds per-(patch, wave) constants; the
+    // device refuses to run when the patches need more than fit
+    uint64_t cap = (ws_bytes - L0.coef) / sizeof(wt::PairCoef);
+    P->L = wt::ws_layout(n_patches, cap);
+    while (P->L.end > ws_bytes && cap > 0) P->L = wt::ws_layout(n_patches, --cap);
+    return WT_OK;
+}
+
+wt_status check_outputs(const float* pos, const float* nrm, uint32_t flags) {
+    size_t a = (flags & WT_LAYOUT_VEC3) ? 4 : 16;
+    if (!pos) return fail(WT_ERR_INVALID_ARG, "pos_out is NULL");
+    if (!aligned(pos, a)) return fail(WT_ERR_INVALID_ARG, "pos_out not %zu-byte aligned", a);
+    if (nrm && !aligned(nrm, a)) return fail(WT_ERR_INVALID_ARG, "nrm_out not %zu-byte aligned", a);
+    return WT_OK;
+}
+
+wt::FwdConfig current_cfg() {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    return g_fwd_cfg;
+}
+
+wt_status run_displace(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
+                       const wt_heightmap* hm, float* pos, float* nrm, uint64_t cap, uint32_t flags, void* ws,
+                       size_t ws_bytes, cudaStream_t s, const wt::FwdConfig& cfg) {
+    Prepared P;
+    wt_status st = check_common(patches, n_patches, waves, n_waves, hm, cap, flags, ws, ws_bytes, &P);
+    if (st != WT_OK) return st;
+    st = check_outputs(pos, nrm, flags);
+    if (st != WT_OK) return st;
+    if (n_patches == 0) return WT_OK;
+    cudaError_t e = wt::launch_prep(patches, n_patches, waves, n_waves, P.hm, cap, 32u * cfg.s, ws, P.L, s);
+    if (e != cudaSuccess) return cuda_fail(e, "prep launch");
+    if (flags & WT_PHASE_FP32_NAIVE)
+        e = wt::launch_forward_naive(patches, n_patches, waves, P.hm, pos, nrm, flags, ws, P.L, cap, s);
+    else
+        e = wt::launch_forward(cfg, patches, n_patches, P.hm, pos, nrm, flags, ws, P.L, s);
+    if (e != cudaSuccess) return cuda_fail(e, "forward launch");
+    return WT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* wt_version(void) { return "wave-tool-gb300 0.1 (sm_103a)"; }
+
+const char* wt_last_error(void) { return g_last_error.c_str(); }
+
+wt_status wt_displace_workspace_size(uint32_t n_patches, uint64_t total_wave_slots, size_t* bytes) {
+    if (!bytes) return fail(WT_ERR_INVALID_ARG, "bytes is NULL");
+    if (n_patches > kMaxPatches) return fail(WT_ERR_INVALID_ARG, "n_patches %u > %u", n_patches, kMaxPatches);
+    if (total_wave_slots > 0xffffffffull) return fail(WT_ERR_INVALID_ARG, "total_wave_slots exceeds 2^32-1");
+    *bytes = wt::ws_layout(n_patches, total_wave_slots).end;
+    return WT_OK;
+}
+
+wt_status wt_adjoint_workspace_size(const wt_patch* host_patches, uint32_t n_patches, size_t* bytes) {
+    if (!bytes) return fail(WT_ERR_INVALID_ARG, "bytes is NULL");
+    if (n_patches > 0 && !host_patches) return fail(WT_ERR_INVALID_ARG, "host_patches is NULL");
+    return fail(WT_ERR_UNSUPPORTED, "adjoint not built yet");
+}
+
+wt_status wt_workspace_status(const void* workspace, wt_stream stream, uint32_t* bad_patch) {
+    if (!workspace) return fail(WT_ERR_INVALID_ARG, "workspace is NULL");
+    uint32_t h[2] = {0, 0};
+    cudaError_t e = cudaMemcpyAsync(h, workspace, sizeof(h), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "reading workspace status");
+    if (bad_patch) *bad_patch = h[1];
+    if (h[0] == WT_OK) return WT_OK;
+    if (h[0] == WT_ERR_NOMEM) return fail(WT_ERR_NOMEM, "workspace too small for the patches' wave slots");
+    return fail((wt_status)h[0], "device-side validation failed at patch %u", h[1]);
+}
+
+wt_status wt_gerstner_displace(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
+                               uint32_t n_waves, const wt_heightmap* hm, float* pos_out, float* nrm_out,
+                               uint64_t out_capacity, uint32_t flags, void* workspace, size_t workspace_bytes,
+                               wt_stream stream) {
+    return run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags,
+                        workspace, workspace_bytes, (cudaStream_t)stream, current_cfg());
+}
+
+wt_status wt_gerstner_displace_unbatched(const wt_patch* host_patches, const wt_patch* patches,
+                                         uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
+                                         const wt_heightmap* hm, float* pos_out, float* nrm_out,
+                                         uint64_t out_capacity, uint32_t flags, void* workspace,
+                                         size_t workspace_bytes, wt_stream stream) {
+    if (n_patches > 0 && !host_patches) return fail(WT_ERR_INVALID_ARG, "host_patches is NULL");
+    wt::FwdConfig cfg = current_cfg();
+    for (uint32_t i = 0; i < n_patches; ++i) {
+        wt_status st = run_displace(patches + i, 1, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags,
+                                    workspace, workspace_bytes, (cudaStream_t)stream, cfg);
+        if (st != WT_OK) return st;
+    }
+    return WT_OK;
+}
+
+wt_status wt_gerstner_adjoint(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
+                              uint32_t n_waves, const wt_heightmap* hm, const float* d_pos, const float* d_nrm,
+                              uint64_t out_capacity, uint32_t flags, wt_wave_grad* grad_out, void* workspace,
+                              size_t workspace_bytes, wt_stream stream) {
+    (void)patches; (void)n_patches; (void)waves; (void)n_waves; (void)hm; (void)d_pos; (void)d_nrm;
+    (void)out_capacity; (void)flags; (void)grad_out; (void)workspace; (void)workspace_bytes; (void)stream;
+    return fail(WT_ERR_UNSUPPORTED, "adjoint not built yet");
+}
+
+wt_status wt_grid_indices(uint32_t cols, uint32_t rows, uint32_t base_vertex, uint32_t* idx_out, wt_stream stream) {
+    if (cols < 2 || rows < 2) return fail(WT_ERR_INVALID_ARG, "grid %ux%u: need at least 2x2", cols, rows);
+    if (!idx_out) return fail(WT_ERR_INVALID_ARG, "idx_out is NULL");
+    if (!aligned(idx_out, 4)) return fail(WT_ERR_INVALID_ARG, "idx_out not 4-byte aligned");
+    if ((uint64_t)base_vertex + (uint64_t)cols * rows > 0x100000000ull)
+        return fail(WT_ERR_INVALID_ARG, "vertex indices exceed uint32");
+    cudaError_t e = wt::launch_indices(cols, rows, base_vertex, idx_out, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "index launch");
+    return WT_OK;
+}
+
+wt_status wt_noise_synth(const wt_noise_term* terms, uint32_t n_terms, uint32_t width, uint32_t height,
+                         float* texels_out, void* workspace, size_t workspace_bytes, wt_stream stream) {
+    if (width < 1 || height < 1 || width > 32768 || height > 32768)
+        return fail(WT_ERR_INVALID_ARG, "noise size %ux%u outside [1, 32768]", width, height);
+    if (n_terms > 0 && !terms) return fail(WT_ERR_INVALID_ARG, "terms is NULL");
+    if (!texels_out || !aligned(texels_out, 4)) return fail(WT_ERR_INVALID_ARG, "texels_out NULL or misaligned");
+    if (!workspace || !aligned(workspace, 16)) return fail(WT_ERR_INVALID_ARG, "workspace NULL or misaligned");
+    if (workspace_bytes < 16) return fail(WT_ERR_NOMEM, "noise needs 16 bytes of workspace");
+    cudaError_t e = wt::launch_noise(terms, n_terms, width, height, texels_out, workspace, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "noise launch");
+    return WT_OK;
+}
+
+wt_status wt_wave_from_reference(float amplitude_A, float frequency_w, float phase_constant_phi, float steepness_Q,
+                                 float dir_x, float dir_z, uint32_t wave_count, wt_wave* out) {
+    if (!out) return fail(WT_ERR_INVALID_ARG, "out is NULL");
+    if (!(amplitude_A >= 0.0f) || !(frequency_w >= 0.0f) || !(phase_constant_phi >= 0.0f) ||
+        !(steepness_Q >= 0.0f && steepness_Q <= 1.0f) || !std::isfinite(amplitude_A) ||
+        !std::isfinite(frequency_w) || !std::isfinite(phase_constant_phi))
+        return fail(WT_ERR_INVALID_ARG, "reference wave outside the ranges asserted in GerstnerWave");
+    if (!std::isfinite(dir_x) || !std::isfinite(dir_z)) return fail(WT_ERR_INVALID_ARG, "direction not finite");
+    if (wave_count == 0) return fail(WT_ERR_INVALID_ARG, "wave_count is 0");
+    if (frequency_w == 0.0f && amplitude_A != 0.0f && phase_constant_phi != 0.0f)
+        return fail(WT_ERR_UNSUPPORTED, "w = 0 with A*phi != 0 is a uniform bob, not a travelling wave");
+    // render-engine.cpp:1073, in FP32 and the same operation order
+    volatile float wa = frequency_w * amplitude_A;
+    float q = 0.0f;
+    if (wa != 0.0f) {
+        volatile float denom = wa * (float)wave_count;
+        q = steepness_Q / denom;
+    }
+    std::memset(out, 0, sizeof(*out));
+    out->amplitude = amplitude_A;
+    out->wavelength = frequency_w > 0.0f ? (float)(6.283185307179586476925286766559 / (double)frequency_w) : INFINITY;
+    out->dir_x = dir_x;
+    out->dir_z = dir_z;
+    out->steepness_q = q;
+    out->speed = frequency_w > 0.0f ? (float)((double)phase_constant_phi / (double)frequency_w) : 0.0f;
+    out->phase = 0.0f;
+    return WT_OK;
+}
+
+wt_status wt_measure_peaks(void* scratch, size_t scratch_bytes, double* fma_per_s, double* sin_per_s,
+                           wt_stream stream) {
+    if (!scratch || !fma_per_s || !sin_per_s) return fail(WT_ERR_INVALID_ARG, "NULL argument");
+    if (scratch_bytes < (4u << 20)) return fail(WT_ERR_NOMEM, "peak probes need 4 MiB of scratch");
+    cudaError_t e = wt::measure_peaks(scratch, scratch_bytes, fma_per_s, sin_per_s, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "peak probes");
+    return WT_OK;
+}
+
+}  // extern "C"

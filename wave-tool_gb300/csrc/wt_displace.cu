@@ -1,0 +1,592 @@
+// wt_displace.cu — forward Gerstner path on sm_103a.
+//
+// Replaces the per-vertex work of assets/shaders/water-grid.vert:114-194
+// (grid bilerp :87-91, Gerstner sum :74-85, heightmap :93-111 sampled at the
+// displaced point :141-144, bounce :147, normal :164-190) and the uniform
+// upload of src/render-engine.cpp:1057-1110 (steepness already normalised by
+// the caller, :1073).
+//
+// Three launches, all stream-ordered and graph-capturable:
+//   k_prep_scan  (1 block)   validate patches, prefix sums, LPT sort of
+//                            patches by wave count, tile queue reset
+//   k_prep_coef  (grid)      FP64 per-(patch, wave) phase constants in 64-bit
+//                            fixed-point turns + FP32 sum coefficients;
+//                            per-patch local frame
+//   k_forward    (persistent) one tile = one patch row segment of 32*S
+//                            vertices per warp; lane l owns columns
+//                            c0 + l + 32 j, j < S.  Per wave: one MUFU sincos
+//                            per lane, then S-1 exact-step rotations on the
+//                            FMA pipe; 8 FMAs accumulate displacement and the
+//                            surface Jacobian.  Epilogue: heightmap bilerp +
+//                            gradient, exact normal, streaming float4 stores.
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "wt_internal.h"
+
+namespace wt {
+namespace {
+
+constexpr uint32_t kNoPatch = 0xffffffffu;
+constexpr int kSortBins = 4096;
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+constexpr float kTurnToRad = 1.4629180792671596e-09f;  // 2*pi / 2^32
+
+__device__ __forceinline__ void flag_error(WsHeader* h, uint32_t code, uint32_t patch) {
+    atomicCAS(&h->status, 0u, code);
+    atomicMin(&h->bad_patch, patch);
+}
+
+__device__ __forceinline__ bool finitef(float x) { return isfinite(x); }
+
+__device__ bool wave_ok(const wt_wave& w) {
+    bool lam_ok = (w.wavelength > 0.0f) && !isnan(w.wavelength);  // +inf allowed (k = 0)
+    return lam_ok && finitef(w.amplitude) && finitef(w.dir_x) && finitef(w.dir_z) &&
+           finitef(w.steepness_q) && finitef(w.speed) && finitef(w.phase);
+}
+
+// Block-wide exclusive scan of a u32 array in global memory, in place, in
+// chunks of blockDim.x.  Returns the total.  All threads must call.
+__device__ uint32_t block_exclusive_scan(uint32_t* a, uint32_t n) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (uint32_t base = 0; base < n; base += blockDim.x) {
+        uint32_t i = base + threadIdx.x;
+        uint32_t v = i < n ? a[i] : 0u;
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sums[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = lane < nwarps ? warp_sums[lane] : 0u;
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            warp_sums[lane] = w;  // inclusive
+        }
+        __syncthreads();
+        uint32_t excl = carry + (warp > 0 ? warp_sums[warp - 1] : 0u) + x - v;
+        if (i < n) a[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_sums[nwarps - 1];
+        __syncthreads();
+    }
+    return carry;
+}
+
+// ---- stage 1: validation, prefix sums, LPT order ---------------------------
+__global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__ patches, uint32_t n,
+                                                    const wt_wave* __restrict__ waves, uint32_t n_waves,
+                                                    uint64_t out_capacity, uint64_t coef_capacity,
+                                                    uint32_t tile_cols, char* ws, WsLayout L) {
+    WsHeader* hdr = reinterpret_cast<WsHeader*>(ws);
+    uint32_t* sorted = reinterpret_cast<uint32_t*>(ws + L.sorted);
+    uint32_t* tile_pre = reinterpret_cast<uint32_t*>(ws + L.tile_pre);
+    uint32_t* pair_off = reinterpret_cast<uint32_t*>(ws + L.pair_off);
+    uint32_t* tiles = reinterpret_cast<uint32_t*>(ws + L.tiles);
+    __shared__ uint32_t bins[kSortBins];
+
+    if (threadIdx.x == 0) {
+        hdr->status = 0;
+        hdr->bad_patch = kNoPatch;
+        hdr->tile_counter = 0;
+        hdr->n_patches = n;
+        hdr->tile_cols = tile_cols;
+    }
+    for (int i = threadIdx.x; i < kSortBins; i += blockDim.x) bins[i] = 0;
+    __syncthreads();
+
+    // validate; pair_off <- wave counts, tile_pre <- tile counts (original order)
+    for (uint32_t p = threadIdx.x; p < n; p += blockDim.x) {
+        wt_patch P = patches[p];
+        uint64_t verts = (uint64_t)P.cols * P.rows;
+        bool ok = P.cols >= 2 && P.rows >= 2 && P.cols <= (1u << 20) && P.rows <= (1u << 20) &&
+                  verts < (1ull << 31) && P.flags == 0 &&
+                  (uint64_t)P.wave_offset + P.wave_count <= n_waves &&
+                  P.out_offset <= out_capacity && verts <= out_capacity - P.out_offset &&
+                  finitef(P.bl[0]) && finitef(P.bl[1]) && finitef(P.br[0]) && finitef(P.br[1]) &&
+                  finitef(P.tl[0]) && finitef(P.tl[1]) && finitef(P.tr[0]) && finitef(P.tr[1]) &&
+                  isfinite(P.time_s) && finitef(P.y_offset);
+        if (ok)
+            for (uint32_t j = 0; j < P.wave_count && ok; ++j) ok = wave_ok(waves[P.wave_offset + j]);
+        if (!ok) flag_error(hdr, WT_ERR_INVALID_ARG, p);
+        pair_off[p] = ok ? P.wave_count : 0u;
+        tiles[p] = ok ? P.rows * ((P.cols + tile_cols - 1) / tile_cols) : 0u;
+        uint32_t key = P.wave_count < kSortBins ? P.wave_count : kSortBins - 1;
+        atomicAdd(&bins[kSortBins - 1 - key], 1u);  // descending wave count
+    }
+    __syncthreads();
+    uint32_t total_pairs = block_exclusive_scan(pair_off, n);
+    if (threadIdx.x == 0) pair_off[n] = total_pairs;
+    if (total_pairs > coef_capacity) {
+        // workspace too small for the wave slots: run nothing
+        if (threadIdx.x == 0) { atomicCAS(&hdr->status, 0u, (uint32_t)WT_ERR_NOMEM); hdr->total_tiles = 0; }
+        for (uint32_t p = threadIdx.x; p <= n; p += blockDim.x) tile_pre[p] = 0;
+        return;
+    }
+    // counting sort by descending wave count (bin order), ties in any order:
+    // the order only schedules tiles, results do not depend on it
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (int b = 0; b < kSortBins; ++b) { uint32_t c = bins[b]; bins[b] = acc; acc += c; }
+    }
+    __syncthreads();
+    // sorted <- order; the tile counts are read back through it below
+    for (uint32_t p = threadIdx.x; p < n; p += blockDim.x) {
+        uint32_t wc = patches[p].wave_count;
+        uint32_t key = wc < kSortBins ? wc : kSortBins - 1;
+        uint32_t slot = atomicAdd(&bins[kSortBins - 1 - key], 1u);
+        sorted[slot] = p;
+    }
+    __syncthreads();
+    for (uint32_t q = threadIdx.x; q < n; q += blockDim.x) tile_pre[q] = tiles[sorted[q]];
+    __syncthreads();
+    uint32_t total_tiles = block_exclusive_scan(tile_pre, n);
+    if (threadIdx.x == 0) {
+        tile_pre[n] = total_tiles;
+        hdr->total_tiles = total_tiles;
+    }
+}
+
+__device__ __forceinline__ unsigned long long to_fixed_turns(double turns) {
+    double f = turns - floor(turns);                 // [0, 1)
+    double hi = floor(f * 4294967296.0);             // < 2^32
+    double lo = floor((f * 4294967296.0 - hi) * 4294967296.0);
+    return ((unsigned long long)hi << 32) | (unsigned long long)lo;
+}
+
+// positive remainder of x by m (FP64)
+__device__ __forceinline__ double pmod(double x, double m) {
+    double r = x - m * floor(x / m);
+    return r >= m ? r - m : (r < 0.0 ? r + m : r);
+}
+
+// ---- stage 2: FP64 constants per (patch, wave) and per patch ---------------
+__global__ void __launch_bounds__(256) k_prep_coef(const wt_patch* __restrict__ patches, uint32_t n,
+                                                   const wt_wave* __restrict__ waves, HmDev hm, char* ws,
+                                                   WsLayout L) {
+#if __CUDA_ARCH__ >= 900
+    cudaGridDependencySynchronize();
+#endif
+    const uint32_t* pair_off = reinterpret_cast<const uint32_t*>(ws + L.pair_off);
+    PatchAux* aux = reinterpret_cast<PatchAux*>(ws + L.aux);
+    PairCoef* coef = reinterpret_cast<PairCoef*>(ws + L.coef);
+    const uint32_t total = pair_off[n];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t P = blockIdx.x * blockDim.x + threadIdx.x; P < total; P += stride) {
+        // owning patch: last p with pair_off[p] <= P
+        uint32_t lo = 0, hi = n + 1;
+        while (lo < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (pair_off[mid] <= P) lo = mid + 1; else hi = mid;
+        }
+        uint32_t p = lo - 1;
+        const wt_patch& Pt = patches[p];
+        const wt_wave w = waves[Pt.wave_offset + (P - pair_off[p])];
+        double lam = w.wavelength;
+        double inv_lam = isinf(lam) ? 0.0 : 1.0 / lam;     // k / 2pi
+        double k = kTwoPi * inv_lam;
+        double Dx = w.dir_x, Dz = w.dir_z, A = w.amplitude, Q = w.steepness_q;
+        double blx = Pt.bl[0], blz = Pt.bl[1];
+        double e1x = (double)Pt.br[0] - blx, e1z = (double)Pt.br[1] - blz;
+        double e2x = (double)Pt.tl[0] - blx, e2z = (double)Pt.tl[1] - blz;
+        double e3x = (double)Pt.tr[0] - Pt.tl[0] - Pt.br[0] + blx;
+        double e3z = (double)Pt.tr[1] - Pt.tl[1] - Pt.br[1] + blz;
+        double cm1 = (double)(Pt.cols - 1), rm1 = (double)(Pt.rows - 1);
+        // theta / 2pi at (col, row) = t00 + col*ta + row*tb + col*row*tg
+        double t00 = (Dx * blx + Dz * blz) * inv_lam + (double)w.speed * Pt.time_s * inv_lam +
+                     (double)w.phase * (1.0 / kTwoPi);
+        double ta = (Dx * e1x + Dz * e1z) * inv_lam / cm1;
+        double tb = (Dx * e2x + Dz * e2z) * inv_lam / rm1;
+        double tg = (Dx * e3x + Dz * e3z) * inv_lam / (cm1 * rm1);
+        PairCoef c;
+        c.t00 = to_fixed_turns(t00);
+        c.ta = to_fixed_turns(ta);
+        c.tb = to_fixed_turns(tb);
+        c.tg = to_fixed_turns(tg);
+        c.qadx = (float)(Q * A * Dx);
+        c.a = (float)A;
+        c.qadz = (float)(Q * A * Dz);
+        c.akdx = (float)(A * k * Dx);
+        c.akdz = (float)(A * k * Dz);
+        c.qakxx = (float)(Q * A * k * Dx * Dx);
+        c.qakxz = (float)(Q * A * k * Dx * Dz);
+        c.qakzz = (float)(Q * A * k * Dz * Dz);
+        coef[P] = c;
+    }
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
+        const wt_patch& Pt = patches[p];
+        double blx = Pt.bl[0], blz = Pt.bl[1];
+        PatchAux a;
+        a.e1x = (float)((double)Pt.br[0] - blx);
+        a.e1z = (float)((double)Pt.br[1] - blz);
+        a.e2x = (float)((double)Pt.tl[0] - blx);
+        a.e2z = (float)((double)Pt.tl[1] - blz);
+        a.e3x = (float)((double)Pt.tr[0] - Pt.tl[0] - Pt.br[0] + blx);
+        a.e3z = (float)((double)Pt.tr[1] - Pt.tl[1] - Pt.br[1] + blz);
+        a.blx = Pt.bl[0];
+        a.blz = Pt.bl[1];
+        a.inv_cm1 = Pt.cols > 1 ? 1.0f / (float)(Pt.cols - 1) : 0.0f;
+        a.inv_rm1 = Pt.rows > 1 ? 1.0f / (float)(Pt.rows - 1) : 0.0f;
+        if (hm.present) {
+            double W = hm.width, H = hm.height;
+            double pu = hm.wrap == WT_WRAP_MIRRORED_REPEAT ? 2.0 * W : W;
+            double pv = hm.wrap == WT_WRAP_MIRRORED_REPEAT ? 2.0 * H : H;
+            // texel coordinate of the world point X: sample_scale*W*X - 0.5;
+            // the BL part is reduced by the wrap period in FP64
+            a.hu0 = (float)(pmod((double)hm.sample_scale * W * blx, pu) - 0.5);
+            a.hv0 = (float)(pmod(-(double)hm.sample_scale * H * blz, pv) - 0.5);
+            a.su = (float)((double)hm.sample_scale * W);
+            a.sv = (float)(-(double)hm.sample_scale * H);
+        } else {
+            a.hu0 = a.hv0 = a.su = a.sv = 0.0f;
+        }
+        a.y_offset = Pt.y_offset;
+        a.pair_offset = pair_off[p];
+        aux[p] = a;
+    }
+}
+
+// ---- shared epilogue -------------------------------------------------------
+
+// texel index wrap (GL spec: REPEAT i mod n; MIRRORED_REPEAT
+// (n-1) - mirror((i mod 2n) - n)), for |i| < 2^24 via FP32 floor division
+__device__ __forceinline__ int wrap_texel(int i, int n, float inv_n, uint32_t mode) {
+    if (mode == WT_WRAP_MIRRORED_REPEAT) {
+        int n2 = 2 * n;
+        int q = __float2int_rd((float)i * (0.5f * inv_n));
+        int m = i - q * n2;
+        m += (m < 0) ? n2 : 0;
+        m -= (m >= n2) ? n2 : 0;
+        int a = m - n;
+        int mir = a >= 0 ? a : -(1 + a);
+        return n - 1 - mir;
+    }
+    int q = __float2int_rd((float)i * inv_n);
+    int m = i - q * n;
+    m += (m < 0) ? n : 0;
+    m -= (m >= n) ? n : 0;
+    return m;
+}
+
+struct VertexSums {
+    float dx, dy, dz, jx, jz, sxx, sxz, szz;
+};
+
+// Heightmap, bounce, normal, stores for one vertex.
+__device__ __forceinline__ void finish_vertex(const VertexSums& s, float xl, float zl, const PatchAux& a,
+                                              const HmDev& hm, float inv_w, float inv_h, uint64_t vidx,
+                                              float* __restrict__ pos, float* __restrict__ nrm,
+                                              uint32_t flags) {
+    float px0 = 1.0f - s.sxx, px1 = s.jx, px2 = -s.sxz;
+    float pz0 = -s.sxz, pz1 = s.jz, pz2 = 1.0f - s.szz;
+    float dy = s.dy;
+    if (hm.present) {
+        float ut = fmaf(a.su, xl + s.dx, a.hu0);
+        float vt = fmaf(a.sv, zl + s.dz, a.hv0);
+        float fi = floorf(ut), fj = floorf(vt);
+        float al = ut - fi, be = vt - fj;
+        int i0 = (int)fi, j0 = (int)fj;
+        int W = (int)hm.width, H = (int)hm.height;
+        int ia = wrap_texel(i0, W, inv_w, hm.wrap), ib = wrap_texel(i0 + 1, W, inv_w, hm.wrap);
+        int ja = wrap_texel(j0, H, inv_h, hm.wrap), jb = wrap_texel(j0 + 1, H, inv_h, hm.wrap);
+        float t00 = __ldg(hm.texels + ja * W + ia), t10 = __ldg(hm.texels + ja * W + ib);
+        float t01 = __ldg(hm.texels + jb * W + ia), t11 = __ldg(hm.texels + jb * W + ib);
+        float r0 = fmaf(al, t10 - t00, t00), r1 = fmaf(al, t11 - t01, t01);
+        float r = fmaf(be, r1 - r0, r0);
+        float dru = fmaf(be, (t11 - t01) - (t10 - t00), t10 - t00);
+        float drv = r1 - r0;
+        float k2 = 2.0f * hm.disp_scale;
+        dy = fmaf(k2, r - 0.5f, dy);
+        float hx = k2 * dru * a.su, hz = k2 * drv * a.sv;
+        px1 = fmaf(hx, px0, fmaf(hz, px2, px1));
+        pz1 = fmaf(hx, pz0, fmaf(hz, pz2, pz1));
+    }
+    dy += a.y_offset;
+    // N = dP/dz x dP/dx
+    float n0 = pz1 * px2 - pz2 * px1;
+    float n1 = pz2 * px0 - pz0 * px2;
+    float n2 = pz0 * px1 - pz1 * px0;
+    float inv = rsqrtf(fmaf(n0, n0, fmaf(n1, n1, n2 * n2)));
+    float ox, oz, ow;
+    if (flags & WT_OUT_DISPLACEMENT) { ox = s.dx; oz = s.dz; ow = 0.0f; }
+    else { ox = a.blx + (xl + s.dx); oz = a.blz + (zl + s.dz); ow = 1.0f; }
+    if (flags & WT_LAYOUT_VEC3) {
+        float* P = pos + 3 * vidx;
+        __stcs(P, ox); __stcs(P + 1, dy); __stcs(P + 2, oz);
+        if (nrm) {
+            float* N = nrm + 3 * vidx;
+            __stcs(N, n0 * inv); __stcs(N + 1, n1 * inv); __stcs(N + 2, n2 * inv);
+        }
+    } else {
+        __stcs(reinterpret_cast<float4*>(pos) + vidx, make_float4(ox, dy, oz, ow));
+        if (nrm) __stcs(reinterpret_cast<float4*>(nrm) + vidx, make_float4(n0 * inv, n1 * inv, n2 * inv, 0.0f));
+    }
+}
+
+__device__ __forceinline__ uint32_t hi32_round(unsigned long long x) {
+    return (uint32_t)((x + 0x80000000ull) >> 32);
+}
+
+// ---- stage 3: the persistent forward kernel --------------------------------
+template <int S, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB)
+k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ pos,
+          float* __restrict__ nrm, uint32_t flags, char* __restrict__ ws, WsLayout L) {
+#if __CUDA_ARCH__ >= 900
+    cudaGridDependencySynchronize();
+#endif
+    constexpr int TILE = 32 * S;
+    __shared__ float4 stage[THREADS / 32][32 * 3];
+    WsHeader* hdr = reinterpret_cast<WsHeader*>(ws);
+    const uint32_t* sorted = reinterpret_cast<const uint32_t*>(ws + L.sorted);
+    const uint32_t* tile_pre = reinterpret_cast<const uint32_t*>(ws + L.tile_pre);
+    const PatchAux* aux = reinterpret_cast<const PatchAux*>(ws + L.aux);
+    const PairCoef* coef = reinterpret_cast<const PairCoef*>(ws + L.coef);
+    const int lane = threadIdx.x & 31;
+    float4* wst = stage[threadIdx.x >> 5];
+    const uint32_t n = hdr->n_patches;
+    const uint32_t total = hdr->total_tiles;
+    const float inv_w = hm.present ? 1.0f / (float)hm.width : 0.0f;
+    const float inv_h = hm.present ? 1.0f / (float)hm.height : 0.0f;
+
+    for (;;) {
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(&hdr->tile_counter, 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= total) break;
+        uint32_t lo = 0, hi = n + 1;
+        while (lo < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (tile_pre[mid] <= t) lo = mid + 1; else hi = mid;
+        }
+        const uint32_t q = lo - 1;
+        const uint32_t p = sorted[q];
+        const uint32_t lt = t - tile_pre[q];
+        const uint32_t cols = patches[p].cols;
+        const uint32_t nwaves = patches[p].wave_count;
+        const uint64_t out0 = patches[p].out_offset;
+        const PatchAux a = aux[p];
+        const uint32_t tpr = (cols + TILE - 1) / TILE;
+        const uint32_t row = lt / tpr;
+        const uint32_t c0 = (lt - row * tpr) * TILE;
+
+        float acc[S][8];
+#pragma unroll
+        for (int j = 0; j < S; ++j)
+#pragma unroll
+            for (int m = 0; m < 8; ++m) acc[j][m] = 0.0f;
+
+        for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
+            const uint32_t nw = min(32u, nwaves - w0);
+            __syncwarp();
+            if ((uint32_t)lane < nw) {
+                const PairCoef c = coef[a.pair_offset + w0 + lane];
+                // phase of this wave at (c0, row) and its per-column step on this row
+                unsigned long long t64 = c.t00 + (unsigned long long)c0 * c.ta + (unsigned long long)row * c.tb +
+                                         (unsigned long long)c0 * row * c.tg;
+                unsigned long long a64 = c.ta + (unsigned long long)row * c.tg;
+                uint32_t t32 = hi32_round(t64), a32 = hi32_round(a64), d32 = hi32_round(a64 * 32ull);
+                // rotation by the 32-column step: sincospi of the high part
+                // (exact in FP32), then a first-order turn by the low 8 bits
+                const uint32_t dhi = d32 & 0xffffff00u;
+                float sd, cd;
+                sincospif((float)(int)dhi * 4.656612873077393e-10f, &sd, &cd);  // sin(2*pi*turns)
+                const float eps = (float)(d32 - dhi) * kTurnToRad;
+                const float cdn = fmaf(-sd, eps, cd);
+                sd = fmaf(cd, eps, sd);
+                cd = cdn;
+                wst[3 * lane] = make_float4(__uint_as_float(t32), __uint_as_float(a32), cd, sd);
+                wst[3 * lane + 1] = make_float4(c.qadx, c.a, c.qadz, c.akdx);
+                wst[3 * lane + 2] = make_float4(c.akdz, c.qakxx, c.qakxz, c.qakzz);
+            }
+            __syncwarp();
+            for (uint32_t i = 0; i < nw; ++i) {
+                const float4 w0v = wst[3 * i];
+                const float4 w1 = wst[3 * i + 1];
+                const float4 w2 = wst[3 * i + 2];
+                uint32_t tl = __float_as_uint(w0v.x) + (uint32_t)lane * __float_as_uint(w0v.y);
+                float ang = (float)(int)tl * kTurnToRad;
+                float s, c;
+                __sincosf(ang, &s, &c);
+                const float cd = w0v.z, sd = w0v.w;
+#pragma unroll
+                for (int j = 0; j < S; ++j) {
+                    if (j > 0) {
+                        float cn = fmaf(c, cd, -s * sd);
+                        float sn = fmaf(s, cd, c * sd);
+                        c = cn;
+                        s = sn;
+                    }
+                    acc[j][0] = fmaf(w1.x, c, acc[j][0]);
+                    acc[j][1] = fmaf(w1.y, s, acc[j][1]);
+                    acc[j][2] = fmaf(w1.z, c, acc[j][2]);
+                    acc[j][3] = fmaf(w1.w, c, acc[j][3]);
+                    acc[j][4] = fmaf(w2.x, c, acc[j][4]);
+                    acc[j][5] = fmaf(w2.y, s, acc[j][5]);
+                    acc[j][6] = fmaf(w2.z, s, acc[j][6]);
+                    acc[j][7] = fmaf(w2.w, s, acc[j][7]);
+                }
+            }
+        }
+
+        const float v = (float)row * a.inv_rm1;
+        const uint64_t rowbase = out0 + (uint64_t)row * cols;
+#pragma unroll
+        for (int j = 0; j < S; ++j) {
+            const uint32_t col = c0 + lane + 32 * j;
+            if (col < cols) {
+                const float u = (float)col * a.inv_cm1;
+                const float uv = u * v;
+                const float xl = fmaf(u, a.e1x, fmaf(v, a.e2x, uv * a.e3x));
+                const float zl = fmaf(u, a.e1z, fmaf(v, a.e2z, uv * a.e3z));
+                VertexSums s{acc[j][0], acc[j][1], acc[j][2], acc[j][3], acc[j][4], acc[j][5], acc[j][6], acc[j][7]};
+                finish_vertex(s, xl, zl, a, hm, inv_w, inv_h, rowbase + col, pos, nrm, flags);
+            }
+        }
+    }
+}
+
+// ---- FP32-naive phase (precision studies only) -----------------------------
+// The reference's arithmetic: theta = w*dot(D, xz) + phi*t in FP32 with world
+// xz (water-grid.vert:78), accurate sinf/cosf so that only the phase
+// representation differs from the default path.
+__global__ void __launch_bounds__(256) k_forward_naive(const wt_patch* __restrict__ patches, uint32_t n,
+                                                       const wt_wave* __restrict__ waves, HmDev hm,
+                                                       float* __restrict__ pos, float* __restrict__ nrm,
+                                                       uint32_t flags, const char* __restrict__ ws, WsLayout L) {
+    const PatchAux* aux = reinterpret_cast<const PatchAux*>(ws + L.aux);
+    const WsHeader* hdr = reinterpret_cast<const WsHeader*>(ws);
+    const uint32_t* tile_pre = reinterpret_cast<const uint32_t*>(ws + L.tile_pre);
+    const uint32_t* sorted = reinterpret_cast<const uint32_t*>(ws + L.sorted);
+    const float inv_w = hm.present ? 1.0f / (float)hm.width : 0.0f;
+    const float inv_h = hm.present ? 1.0f / (float)hm.height : 0.0f;
+    for (uint32_t q = 0; q < n; ++q) {
+        if (tile_pre[q + 1] == tile_pre[q]) continue;  // invalid patch
+        const uint32_t p = sorted[q];
+        const wt_patch P = patches[p];
+        const PatchAux a = aux[p];
+        const uint64_t nv = (uint64_t)P.cols * P.rows;
+        const float t = (float)P.time_s;
+        for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < nv;
+             v += (uint64_t)gridDim.x * blockDim.x) {
+            uint32_t row = (uint32_t)(v / P.cols), col = (uint32_t)(v - (uint64_t)row * P.cols);
+            float u = (float)col * a.inv_cm1, vv = (float)row * a.inv_rm1, uv = u * vv;
+            float xl = fmaf(u, a.e1x, fmaf(vv, a.e2x, uv * a.e3x));
+            float zl = fmaf(u, a.e1z, fmaf(vv, a.e2z, uv * a.e3z));
+            float xw = a.blx + xl, zw = a.blz + zl;
+            VertexSums s{0, 0, 0, 0, 0, 0, 0, 0};
+            for (uint32_t i = 0; i < P.wave_count; ++i) {
+                const wt_wave w = waves[P.wave_offset + i];
+                float k = isinf(w.wavelength) ? 0.0f : (float)(kTwoPi / (double)w.wavelength);
+                float phi = w.speed * k;
+                float th = k * (w.dir_x * xw + w.dir_z * zw) + phi * t + w.phase;
+                float sn, c;
+                sincosf(th, &sn, &c);
+                float A = w.amplitude, Q = w.steepness_q;
+                s.dx += Q * A * w.dir_x * c; s.dy += A * sn; s.dz += Q * A * w.dir_z * c;
+                s.jx += A * k * w.dir_x * c; s.jz += A * k * w.dir_z * c;
+                s.sxx += Q * A * k * w.dir_x * w.dir_x * sn;
+                s.sxz += Q * A * k * w.dir_x * w.dir_z * sn;
+                s.szz += Q * A * k * w.dir_z * w.dir_z * sn;
+            }
+            finish_vertex(s, xl, zl, a, hm, inv_w, inv_h, P.out_offset + v, pos, nrm, flags);
+        }
+    }
+    (void)hdr;
+}
+
+template <int S, int THREADS, int MINB>
+cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const HmDev& hm, float* pos,
+                         float* nrm, uint32_t flags, void* ws, const WsLayout& L, cudaStream_t s) {
+    static int sms = -1;
+    static int occ = -1;
+    if (sms < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_forward<S, THREADS, MINB>, THREADS, 0);
+        if (occ < 1) occ = 1;
+    }
+    int bps = cfg.blocks_per_sm > 0 ? (cfg.blocks_per_sm < occ ? cfg.blocks_per_sm : occ) : occ;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)(sms * bps));
+    lc.blockDim = dim3(THREADS);
+    lc.dynamicSmemBytes = 0;
+    lc.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    return cudaLaunchKernelEx(&lc, k_forward<S, THREADS, MINB>, patches, hm, pos, nrm, flags,
+                              static_cast<char*>(ws), L);
+}
+
+}  // namespace
+
+cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
+                        const HmDev& hm, uint64_t out_capacity, uint32_t tile_cols, void* ws,
+                        const WsLayout& L, cudaStream_t s) {
+    char* w = static_cast<char*>(ws);
+    // coefficient capacity = what the caller's workspace holds past the fixed part
+    // (the header records the real total; the scan refuses to overflow it)
+    uint64_t coef_cap = (L.end - L.coef) / sizeof(PairCoef);
+    k_prep_scan<<<1, 1024, 0, s>>>(patches, n_patches, waves, n_waves, out_capacity, coef_cap, tile_cols, w, L);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    static int sms = -1;
+    if (sms < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)sms);
+    lc.blockDim = dim3(256);
+    lc.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    return cudaLaunchKernelEx(&lc, k_prep_coef, patches, n_patches, waves, hm, w, L);
+}
+
+bool forward_config_supported(const FwdConfig& c) {
+    return (c.s == 8 && (c.warps == 8 || c.warps == 4)) || (c.s == 4 && (c.warps == 8 || c.warps == 4));
+}
+
+cudaError_t launch_forward(const FwdConfig& cfg, const wt_patch* patches, uint32_t, const HmDev& hm,
+                           float* pos, float* nrm, uint32_t flags, void* ws, const WsLayout& L,
+                           cudaStream_t s) {
+    if (cfg.s == 8 && cfg.warps == 8) return launch_fwd_t<8, 256, 2>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
+    if (cfg.s == 8 && cfg.warps == 4) return launch_fwd_t<8, 128, 4>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
+    if (cfg.s == 4 && cfg.warps == 8) return launch_fwd_t<4, 256, 3>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
+    if (cfg.s == 4 && cfg.warps == 4) return launch_fwd_t<4, 128, 6>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_forward_naive(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
+                                 const HmDev& hm, float* pos, float* nrm, uint32_t flags, void* ws,
+                                 const WsLayout& L, uint64_t, cudaStream_t s) {
+    static int sms = -1;
+    if (sms < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    k_forward_naive<<<sms * 4, 256, 0, s>>>(patches, n_patches, waves, hm, pos, nrm, flags,
+                                            static_cast<const char*>(ws), L);
+    return cudaGetLastError();
+}
+
+}  // namespace wt

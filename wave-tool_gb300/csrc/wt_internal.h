@@ -1,0 +1,113 @@
+// wt_internal.h — shared declarations of the host API (wt_api.cpp) and the
+// kernels (*.cu).  Not part of the public ABI.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "../../include/wt.h"
+
+namespace wt {
+
+// ---- workspace layout ------------------------------------------------------
+// [0, 256)                 WsHeader
+// sorted   u32[n_patches]  patch indices, descending wave count (LPT order)
+// tile_pre u32[n+1]        exclusive prefix of tiles over the sorted order
+// pair_off u32[n+1]        exclusive prefix of wave_count (original order)
+// tiles    u32[n]          tile count per patch (original order, 0 = invalid)
+// aux      PatchAux[n]
+// coef     PairCoef[total_wave_slots]
+struct WsHeader {
+    uint32_t status;       // wt_status of device-side validation (0 = ok)
+    uint32_t bad_patch;    // smallest offending patch index (0xffffffff none)
+    uint32_t tile_counter; // dynamic tile queue head
+    uint32_t total_tiles;
+    uint32_t n_patches;
+    uint32_t tile_cols;    // vertices per tile row (32 * S)
+    uint32_t pad[58];
+};
+static_assert(sizeof(WsHeader) == 256, "header size");
+
+// Per-patch constants, computed once per launch by the prep kernel.
+struct alignas(16) PatchAux {
+    float e1x, e1z;     // BR - BL          (local frame, metres)
+    float e2x, e2z;     // TL - BL
+    float e3x, e3z;     // TR - TL - BR + BL
+    float blx, blz;     // world BL (for world-space output)
+    float inv_cm1;      // 1 / (cols - 1)
+    float inv_rm1;      // 1 / (rows - 1)
+    float hu0, hv0;     // heightmap texel coordinate of BL, reduced by the wrap period, minus 0.5
+    float su, sv;       // texels per metre along x and along z (sv carries the -z flip)
+    float y_offset;
+    uint32_t pair_offset;
+};
+static_assert(sizeof(PatchAux) == 64, "aux size");
+
+// Per-(patch, wave) constants.  The phase theta(col, row) of the wave on the
+// patch's bilinear grid is, exactly,
+//   theta = theta00 + col*a + row*b + col*row*g
+// and is carried in turns (theta / 2pi) as 64-bit fixed point mod 1, so that
+// integer wrap-around performs the mod-2pi reduction for free.
+struct alignas(16) PairCoef {
+    unsigned long long t00, ta, tb, tg;  // turns * 2^64
+    float qadx, a, qadz, akdx;           // Q*A*Dx, A, Q*A*Dz, A*k*Dx
+    float akdz, qakxx, qakxz, qakzz;     // A*k*Dz, Q*A*k*Dx^2, Q*A*k*Dx*Dz, Q*A*k*Dz^2
+};
+static_assert(sizeof(PairCoef) == 64, "coef size");
+
+struct WsLayout {
+    size_t sorted, tile_pre, pair_off, tiles, aux, coef, end;
+};
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+inline WsLayout ws_layout(uint32_t n_patches, uint64_t total_wave_slots) {
+    WsLayout L;
+    size_t o = sizeof(WsHeader);
+    L.sorted = o;   o = align_up(o + 4ull * n_patches, 16);
+    L.tile_pre = o; o = align_up(o + 4ull * (n_patches + 1), 16);
+    L.pair_off = o; o = align_up(o + 4ull * (n_patches + 1), 16);
+    L.tiles = o;    o = align_up(o + 4ull * n_patches, 64);
+    L.aux = o;      o = align_up(o + sizeof(PatchAux) * (size_t)n_patches, 64);
+    L.coef = o;     o = align_up(o + sizeof(PairCoef) * (size_t)total_wave_slots, 256);
+    L.end = o;
+    return L;
+}
+
+// Tuning of the forward launch.
+struct FwdConfig {
+    int s;              // vertices per lane per tile row (tile = 32*s columns)
+    int chunk;          // waves staged per warp at a time (<= 32)
+    int warps;          // warps per block
+    int blocks_per_sm;  // persistent grid = SMs * blocks_per_sm (0 = occupancy max)
+};
+
+struct HmDev {
+    const float* texels;
+    uint32_t width, height;
+    float sample_scale, disp_scale;
+    uint32_t wrap;
+    int present;
+};
+
+// ---- launchers (wt_displace.cu) -------------------------------------------
+cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
+                        uint32_t n_waves, const HmDev& hm, uint64_t out_capacity,
+                        uint32_t tile_cols, void* ws, const WsLayout& L, cudaStream_t s);
+cudaError_t launch_forward(const FwdConfig& cfg, const wt_patch* patches, uint32_t n_patches,
+                           const HmDev& hm, float* pos, float* nrm, uint32_t flags, void* ws,
+                           const WsLayout& L, cudaStream_t s);
+cudaError_t launch_forward_naive(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
+                                 const HmDev& hm, float* pos, float* nrm, uint32_t flags,
+                                 void* ws, const WsLayout& L, uint64_t total_vertices,
+                                 cudaStream_t s);
+bool forward_config_supported(const FwdConfig& cfg);
+
+// ---- misc kernels (wt_misc.cu) --------------------------------------------
+cudaError_t launch_indices(uint32_t cols, uint32_t rows, uint32_t base, uint32_t* out, cudaStream_t s);
+cudaError_t launch_noise(const wt_noise_term* terms, uint32_t n_terms, uint32_t w, uint32_t h,
+                         float* out, void* ws, cudaStream_t s);
+cudaError_t measure_peaks(void* scratch, size_t bytes, double* fma, double* sin, cudaStream_t s);
+
+}  // namespace wt

@@ -1,0 +1,198 @@
+// wt_misc.cu — index buffer, noise heightmap synthesis, peak-rate probes.
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "wt_internal.h"
+
+namespace wt {
+namespace {
+
+// ---- projected-grid index buffer (src/program.cpp:686-717) ----------------
+// One thread per output index: k = 6*cell + m, cell = row*(cols-1) + col,
+// triangles (r,c) (r+1,c+1) (r+1,c) and (r,c) (r,c+1) (r+1,c+1).
+// Coalesced 4-byte stores; the buffer is HBM-write-bound.
+__global__ void __launch_bounds__(256) k_indices(uint32_t cols, uint32_t rows, uint32_t base, uint32_t* __restrict__ out,
+                                                 uint64_t total) {
+    const uint32_t cm1 = cols - 1;
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < total;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t cell = k / 6;
+        uint32_t m = (uint32_t)(k - cell * 6);
+        uint32_t row = (uint32_t)(cell / cm1);
+        uint32_t col = (uint32_t)(cell - (uint64_t)row * cm1);
+        // m:      0     1       2     3     4     5
+        // dr:     0     1       1     0     0     1
+        // dc:     0     1       0     0     1     1
+        uint32_t dr = (0x26u >> m) & 1u;  // bits 1,2,5
+        uint32_t dc = (0x32u >> m) & 1u;  // bits 1,4,5
+        __stcs(out + k, base + (row + dr) * cols + col + dc);
+    }
+}
+
+// ---- noise heightmap -------------------------------------------------------
+__device__ __forceinline__ uint32_t ordered(float f) {
+    uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float unordered(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+__global__ void k_noise_init(uint32_t* mm) {
+    mm[0] = 0xffffffffu;  // min (ordered)
+    mm[1] = 0u;           // max (ordered)
+}
+
+// h(i, j) = sum a sin(2*pi*((kx*i mod W)/W + (ky*j mod H)/H) + psi): the
+// integer products are reduced exactly before the turn is formed.
+__global__ void __launch_bounds__(256) k_noise(const wt_noise_term* __restrict__ terms, uint32_t n_terms, uint32_t W,
+                                               uint32_t H, float* __restrict__ out, uint32_t* mm) {
+    __shared__ float4 st[256];
+    const uint32_t i = blockIdx.x * 16 + (threadIdx.x & 15);
+    const uint32_t j = blockIdx.y * 16 + (threadIdx.x >> 4);
+    const bool in = i < W && j < H;
+    float h = 0.0f;
+    for (uint32_t b = 0; b < n_terms; b += 256) {
+        __syncthreads();
+        if (b + threadIdx.x < n_terms) {
+            wt_noise_term t = terms[b + threadIdx.x];
+            float sp, cp;
+            sincosf(t.phase, &sp, &cp);
+            st[threadIdx.x] = make_float4(__int_as_float(t.kx), __int_as_float(t.ky), t.amplitude * cp,
+                                          t.amplitude * sp);
+        }
+        __syncthreads();
+        const uint32_t nb = min(256u, n_terms - b);
+        for (uint32_t m = 0; m < nb; ++m) {
+            float4 t = st[m];
+            long long ni = ((long long)__float_as_int(t.x) * i) % (long long)W;
+            long long nj = ((long long)__float_as_int(t.y) * j) % (long long)H;
+            ni += ni < 0 ? W : 0;
+            nj += nj < 0 ? H : 0;
+            float turns = (float)ni / (float)W + (float)nj / (float)H;
+            float s, c;
+            sincospif(2.0f * turns, &s, &c);
+            // a sin(x + psi) = (a cos psi) sin x + (a sin psi) cos x
+            h = fmaf(t.z, s, fmaf(t.w, c, h));
+        }
+    }
+    // block min / max, then one atomic each
+    float lo = in ? h : INFINITY, hi = in ? h : -INFINITY;
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0 && lo <= hi) {
+        atomicMin(mm, ordered(lo));
+        atomicMax(mm + 1, ordered(hi));
+    }
+    if (in) out[(size_t)j * W + i] = h;
+}
+
+__global__ void __launch_bounds__(256) k_noise_norm(float* __restrict__ out, size_t n, const uint32_t* mm) {
+    const float lo = unordered(mm[0]), hi = unordered(mm[1]);
+    const float span = hi - lo;
+    const float inv = span > 0.0f ? 1.0f / span : 0.0f;
+    for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x)
+        out[v] = (out[v] - lo) * inv;
+}
+
+// ---- peak probes -----------------------------------------------------------
+// Eight independent dependent chains per thread: issue-bound FP32 FMA and
+// MUFU sine, the two pipes the Gerstner sum can run on.
+__global__ void __launch_bounds__(256) k_peak_fma(float* out, int iters, float a, float b) {
+    float x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = threadIdx.x * 1e-3f + j;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = fmaf(x[j], a, b);
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += x[j];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(256) k_peak_sin(float* out, int iters) {
+    float x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = threadIdx.x * 1e-3f + j;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = __sinf(x[j]);
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += x[j];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+int device_sms() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+}  // namespace
+
+cudaError_t launch_indices(uint32_t cols, uint32_t rows, uint32_t base, uint32_t* out, cudaStream_t s) {
+    uint64_t total = 6ull * (cols - 1) * (rows - 1);
+    if (total == 0) return cudaSuccess;
+    uint64_t want = (total + 255) / 256;
+    unsigned blocks = (unsigned)(want < (uint64_t)device_sms() * 16 ? want : (uint64_t)device_sms() * 16);
+    k_indices<<<blocks, 256, 0, s>>>(cols, rows, base, out, total);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_noise(const wt_noise_term* terms, uint32_t n_terms, uint32_t w, uint32_t h, float* out,
+                         void* ws, cudaStream_t s) {
+    uint32_t* mm = static_cast<uint32_t*>(ws);
+    k_noise_init<<<1, 1, 0, s>>>(mm);
+    dim3 grid((w + 15) / 16, (h + 15) / 16);
+    k_noise<<<grid, 256, 0, s>>>(terms, n_terms, w, h, out, mm);
+    size_t n = (size_t)w * h;
+    unsigned blocks = (unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    k_noise_norm<<<blocks, 256, 0, s>>>(out, n, mm);
+    return cudaGetLastError();
+}
+
+cudaError_t measure_peaks(void* scratch, size_t bytes, double* fma, double* sin_rate, cudaStream_t s) {
+    const int sms = device_sms();
+    const int blocks = sms * 8, threads = 256;
+    if ((size_t)blocks * threads * sizeof(float) > bytes) return cudaErrorInvalidValue;
+    float* out = static_cast<float*>(scratch);
+    cudaEvent_t e0, e1;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e != cudaSuccess) return e;
+    e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) { cudaEventDestroy(e0); return e; }
+    const int it_fma = 1 << 15, it_sin = 1 << 12;
+    float best_fma = 1e30f, best_sin = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        float ms = 0.0f;
+        cudaEventRecord(e0, s);
+        k_peak_fma<<<blocks, threads, 0, s>>>(out, it_fma, 0.999f, 0.001f);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best_fma) best_fma = ms;
+        cudaEventRecord(e0, s);
+        k_peak_sin<<<blocks, threads, 0, s>>>(out, it_sin);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best_sin) best_sin = ms;
+    }
+    e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return e;
+    const double lanes = (double)blocks * threads;
+    *fma = lanes * 8.0 * it_fma / (best_fma * 1e-3);
+    *sin_rate = lanes * 8.0 * it_sin / (best_sin * 1e-3);
+    return cudaSuccess;
+}
+
+}  // namespace wt
