@@ -62,5 +62,5 @@ def rel_err(a, b):
 
 
 def angle_deg(n1, n2):
-    c = np.clip(np.sum(n1 * n2, axis=-1) / (np.linalg.norm(n1, axis=-1) * np.linalg.norm(n2, axis=-1)), -1, 1)
-    return np.degrees(np.arccos(c))
+    """Angle between vectors, atan2(|a x b|, a.b): accurate near zero."""
+    return np.degrees(np.arctan2(np.linalg.norm(np.cross(n1, n2), axis=-1), np.sum(n1 * n2, axis=-1)))

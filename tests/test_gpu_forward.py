@@ -35,12 +35,13 @@ def check_against_f64(oracle, w, pos, nrm, tex, flags=0, disp_tol=DISP_TOL):
     pos64, disp64, nrm64, edge = oracle.displace_f64(w.patches, w.waves, tex, w.heightmap)
     if flags & 1:
         err = rel_err(pos[:, :3].astype(np.float64), disp64)
+        assert err <= disp_tol, f"displacement rel err {err:.3e}"
     else:
+        # world positions carry the FP32 rounding of the world coordinate on
+        # top of the displacement error
         err = rel_err(pos[:, :3].astype(np.float64) - (pos64 - disp64), disp64)
-        # world positions carry one FP32 rounding of the world coordinate
         ulp = np.spacing(np.abs(pos64).astype(np.float32)).astype(np.float64)
         assert np.all(np.abs(pos[:, :3] - pos64) <= 4 * ulp + disp_tol * np.abs(disp64).max())
-    assert err <= disp_tol, f"displacement rel err {err:.3e}"
     if nrm is not None:
         ok = edge > 1e-3
         ang = angle_deg(nrm[ok, :3].astype(np.float64), nrm64[ok])
@@ -158,7 +159,7 @@ def test_golden_reference_cases(wt, oracle, gpu):
         ref = c["world"][:, :3].astype(np.float64)
         dmax = max(np.abs(disp64).max(), 1e-3)
         # the reference's own FP32 error: phase magnitude * 2^-22 * sum(A (1 + Q k A))
-        th = float(np.max(np.abs(c["waves"][:, 1]))) * float(np.abs(c["corners"]).max()) * 1.5 + \
+        th = float(np.max(np.abs(c["waves"][:, 1]), initial=0)) * float(np.abs(c["corners"]).max()) * 1.5 + \
             float(np.max(np.abs(c["waves"][:, 2]), initial=0)) * float(c["scalars"][0])
         ref_tol = (th + 10.0) * 2.0 ** -20 * (np.abs(waves["amplitude"]).sum() + 1.0) + \
             4 * np.spacing(np.float32(np.abs(ref).max())) + 2e-3 * float(c["scalars"][2])

@@ -82,6 +82,15 @@ __device__ uint32_t block_exclusive_scan(uint32_t* a, uint32_t n) {
 }
 
 // ---- stage 1: validation, prefix sums, LPT order ---------------------------
+__device__ __forceinline__ bool patch_ok(const wt_patch& P, uint32_t n_waves, uint64_t out_capacity) {
+    const uint64_t verts = (uint64_t)P.cols * P.rows;
+    return P.cols >= 2 && P.rows >= 2 && P.cols <= (1u << 20) && P.rows <= (1u << 20) && verts < (1ull << 31) &&
+           P.flags == 0 && (uint64_t)P.wave_offset + P.wave_count <= n_waves && P.out_offset <= out_capacity &&
+           verts <= out_capacity - P.out_offset && finitef(P.bl[0]) && finitef(P.bl[1]) && finitef(P.br[0]) &&
+           finitef(P.br[1]) && finitef(P.tl[0]) && finitef(P.tl[1]) && finitef(P.tr[0]) && finitef(P.tr[1]) &&
+           isfinite(P.time_s) && finitef(P.y_offset);
+}
+
 __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__ patches, uint32_t n,
                                                     const wt_wave* __restrict__ waves, uint32_t n_waves,
                                                     uint64_t out_capacity, uint64_t coef_capacity,
@@ -103,53 +112,59 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
     for (int i = threadIdx.x; i < kSortBins; i += blockDim.x) bins[i] = 0;
     __syncthreads();
 
-    // validate; pair_off <- wave counts, tile_pre <- tile counts (original order)
+    // structural validation; pair_off <- wave counts of the patches that pass
     for (uint32_t p = threadIdx.x; p < n; p += blockDim.x) {
-        wt_patch P = patches[p];
-        uint64_t verts = (uint64_t)P.cols * P.rows;
-        bool ok = P.cols >= 2 && P.rows >= 2 && P.cols <= (1u << 20) && P.rows <= (1u << 20) &&
-                  verts < (1ull << 31) && P.flags == 0 &&
-                  (uint64_t)P.wave_offset + P.wave_count <= n_waves &&
-                  P.out_offset <= out_capacity && verts <= out_capacity - P.out_offset &&
-                  finitef(P.bl[0]) && finitef(P.bl[1]) && finitef(P.br[0]) && finitef(P.br[1]) &&
-                  finitef(P.tl[0]) && finitef(P.tl[1]) && finitef(P.tr[0]) && finitef(P.tr[1]) &&
-                  isfinite(P.time_s) && finitef(P.y_offset);
-        if (ok)
-            for (uint32_t j = 0; j < P.wave_count && ok; ++j) ok = wave_ok(waves[P.wave_offset + j]);
+        const wt_patch P = patches[p];
+        const bool ok = patch_ok(P, n_waves, out_capacity);
         if (!ok) flag_error(hdr, WT_ERR_INVALID_ARG, p);
         pair_off[p] = ok ? P.wave_count : 0u;
         tiles[p] = ok ? P.rows * ((P.cols + tile_cols - 1) / tile_cols) : 0u;
-        uint32_t key = P.wave_count < kSortBins ? P.wave_count : kSortBins - 1;
+        const uint32_t key = P.wave_count < kSortBins ? P.wave_count : kSortBins - 1;
         atomicAdd(&bins[kSortBins - 1 - key], 1u);  // descending wave count
     }
     __syncthreads();
-    uint32_t total_pairs = block_exclusive_scan(pair_off, n);
+    const uint32_t total_pairs = block_exclusive_scan(pair_off, n);
     if (threadIdx.x == 0) pair_off[n] = total_pairs;
-    if (total_pairs > coef_capacity) {
-        // workspace too small for the wave slots: run nothing
-        if (threadIdx.x == 0) { atomicCAS(&hdr->status, 0u, (uint32_t)WT_ERR_NOMEM); hdr->total_tiles = 0; }
+    __syncthreads();
+    // wave validation, one pair per thread; a patch with a bad wave runs no tiles
+    for (uint32_t P = threadIdx.x; P < total_pairs; P += blockDim.x) {
+        uint32_t lo = 0, hi = n + 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (pair_off[mid] <= P) lo = mid + 1; else hi = mid;
+        }
+        const uint32_t p = lo - 1;
+        if (!wave_ok(waves[patches[p].wave_offset + (P - pair_off[p])])) {
+            flag_error(hdr, WT_ERR_INVALID_ARG, p);
+            tiles[p] = 0;
+        }
+    }
+    const bool nomem = total_pairs > coef_capacity;
+    __syncthreads();
+    if (nomem) {
+        // workspace too small for the wave slots: run nothing.  pair_off[n]
+        // bounds every coefficient write of the next kernel.
+        if (threadIdx.x == 0) {
+            atomicCAS(&hdr->status, 0u, (uint32_t)WT_ERR_NOMEM);
+            hdr->total_tiles = 0;
+            pair_off[n] = 0;
+        }
         for (uint32_t p = threadIdx.x; p <= n; p += blockDim.x) tile_pre[p] = 0;
         return;
     }
     // counting sort by descending wave count (bin order), ties in any order:
     // the order only schedules tiles, results do not depend on it
+    block_exclusive_scan(bins, kSortBins);
     __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t acc = 0;
-        for (int b = 0; b < kSortBins; ++b) { uint32_t c = bins[b]; bins[b] = acc; acc += c; }
-    }
-    __syncthreads();
-    // sorted <- order; the tile counts are read back through it below
     for (uint32_t p = threadIdx.x; p < n; p += blockDim.x) {
-        uint32_t wc = patches[p].wave_count;
-        uint32_t key = wc < kSortBins ? wc : kSortBins - 1;
-        uint32_t slot = atomicAdd(&bins[kSortBins - 1 - key], 1u);
-        sorted[slot] = p;
+        const uint32_t wc = patches[p].wave_count;
+        const uint32_t key = wc < kSortBins ? wc : kSortBins - 1;
+        sorted[atomicAdd(&bins[kSortBins - 1 - key], 1u)] = p;
     }
     __syncthreads();
     for (uint32_t q = threadIdx.x; q < n; q += blockDim.x) tile_pre[q] = tiles[sorted[q]];
     __syncthreads();
-    uint32_t total_tiles = block_exclusive_scan(tile_pre, n);
+    const uint32_t total_tiles = block_exclusive_scan(tile_pre, n);
     if (threadIdx.x == 0) {
         tile_pre[n] = total_tiles;
         hdr->total_tiles = total_tiles;
@@ -176,9 +191,16 @@ __global__ void __launch_bounds__(256) k_prep_coef(const wt_patch* __restrict__ 
 #if __CUDA_ARCH__ >= 900
     cudaGridDependencySynchronize();
 #endif
-    const uint32_t* pair_off = reinterpret_cast<const uint32_t*>(ws + L.pair_off);
+    const uint32_t* pair_off_g = reinterpret_cast<const uint32_t*>(ws + L.pair_off);
     PatchAux* aux = reinterpret_cast<PatchAux*>(ws + L.aux);
     PairCoef* coef = reinterpret_cast<PairCoef*>(ws + L.coef);
+    constexpr uint32_t kSmemOffsets = 4096;
+    __shared__ uint32_t off_s[kSmemOffsets];
+    const bool in_smem = n + 1 <= kSmemOffsets;
+    if (in_smem)
+        for (uint32_t i = threadIdx.x; i <= n; i += blockDim.x) off_s[i] = pair_off_g[i];
+    __syncthreads();
+    const uint32_t* pair_off = in_smem ? off_s : pair_off_g;
     const uint32_t total = pair_off[n];
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t P = blockIdx.x * blockDim.x + threadIdx.x; P < total; P += stride) {
@@ -200,13 +222,13 @@ __global__ void __launch_bounds__(256) k_prep_coef(const wt_patch* __restrict__ 
         double e2x = (double)Pt.tl[0] - blx, e2z = (double)Pt.tl[1] - blz;
         double e3x = (double)Pt.tr[0] - Pt.tl[0] - Pt.br[0] + blx;
         double e3z = (double)Pt.tr[1] - Pt.tl[1] - Pt.br[1] + blz;
-        double cm1 = (double)(Pt.cols - 1), rm1 = (double)(Pt.rows - 1);
+        const double inv_cm1 = 1.0 / (double)(Pt.cols - 1), inv_rm1 = 1.0 / (double)(Pt.rows - 1);
         // theta / 2pi at (col, row) = t00 + col*ta + row*tb + col*row*tg
         double t00 = (Dx * blx + Dz * blz) * inv_lam + (double)w.speed * Pt.time_s * inv_lam +
                      (double)w.phase * (1.0 / kTwoPi);
-        double ta = (Dx * e1x + Dz * e1z) * inv_lam / cm1;
-        double tb = (Dx * e2x + Dz * e2z) * inv_lam / rm1;
-        double tg = (Dx * e3x + Dz * e3z) * inv_lam / (cm1 * rm1);
+        double ta = (Dx * e1x + Dz * e1z) * inv_lam * inv_cm1;
+        double tb = (Dx * e2x + Dz * e2z) * inv_lam * inv_rm1;
+        double tg = (Dx * e3x + Dz * e3z) * inv_lam * (inv_cm1 * inv_rm1);
         PairCoef c;
         c.t00 = to_fixed_turns(t00);
         c.ta = to_fixed_turns(ta);
@@ -257,24 +279,38 @@ __global__ void __launch_bounds__(256) k_prep_coef(const wt_patch* __restrict__ 
 
 // ---- shared epilogue -------------------------------------------------------
 
-// texel index wrap (GL spec: REPEAT i mod n; MIRRORED_REPEAT
-// (n-1) - mirror((i mod 2n) - n)), for |i| < 2^24 via FP32 floor division
-__device__ __forceinline__ int wrap_texel(int i, int n, float inv_n, uint32_t mode) {
-    if (mode == WT_WRAP_MIRRORED_REPEAT) {
-        int n2 = 2 * n;
-        int q = __float2int_rd((float)i * (0.5f * inv_n));
-        int m = i - q * n2;
-        m += (m < 0) ? n2 : 0;
-        m -= (m >= n2) ? n2 : 0;
-        int a = m - n;
-        int mir = a >= 0 ? a : -(1 + a);
-        return n - 1 - mir;
-    }
-    int q = __float2int_rd((float)i * inv_n);
-    int m = i - q * n;
-    m += (m < 0) ? n : 0;
-    m -= (m >= n) ? n : 0;
-    return m;
+// Texel coordinate -> the two texel indices of the GL_LINEAR footprint and
+// the weight, with the GL wrap of integer texel indices (REPEAT: i mod n;
+// MIRRORED_REPEAT: (n-1) - mirror((i mod 2n) - n)).  The coordinate is first
+// reduced by the wrap period (exact for |x| < 2^24); indices are clamped into
+// range whatever the input (huge or NaN coordinates give garbage, never an
+// out-of-bounds read).
+struct Footprint {
+    int i0, i1;
+    float w;
+};
+
+__device__ __forceinline__ int mirror_index(int m, int n) {
+    int a = m - n;
+    return n - 1 - (a >= 0 ? a : -(1 + a));
+}
+
+__device__ __forceinline__ Footprint footprint(float x, int n, uint32_t mode) {
+    const bool mir = mode == WT_WRAP_MIRRORED_REPEAT;
+    const int P = mir ? 2 * n : n;
+    const float Pf = (float)P;
+    const float r = x - Pf * floorf(x * (1.0f / Pf));
+    const float fi = floorf(r);
+    Footprint f;
+    f.w = r - fi;
+    int i0 = __float2int_rd(r);
+    i0 += i0 < 0 ? P : 0;
+    i0 -= i0 >= P ? P : 0;
+    i0 = min(max(i0, 0), P - 1);
+    int i1 = i0 + 1 == P ? 0 : i0 + 1;
+    f.i0 = mir ? mirror_index(i0, n) : i0;
+    f.i1 = mir ? mirror_index(i1, n) : i1;
+    return f;
 }
 
 struct VertexSums {
@@ -283,21 +319,19 @@ struct VertexSums {
 
 // Heightmap, bounce, normal, stores for one vertex.
 __device__ __forceinline__ void finish_vertex(const VertexSums& s, float xl, float zl, const PatchAux& a,
-                                              const HmDev& hm, float inv_w, float inv_h, uint64_t vidx,
+                                              const HmDev& hm, uint64_t vidx,
                                               float* __restrict__ pos, float* __restrict__ nrm,
                                               uint32_t flags) {
     float px0 = 1.0f - s.sxx, px1 = s.jx, px2 = -s.sxz;
     float pz0 = -s.sxz, pz1 = s.jz, pz2 = 1.0f - s.szz;
     float dy = s.dy;
     if (hm.present) {
-        float ut = fmaf(a.su, xl + s.dx, a.hu0);
-        float vt = fmaf(a.sv, zl + s.dz, a.hv0);
-        float fi = floorf(ut), fj = floorf(vt);
-        float al = ut - fi, be = vt - fj;
-        int i0 = (int)fi, j0 = (int)fj;
-        int W = (int)hm.width, H = (int)hm.height;
-        int ia = wrap_texel(i0, W, inv_w, hm.wrap), ib = wrap_texel(i0 + 1, W, inv_w, hm.wrap);
-        int ja = wrap_texel(j0, H, inv_h, hm.wrap), jb = wrap_texel(j0 + 1, H, inv_h, hm.wrap);
+        const float ut = fmaf(a.su, xl + s.dx, a.hu0);
+        const float vt = fmaf(a.sv, zl + s.dz, a.hv0);
+        const int W = (int)hm.width, H = (int)hm.height;
+        const Footprint fu = footprint(ut, W, hm.wrap), fv = footprint(vt, H, hm.wrap);
+        const float al = fu.w, be = fv.w;
+        const int ia = fu.i0, ib = fu.i1, ja = fv.i0, jb = fv.i1;
         float t00 = __ldg(hm.texels + ja * W + ia), t10 = __ldg(hm.texels + ja * W + ib);
         float t01 = __ldg(hm.texels + jb * W + ia), t11 = __ldg(hm.texels + jb * W + ib);
         float r0 = fmaf(al, t10 - t00, t00), r1 = fmaf(al, t11 - t01, t01);
@@ -355,8 +389,6 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
     float4* wst = stage[threadIdx.x >> 5];
     const uint32_t n = hdr->n_patches;
     const uint32_t total = hdr->total_tiles;
-    const float inv_w = hm.present ? 1.0f / (float)hm.width : 0.0f;
-    const float inv_h = hm.present ? 1.0f / (float)hm.height : 0.0f;
 
     for (;;) {
         uint32_t t = 0;
@@ -449,7 +481,7 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
                 const float xl = fmaf(u, a.e1x, fmaf(v, a.e2x, uv * a.e3x));
                 const float zl = fmaf(u, a.e1z, fmaf(v, a.e2z, uv * a.e3z));
                 VertexSums s{acc[j][0], acc[j][1], acc[j][2], acc[j][3], acc[j][4], acc[j][5], acc[j][6], acc[j][7]};
-                finish_vertex(s, xl, zl, a, hm, inv_w, inv_h, rowbase + col, pos, nrm, flags);
+                finish_vertex(s, xl, zl, a, hm, rowbase + col, pos, nrm, flags);
             }
         }
     }
@@ -464,11 +496,8 @@ __global__ void __launch_bounds__(256) k_forward_naive(const wt_patch* __restric
                                                        float* __restrict__ pos, float* __restrict__ nrm,
                                                        uint32_t flags, const char* __restrict__ ws, WsLayout L) {
     const PatchAux* aux = reinterpret_cast<const PatchAux*>(ws + L.aux);
-    const WsHeader* hdr = reinterpret_cast<const WsHeader*>(ws);
     const uint32_t* tile_pre = reinterpret_cast<const uint32_t*>(ws + L.tile_pre);
     const uint32_t* sorted = reinterpret_cast<const uint32_t*>(ws + L.sorted);
-    const float inv_w = hm.present ? 1.0f / (float)hm.width : 0.0f;
-    const float inv_h = hm.present ? 1.0f / (float)hm.height : 0.0f;
     for (uint32_t q = 0; q < n; ++q) {
         if (tile_pre[q + 1] == tile_pre[q]) continue;  // invalid patch
         const uint32_t p = sorted[q];
@@ -498,10 +527,9 @@ __global__ void __launch_bounds__(256) k_forward_naive(const wt_patch* __restric
                 s.sxz += Q * A * k * w.dir_x * w.dir_z * sn;
                 s.szz += Q * A * k * w.dir_z * w.dir_z * sn;
             }
-            finish_vertex(s, xl, zl, a, hm, inv_w, inv_h, P.out_offset + v, pos, nrm, flags);
+            finish_vertex(s, xl, zl, a, hm, P.out_offset + v, pos, nrm, flags);
         }
     }
-    (void)hdr;
 }
 
 template <int S, int THREADS, int MINB>
