@@ -178,6 +178,36 @@ wt_status wt_gerstner_displace(const wt_patch* patches, uint32_t n_patches,
                                uint32_t flags, void* workspace, size_t workspace_bytes,
                                wt_stream stream);
 
+/* Limits of wt_gerstner_displace_noalloc. */
+#define WT_NOALLOC_MAX_PATCHES 1024u
+#define WT_NOALLOC_MAX_WAVE_SLOTS 16384u
+
+/* wt_gerstner_displace for callers that cannot allocate device memory: a
+ * renderer or engine plugin that runs inside a host application's frame,
+ * where the host owns every device buffer and a cudaMalloc (which may
+ * synchronise the whole device) would stall the frame, or a caller that only
+ * receives ready-made input and output buffers and has no allocator of its
+ * own.  The scratch that wt_gerstner_displace takes as `workspace` lives here
+ * in a fixed array inside the library (about 1.1 MiB, held on every GPU that
+ * loads the library until the process exits); nothing is allocated by this
+ * call.  It has no counterpart in the reference.
+ *   - n_patches <= WT_NOALLOC_MAX_PATCHES and total_wave_slots (the sum of the
+ *     patches' wave_count) <= WT_NOALLOC_MAX_WAVE_SLOTS, else
+ *     WT_ERR_INVALID_ARG;
+ *   - the first call on a device looks up the array's device address; make
+ *     that first call before any stream capture;
+ *   - every call on a device shares the one array, so calls that overlap on
+ *     the GPU (e.g. on two streams at once) race: order them on one stream;
+ *   - the first kernel of each call resets the array's queue and status words,
+ *     so no clearing is needed between calls; device-side validation results
+ *     are not reported (use wt_gerstner_displace to see them). */
+wt_status wt_gerstner_displace_noalloc(const wt_patch* patches, uint32_t n_patches,
+                                       uint64_t total_wave_slots,
+                                       const wt_wave* waves, uint32_t n_waves,
+                                       const wt_heightmap* hm,
+                                       float* pos_out, float* nrm_out, uint64_t out_capacity,
+                                       uint32_t flags, wt_stream stream);
+
 /* The same work issued as one launch pair per patch (no batching).  Exists to
  * measure the batched launch against; results are identical. */
 wt_status wt_gerstner_displace_unbatched(const wt_patch* host_patches,

@@ -1,0 +1,76 @@
+"""wt_gerstner_displace_noalloc: the entry point for callers that cannot
+allocate device memory (an engine or renderer plugin running inside a host
+application's frame, where the host owns every device buffer and a cudaMalloc
+could stall the device; a caller that only receives finished input and output
+buffers).  Its scratch is a fixed array inside the library instead of a
+caller-provided workspace.
+
+Checked through the C ABI against wt_gerstner_displace (which takes a
+workspace) on consecutive calls with different patch tables, so that scratch
+contents left by one call cannot leak into the next.  Collected last; it also
+passes alone in a fresh process (the first call on the device does the
+set-up)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import angle_deg, rel_err
+
+pytestmark = pytest.mark.gpu
+
+DISP_TOL = 1e-5
+ANGLE_TOL_DEG = 1e-2
+
+
+def _noalloc(wt, surf, pos, nrm, flags, n_patches=None, slots=None):
+    import torch
+    hm = surf.heightmap.cstruct() if surf.heightmap is not None else None
+    import ctypes as C
+    st = wt.lib().wt_gerstner_displace_noalloc(
+        surf.patches.data_ptr(), surf.n_patches if n_patches is None else n_patches,
+        surf.wave_slots if slots is None else slots, surf.waves.data_ptr(), surf.n_waves,
+        C.byref(hm) if hm is not None else None, pos.data_ptr(), nrm.data_ptr(), pos.shape[0], flags,
+        wt.stream_handle())
+    torch.cuda.synchronize()
+    return st
+
+
+def _compare(ref_pos, ref_nrm, pos, nrm):
+    a = pos.cpu().numpy().astype(np.float64)
+    b = ref_pos.cpu().numpy().astype(np.float64)
+    assert rel_err(a[:, :3], b[:, :3]) <= DISP_TOL
+    assert angle_deg(nrm.cpu().numpy()[:, :3].astype(np.float64),
+                     ref_nrm.cpu().numpy()[:, :3].astype(np.float64)).max() < ANGLE_TOL_DEG
+
+
+def test_noalloc_matches_workspace_entry_point_on_consecutive_calls(wt, gpu):
+    import torch
+    from wave_tool_gb300 import workloads
+    flags = wt.WT_OUT_DISPLACEMENT
+    cases = [workloads.config3(n_patches=16, seed=2), workloads.small_random(5, n_patches=7, side_range=(2, 200))]
+    surfs = [wt.Surface(w.patches, w.waves, wt.heightmap_from(w.heightmap)) for w in cases]
+    refs = []
+    for s in surfs:
+        p, n = s.displace(flags=flags)
+        refs.append((p.clone(), n.clone()))
+    torch.cuda.synchronize()
+    # A, B, then A again right after B: each call must see nothing of the last
+    for k in (0, 1, 0):
+        s = surfs[k]
+        pos, nrm = s.alloc_outputs(flags)
+        pos.fill_(float("nan"))
+        nrm.fill_(float("nan"))
+        assert _noalloc(wt, s, pos, nrm, flags) == 0, wt.lib().wt_last_error()
+        _compare(*refs[k], pos, nrm)
+
+
+def test_noalloc_rejects_sizes_beyond_its_limits(wt, gpu):
+    from wave_tool_gb300 import workloads
+    w = workloads.small_random(6, n_patches=2)
+    s = wt.Surface(w.patches, w.waves)
+    pos, nrm = s.alloc_outputs()
+    assert _noalloc(wt, s, pos, nrm, 0, n_patches=1025) == wt.abi.WT_ERR_INVALID_ARG
+    assert b"1024" in wt.lib().wt_last_error()
+    assert _noalloc(wt, s, pos, nrm, 0, slots=16385) == wt.abi.WT_ERR_INVALID_ARG
+    assert b"16384" in wt.lib().wt_last_error()

@@ -130,6 +130,11 @@ wt_status run_displace(const wt_patch* patches, uint32_t n_patches, const wt_wav
 
 }  // namespace
 
+namespace wt {
+void set_last_error(const char* msg) { g_last_error = msg; }
+FwdConfig forward_config() { return current_cfg(); }
+}  // namespace wt
+
 extern "C" {
 
 const char* wt_version(void) { return "wave-tool-gb300 0.1 (sm_103a)"; }

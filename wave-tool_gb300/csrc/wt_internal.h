@@ -104,6 +104,10 @@ cudaError_t launch_forward_naive(const wt_patch* patches, uint32_t n_patches, co
                                  cudaStream_t s);
 bool forward_config_supported(const FwdConfig& cfg);
 
+// ---- host helpers (wt_api.cpp) ---------------------------------------------
+void set_last_error(const char* msg);  // message returned by wt_last_error() on this thread
+FwdConfig forward_config();            // the forward launch tuning in effect
+
 // ---- misc kernels (wt_misc.cu) --------------------------------------------
 cudaError_t launch_indices(uint32_t cols, uint32_t rows, uint32_t base, uint32_t* out, cudaStream_t s);
 cudaError_t launch_noise(const wt_noise_term* terms, uint32_t n_terms, uint32_t w, uint32_t h,
