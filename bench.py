@@ -47,6 +47,8 @@ def parse_args():
     ap.add_argument("--patches", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
     ap.add_argument("--no-extras", action="store_true", help="skip the unbatched / single-patch side runs")
+    ap.add_argument("--tuning", default="auto",
+                    help="'auto' (autotune before timing) or WARPS,CHUNK to fix the launch shape")
     return ap.parse_args()
 
 
@@ -197,6 +199,12 @@ def run_ours(args):
     def step():
         surf.displace(pos, nrm, flags=flags)
 
+    if args.tuning == "auto":
+        tuning = surf.autotune(pos, nrm, flags=flags, reps=3)  # launch shape, before any timing
+    else:
+        w_, c_ = (int(x) for x in args.tuning.split(","))
+        wt.set_tuning(w_, 0, c_)
+        tuning = wt.get_tuning()
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -322,7 +330,8 @@ def run_ours(args):
                        "waves_per_patch": "8..64", "grid_side": "64..1024 log-uniform", "heightmap": "512^2 noise",
                        "outputs": "float4 displacement + float4 normal", "phase": "FP64-reduced",
                        "l2": "256 MiB buffer zeroed between timed steps (outside the per-step events)",
-                       "parallelism": f"weak x{world} (each GPU its own 256 patches)"},
+                       "parallelism": f"weak x{world} (each GPU its own 256 patches)",
+                       "tuning": tuning},
             "roofline": {"bound": "fma", "achieved": achieved / 1e9, "peak": peak_fma_terms / 1e9,
                          "unit": "Gterms/s", "frac": achieved / peak_fma_terms,
                          "traffic": traffic_from_profile(),

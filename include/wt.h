@@ -260,6 +260,32 @@ wt_status wt_wave_from_reference(float amplitude_A, float frequency_w,
                                  float dir_x, float dir_z, uint32_t wave_count,
                                  wt_wave* out);
 
+/* ---- launch tuning ------------------------------------------------------- */
+
+/* Launch shape of the persistent forward kernel.  Process-wide; applies to
+ * launches issued after it is set.  No reference counterpart (the reference
+ * has one fixed draw call). */
+typedef struct wt_tuning {
+    uint32_t warps_per_block; /* 4, 6, 8 or 16 (0 = default 8) */
+    uint32_t blocks_per_sm;   /* 0 = as many as fit */
+    uint32_t wave_chunk;      /* waves staged per warp at a time: 8, 16 or 32 (0 = 32) */
+    uint32_t reserved;        /* must be 0 */
+} wt_tuning;
+
+wt_status wt_set_tuning(const wt_tuning* tuning); /* NULL restores the defaults */
+wt_status wt_get_tuning(wt_tuning* tuning);
+
+/* Times every candidate launch shape on the given (device-resident) workload
+ * with `reps` launches each (CUDA events on `stream`, synchronising it),
+ * makes the fastest the process-wide tuning and returns it in *best (may be
+ * NULL).  Arguments as wt_gerstner_displace; the outputs are overwritten. */
+wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches,
+                               const wt_wave* waves, uint32_t n_waves,
+                               const wt_heightmap* hm,
+                               float* pos_out, float* nrm_out, uint64_t out_capacity,
+                               uint32_t flags, void* workspace, size_t workspace_bytes,
+                               uint32_t reps, wt_tuning* best, wt_stream stream);
+
 /* ---- measurement helpers ------------------------------------------------ */
 
 /* Measures this GPU's FP32 FMA rate (FMA/s) and MUFU sine rate (sin/s) with

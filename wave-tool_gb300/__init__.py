@@ -31,7 +31,7 @@ EXPORTED = [
     "wt_workspace_status", "wt_gerstner_displace", "wt_gerstner_displace_noalloc",
     "wt_gerstner_displace_unbatched",
     "wt_gerstner_adjoint", "wt_grid_indices", "wt_noise_synth", "wt_wave_from_reference",
-    "wt_measure_peaks",
+    "wt_measure_peaks", "wt_set_tuning", "wt_get_tuning", "wt_autotune_displace",
 ]
 
 
@@ -45,6 +45,11 @@ class CHeightmap(C.Structure):
     _fields_ = [("texels", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),
                 ("sample_scale", C.c_float), ("disp_scale", C.c_float), ("wrap", C.c_uint32),
                 ("_pad", C.c_uint32)]
+
+
+class CTuning(C.Structure):
+    _fields_ = [("warps_per_block", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("wave_chunk", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 class CWave(C.Structure):
@@ -84,6 +89,10 @@ def lib():
         L.wt_noise_synth.argtypes = [vp, u32, u32, u32, vp, vp, sz, vp]
         L.wt_wave_from_reference.argtypes = [C.c_float] * 6 + [u32, C.POINTER(CWave)]
         L.wt_measure_peaks.argtypes = [vp, sz, C.POINTER(C.c_double), C.POINTER(C.c_double), vp]
+        L.wt_set_tuning.argtypes = [C.POINTER(CTuning)]
+        L.wt_get_tuning.argtypes = [C.POINTER(CTuning)]
+        L.wt_autotune_displace.argtypes = [vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, u64, u32, vp, sz, u32,
+                                           C.POINTER(CTuning), vp]
         for name in EXPORTED:
             if name not in ("wt_version", "wt_last_error"):
                 getattr(L, name).restype = C.c_int
@@ -215,6 +224,17 @@ class Surface:
     def status(self, stream=None):
         return workspace_status(self.workspace, stream)
 
+    def autotune(self, pos, nrm, flags: int = 0, reps: int = 3, stream=None) -> dict:
+        """Times the candidate launch shapes on this surface and keeps the
+        fastest (process-wide)."""
+        hm = self.heightmap.cstruct() if self.heightmap is not None else None
+        best = CTuning()
+        check(lib().wt_autotune_displace(
+            self.patches.data_ptr(), self.n_patches, self.waves.data_ptr(), self.n_waves,
+            C.byref(hm) if hm is not None else None, pos.data_ptr(), _ptr(nrm), pos.shape[0], flags,
+            self.workspace.data_ptr(), self.workspace.numel(), reps, C.byref(best), stream_handle(stream)))
+        return {f: getattr(best, f) for f, _ in CTuning._fields_ if f != "reserved"}
+
 
 def grid_indices(cols: int, rows: int, base_vertex: int = 0, stream=None):
     torch = _torch()
@@ -243,6 +263,16 @@ def wave_from_reference(amplitude_A, frequency_w, phase_constant_phi, steepness_
     for n in WAVE_DTYPE.names:
         out[n] = getattr(w, n)
     return out
+
+
+def set_tuning(warps_per_block: int = 0, blocks_per_sm: int = 0, wave_chunk: int = 0) -> None:
+    check(lib().wt_set_tuning(C.byref(CTuning(warps_per_block, blocks_per_sm, wave_chunk, 0))))
+
+
+def get_tuning() -> dict:
+    t = CTuning()
+    check(lib().wt_get_tuning(C.byref(t)))
+    return {f: getattr(t, f) for f, _ in CTuning._fields_ if f != "reserved"}
 
 
 def measure_peaks(stream=None) -> tuple[float, float]:

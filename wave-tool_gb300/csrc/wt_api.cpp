@@ -252,6 +252,79 @@ wt_status wt_wave_from_reference(float amplitude_A, float frequency_w, float pha
     return WT_OK;
 }
 
+wt_status wt_set_tuning(const wt_tuning* t) {
+    wt::FwdConfig c = {8, 32, 8, 0};
+    if (t) {
+        if (t->reserved != 0) return fail(WT_ERR_INVALID_ARG, "tuning: reserved must be 0");
+        c.warps = t->warps_per_block ? (int)t->warps_per_block : 8;
+        c.blocks_per_sm = (int)t->blocks_per_sm;
+        c.chunk = t->wave_chunk ? (int)t->wave_chunk : 32;
+        if (!wt::forward_config_supported(c)) return fail(WT_ERR_INVALID_ARG, "tuning: warps_per_block must be 4, 6, 8 or 16");
+        if (c.chunk != 8 && c.chunk != 16 && c.chunk != 32) return fail(WT_ERR_INVALID_ARG, "tuning: wave_chunk must be 8, 16 or 32");
+        if (t->blocks_per_sm > 64) return fail(WT_ERR_INVALID_ARG, "tuning: blocks_per_sm > 64");
+    }
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_fwd_cfg = c;
+    return WT_OK;
+}
+
+wt_status wt_get_tuning(wt_tuning* t) {
+    if (!t) return fail(WT_ERR_INVALID_ARG, "tuning is NULL");
+    wt::FwdConfig c = current_cfg();
+    t->warps_per_block = (uint32_t)c.warps;
+    t->blocks_per_sm = (uint32_t)c.blocks_per_sm;
+    t->wave_chunk = (uint32_t)c.chunk;
+    t->reserved = 0;
+    return WT_OK;
+}
+
+wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
+                               const wt_heightmap* hm, float* pos_out, float* nrm_out, uint64_t out_capacity,
+                               uint32_t flags, void* workspace, size_t workspace_bytes, uint32_t reps,
+                               wt_tuning* best, wt_stream stream) {
+    if (reps == 0 || reps > 1000) return fail(WT_ERR_INVALID_ARG, "reps must be in [1, 1000]");
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaEvent_t e0, e1;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+    e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) { cudaEventDestroy(e0); return cuda_fail(e, "cudaEventCreate"); }
+    const int warps[] = {4, 6, 8, 16};
+    const int chunks[] = {8, 16, 32};
+    float best_ms = 1e30f;
+    wt::FwdConfig best_cfg = current_cfg();
+    wt_status st = WT_OK;
+    for (int w : warps) {
+        for (int ch : chunks) {
+            wt::FwdConfig c = {8, ch, w, 0};
+            st = run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags,
+                              workspace, workspace_bytes, s, c);
+            if (st != WT_OK) break;
+            cudaEventRecord(e0, s);
+            for (uint32_t r = 0; r < reps && st == WT_OK; ++r)
+                st = run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags,
+                                  workspace, workspace_bytes, s, c);
+            cudaEventRecord(e1, s);
+            e = cudaEventSynchronize(e1);
+            if (st != WT_OK) break;
+            if (e != cudaSuccess) { st = cuda_fail(e, "autotune timing"); break; }
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best_ms) { best_ms = ms; best_cfg = c; }
+        }
+        if (st != WT_OK) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != WT_OK) return st;
+    {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        g_fwd_cfg = best_cfg;
+    }
+    if (best) return wt_get_tuning(best);
+    return WT_OK;
+}
+
 wt_status wt_measure_peaks(void* scratch, size_t scratch_bytes, double* fma_per_s, double* sin_per_s,
                            wt_stream stream) {
     if (!scratch || !fma_per_s || !sin_per_s) return fail(WT_ERR_INVALID_ARG, "NULL argument");

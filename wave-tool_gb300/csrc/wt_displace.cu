@@ -81,6 +81,21 @@ __device__ uint32_t block_exclusive_scan(uint32_t* a, uint32_t n) {
     return carry;
 }
 
+// Tiling of one patch row: tiles of 32*S columns, S in 1..8, choosing the S
+// whose tiles cover the row with the least padding, with a preference for
+// larger S (each wave's start-up costs about as much as two vertices).
+__host__ __device__ __forceinline__ void row_tiling(uint32_t cols, uint32_t* S_out, uint32_t* tpr_out) {
+    uint32_t bestS = 8, bestT = (cols + 255) / 256;
+    float best = 256.0f * bestT * (1.0f + 2.0f / 8.0f);
+    for (uint32_t S = 7; S >= 1; --S) {
+        const uint32_t t = (cols + 32 * S - 1) / (32 * S);
+        const float cost = 32.0f * S * t * (1.0f + 2.0f / (float)S);
+        if (cost < best) { best = cost; bestS = S; bestT = t; }
+    }
+    *S_out = bestS;
+    *tpr_out = bestT;
+}
+
 // ---- stage 1: validation, prefix sums, LPT order ---------------------------
 __device__ __forceinline__ bool patch_ok(const wt_patch& P, uint32_t n_waves, uint64_t out_capacity) {
     const uint64_t verts = (uint64_t)P.cols * P.rows;
@@ -118,7 +133,9 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
         const bool ok = patch_ok(P, n_waves, out_capacity);
         if (!ok) flag_error(hdr, WT_ERR_INVALID_ARG, p);
         pair_off[p] = ok ? P.wave_count : 0u;
-        tiles[p] = ok ? P.rows * ((P.cols + tile_cols - 1) / tile_cols) : 0u;
+        uint32_t S, tpr;
+        row_tiling(P.cols, &S, &tpr);
+        tiles[p] = ok ? P.rows * tpr : 0u;
         const uint32_t key = P.wave_count < kSortBins ? P.wave_count : kSortBins - 1;
         atomicAdd(&bins[kSortBins - 1 - key], 1u);  // descending wave count
     }
@@ -295,19 +312,26 @@ __device__ __forceinline__ int mirror_index(int m, int n) {
     return n - 1 - (a >= 0 ? a : -(1 + a));
 }
 
-__device__ __forceinline__ Footprint footprint(float x, int n, uint32_t mode) {
+__device__ __forceinline__ Footprint footprint(float x, int n, uint32_t mode, bool pow2) {
     const bool mir = mode == WT_WRAP_MIRRORED_REPEAT;
     const int P = mir ? 2 * n : n;
-    const float Pf = (float)P;
-    const float r = x - Pf * floorf(x * (1.0f / Pf));
-    const float fi = floorf(r);
     Footprint f;
-    f.w = r - fi;
-    int i0 = __float2int_rd(r);
-    i0 += i0 < 0 ? P : 0;
-    i0 -= i0 >= P ? P : 0;
-    i0 = min(max(i0, 0), P - 1);
-    int i1 = i0 + 1 == P ? 0 : i0 + 1;
+    int i0;
+    if (pow2) {
+        // power-of-two sizes: the wrap is a mask; the saturating conversion
+        // keeps any input (NaN -> 0) in range
+        f.w = x - floorf(x);
+        i0 = __float2int_rd(x) & (P - 1);
+    } else {
+        const float Pf = (float)P;
+        const float r = x - Pf * floorf(x * (1.0f / Pf));
+        f.w = r - floorf(r);
+        i0 = __float2int_rd(r);
+        i0 += i0 < 0 ? P : 0;
+        i0 -= i0 >= P ? P : 0;
+        i0 = min(max(i0, 0), P - 1);
+    }
+    const int i1 = i0 + 1 == P ? 0 : i0 + 1;
     f.i0 = mir ? mirror_index(i0, n) : i0;
     f.i1 = mir ? mirror_index(i1, n) : i1;
     return f;
@@ -319,7 +343,7 @@ struct VertexSums {
 
 // Heightmap, bounce, normal, stores for one vertex.
 __device__ __forceinline__ void finish_vertex(const VertexSums& s, float xl, float zl, const PatchAux& a,
-                                              const HmDev& hm, uint64_t vidx,
+                                              const HmDev& hm, bool pow2, uint64_t vidx,
                                               float* __restrict__ pos, float* __restrict__ nrm,
                                               uint32_t flags) {
     float px0 = 1.0f - s.sxx, px1 = s.jx, px2 = -s.sxz;
@@ -329,7 +353,7 @@ __device__ __forceinline__ void finish_vertex(const VertexSums& s, float xl, flo
         const float ut = fmaf(a.su, xl + s.dx, a.hu0);
         const float vt = fmaf(a.sv, zl + s.dz, a.hv0);
         const int W = (int)hm.width, H = (int)hm.height;
-        const Footprint fu = footprint(ut, W, hm.wrap), fv = footprint(vt, H, hm.wrap);
+        const Footprint fu = footprint(ut, W, hm.wrap, pow2), fv = footprint(vt, H, hm.wrap, pow2);
         const float al = fu.w, be = fv.w;
         const int ia = fu.i0, ib = fu.i1, ja = fv.i0, jb = fv.i1;
         float t00 = __ldg(hm.texels + ja * W + ia), t10 = __ldg(hm.texels + ja * W + ib);
@@ -371,15 +395,62 @@ __device__ __forceinline__ uint32_t hi32_round(unsigned long long x) {
 }
 
 // ---- stage 3: the persistent forward kernel --------------------------------
-template <int S, int THREADS, int MINB>
+// Per-wave staging in shared memory (3 float4 per wave, up to 32 waves per warp):
+//   [0] t32, a32 (fixed-point turns), cos d, sin d      d = one 32-column step
+//   [1] Q*A*Dx, A, Q*A*Dz, A*k*Dx
+//   [2] A*k*Dz, Q*A*k*Dx^2, Q*A*k*Dx*Dz, Q*A*k*Dz^2
+// Lane l's vertices j = 0..S-1 sit at columns c0 + l + 32 j.  Vertex 0 takes
+// a MUFU sincos of its exact start phase, vertex 1 an exact rotation by d, and
+// vertices j >= 2 the Chebyshev recurrence x[j] = 2 cos(d) x[j-1] - x[j-2]
+// (one FMA per value; its error grows at most linearly in j).
+constexpr int kStage = 3;
+
+// The wave loop of one tile for a compile-time S: sums of nw staged waves
+// into acc[0..S-1].
+template <int S>
+__device__ __forceinline__ void wave_loop(float (&acc)[8][8], const float4* __restrict__ wst, uint32_t nw,
+                                          uint32_t lane) {
+#pragma unroll 2
+    for (uint32_t i = 0; i < nw; ++i) {
+        const float4 w0v = wst[kStage * i];
+        const float4 w1 = wst[kStage * i + 1];
+        const float4 w2 = wst[kStage * i + 2];
+        const uint32_t tl = __float_as_uint(w0v.x) + lane * __float_as_uint(w0v.y);
+        const float ang = (float)(int)tl * kTurnToRad;
+        const float cd = w0v.z, sd = w0v.w, tc = 2.0f * cd;
+        float c, s, cp = 0.0f, sp = 0.0f;
+        __sincosf(ang, &s, &c);
+#pragma unroll
+        for (int j = 0; j < S; ++j) {
+            if (j == 1) {
+                const float cn = fmaf(c, cd, -s * sd);
+                const float sn = fmaf(s, cd, c * sd);
+                cp = c; sp = s; c = cn; s = sn;
+            } else if (j >= 2) {
+                const float cn = fmaf(tc, c, -cp);
+                const float sn = fmaf(tc, s, -sp);
+                cp = c; sp = s; c = cn; s = sn;
+            }
+            acc[j][0] = fmaf(w1.x, c, acc[j][0]);
+            acc[j][1] = fmaf(w1.y, s, acc[j][1]);
+            acc[j][2] = fmaf(w1.z, c, acc[j][2]);
+            acc[j][3] = fmaf(w1.w, c, acc[j][3]);
+            acc[j][4] = fmaf(w2.x, c, acc[j][4]);
+            acc[j][5] = fmaf(w2.y, s, acc[j][5]);
+            acc[j][6] = fmaf(w2.z, s, acc[j][6]);
+            acc[j][7] = fmaf(w2.w, s, acc[j][7]);
+        }
+    }
+}
+
+template <int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB)
 k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ pos,
-          float* __restrict__ nrm, uint32_t flags, char* __restrict__ ws, WsLayout L) {
+          float* __restrict__ nrm, uint32_t flags, char* __restrict__ ws, WsLayout L, uint32_t chunk) {
 #if __CUDA_ARCH__ >= 900
     cudaGridDependencySynchronize();
 #endif
-    constexpr int TILE = 32 * S;
-    __shared__ float4 stage[THREADS / 32][32 * 3];
+    __shared__ float4 stage[THREADS / 32][32 * kStage];
     WsHeader* hdr = reinterpret_cast<WsHeader*>(ws);
     const uint32_t* sorted = reinterpret_cast<const uint32_t*>(ws + L.sorted);
     const uint32_t* tile_pre = reinterpret_cast<const uint32_t*>(ws + L.tile_pre);
@@ -389,44 +460,55 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
     float4* wst = stage[threadIdx.x >> 5];
     const uint32_t n = hdr->n_patches;
     const uint32_t total = hdr->total_tiles;
+    const bool pow2 = hm.present && (hm.width & (hm.width - 1)) == 0 && (hm.height & (hm.height - 1)) == 0;
 
-    for (;;) {
-        uint32_t t = 0;
-        if (lane == 0) t = atomicAdd(&hdr->tile_counter, 1u);
-        t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= total) break;
-        uint32_t lo = 0, hi = n + 1;
-        while (lo < hi) {
-            uint32_t mid = (lo + hi) >> 1;
-            if (tile_pre[mid] <= t) lo = mid + 1; else hi = mid;
+    // The queue index of the next tile is fetched while the current one runs;
+    // the tile's patch is searched forward from the previous tile's (tiles
+    // come out of the queue in increasing order), galloping when it is far.
+    uint32_t t_next = 0;
+    if (lane == 0) t_next = atomicAdd(&hdr->tile_counter, 1u);
+    uint32_t t = __shfl_sync(0xffffffffu, t_next, 0);
+    uint32_t q = 0;
+    while (t < total) {
+        if (lane == 0) t_next = atomicAdd(&hdr->tile_counter, 1u);
+        if (tile_pre[q + 1] <= t) {
+            uint32_t step = 1, lo = q + 1, hi = q + 2;
+            while (hi <= n && tile_pre[hi] <= t) { lo = hi; step <<= 1; hi = lo + step; }
+            hi = min(hi, n + 1);
+            while (hi - lo > 1) {  // tile_pre[lo] <= t < tile_pre[hi]
+                const uint32_t mid = (lo + hi) >> 1;
+                if (tile_pre[mid] <= t) lo = mid; else hi = mid;
+            }
+            q = lo;
         }
-        const uint32_t q = lo - 1;
         const uint32_t p = sorted[q];
         const uint32_t lt = t - tile_pre[q];
         const uint32_t cols = patches[p].cols;
         const uint32_t nwaves = patches[p].wave_count;
         const uint64_t out0 = patches[p].out_offset;
         const PatchAux a = aux[p];
-        const uint32_t tpr = (cols + TILE - 1) / TILE;
+        uint32_t S, tpr;
+        row_tiling(cols, &S, &tpr);
         const uint32_t row = lt / tpr;
-        const uint32_t c0 = (lt - row * tpr) * TILE;
+        const uint32_t c0 = (lt - row * tpr) * 32u * S;
 
-        float acc[S][8];
+        float acc[8][8];
 #pragma unroll
-        for (int j = 0; j < S; ++j)
+        for (int j = 0; j < 8; ++j)
 #pragma unroll
             for (int m = 0; m < 8; ++m) acc[j][m] = 0.0f;
 
-        for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
-            const uint32_t nw = min(32u, nwaves - w0);
+        for (uint32_t w0 = 0; w0 < nwaves; w0 += chunk) {
+            const uint32_t nw = min(chunk, nwaves - w0);
             __syncwarp();
             if ((uint32_t)lane < nw) {
                 const PairCoef c = coef[a.pair_offset + w0 + lane];
                 // phase of this wave at (c0, row) and its per-column step on this row
-                unsigned long long t64 = c.t00 + (unsigned long long)c0 * c.ta + (unsigned long long)row * c.tb +
-                                         (unsigned long long)c0 * row * c.tg;
-                unsigned long long a64 = c.ta + (unsigned long long)row * c.tg;
-                uint32_t t32 = hi32_round(t64), a32 = hi32_round(a64), d32 = hi32_round(a64 * 32ull);
+                const unsigned long long t64 = c.t00 + (unsigned long long)c0 * c.ta +
+                                               (unsigned long long)row * c.tb +
+                                               (unsigned long long)c0 * row * c.tg;
+                const unsigned long long a64 = c.ta + (unsigned long long)row * c.tg;
+                const uint32_t t32 = hi32_round(t64), a32 = hi32_round(a64), d32 = hi32_round(a64 * 32ull);
                 // rotation by the 32-column step: sincospi of the high part
                 // (exact in FP32), then a first-order turn by the low 8 bits
                 const uint32_t dhi = d32 & 0xffffff00u;
@@ -436,54 +518,40 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
                 const float cdn = fmaf(-sd, eps, cd);
                 sd = fmaf(cd, eps, sd);
                 cd = cdn;
-                wst[3 * lane] = make_float4(__uint_as_float(t32), __uint_as_float(a32), cd, sd);
-                wst[3 * lane + 1] = make_float4(c.qadx, c.a, c.qadz, c.akdx);
-                wst[3 * lane + 2] = make_float4(c.akdz, c.qakxx, c.qakxz, c.qakzz);
+                wst[kStage * lane] = make_float4(__uint_as_float(t32), __uint_as_float(a32), cd, sd);
+                wst[kStage * lane + 1] = make_float4(c.qadx, c.a, c.qadz, c.akdx);
+                wst[kStage * lane + 2] = make_float4(c.akdz, c.qakxx, c.qakxz, c.qakzz);
             }
             __syncwarp();
-            for (uint32_t i = 0; i < nw; ++i) {
-                const float4 w0v = wst[3 * i];
-                const float4 w1 = wst[3 * i + 1];
-                const float4 w2 = wst[3 * i + 2];
-                uint32_t tl = __float_as_uint(w0v.x) + (uint32_t)lane * __float_as_uint(w0v.y);
-                float ang = (float)(int)tl * kTurnToRad;
-                float s, c;
-                __sincosf(ang, &s, &c);
-                const float cd = w0v.z, sd = w0v.w;
-#pragma unroll
-                for (int j = 0; j < S; ++j) {
-                    if (j > 0) {
-                        float cn = fmaf(c, cd, -s * sd);
-                        float sn = fmaf(s, cd, c * sd);
-                        c = cn;
-                        s = sn;
-                    }
-                    acc[j][0] = fmaf(w1.x, c, acc[j][0]);
-                    acc[j][1] = fmaf(w1.y, s, acc[j][1]);
-                    acc[j][2] = fmaf(w1.z, c, acc[j][2]);
-                    acc[j][3] = fmaf(w1.w, c, acc[j][3]);
-                    acc[j][4] = fmaf(w2.x, c, acc[j][4]);
-                    acc[j][5] = fmaf(w2.y, s, acc[j][5]);
-                    acc[j][6] = fmaf(w2.z, s, acc[j][6]);
-                    acc[j][7] = fmaf(w2.w, s, acc[j][7]);
-                }
+            switch (S) {  // warp-uniform
+                case 1: wave_loop<1>(acc, wst, nw, lane); break;
+                case 2: wave_loop<2>(acc, wst, nw, lane); break;
+                case 3: wave_loop<3>(acc, wst, nw, lane); break;
+                case 4: wave_loop<4>(acc, wst, nw, lane); break;
+                case 5: wave_loop<5>(acc, wst, nw, lane); break;
+                case 6: wave_loop<6>(acc, wst, nw, lane); break;
+                case 7: wave_loop<7>(acc, wst, nw, lane); break;
+                default: wave_loop<8>(acc, wst, nw, lane); break;
             }
         }
 
+        // grid position along the row: x(col) = col * du * (e1 + v e3) + v e2
         const float v = (float)row * a.inv_rm1;
+        const float gx = (a.e1x + v * a.e3x) * a.inv_cm1, gz = (a.e1z + v * a.e3z) * a.inv_cm1;
+        const float colf = (float)(c0 + lane);
+        const float xb = fmaf(colf, gx, v * a.e2x), zb = fmaf(colf, gz, v * a.e2z);
         const uint64_t rowbase = out0 + (uint64_t)row * cols;
 #pragma unroll
-        for (int j = 0; j < S; ++j) {
+        for (int j = 0; j < 8; ++j) {
             const uint32_t col = c0 + lane + 32 * j;
-            if (col < cols) {
-                const float u = (float)col * a.inv_cm1;
-                const float uv = u * v;
-                const float xl = fmaf(u, a.e1x, fmaf(v, a.e2x, uv * a.e3x));
-                const float zl = fmaf(u, a.e1z, fmaf(v, a.e2z, uv * a.e3z));
+            if ((uint32_t)j < S && col < cols) {
+                const float xl = fmaf(32.0f * j, gx, xb);
+                const float zl = fmaf(32.0f * j, gz, zb);
                 VertexSums s{acc[j][0], acc[j][1], acc[j][2], acc[j][3], acc[j][4], acc[j][5], acc[j][6], acc[j][7]};
-                finish_vertex(s, xl, zl, a, hm, rowbase + col, pos, nrm, flags);
+                finish_vertex(s, xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags);
             }
         }
+        t = __shfl_sync(0xffffffffu, t_next, 0);
     }
 }
 
@@ -498,6 +566,7 @@ __global__ void __launch_bounds__(256) k_forward_naive(const wt_patch* __restric
     const PatchAux* aux = reinterpret_cast<const PatchAux*>(ws + L.aux);
     const uint32_t* tile_pre = reinterpret_cast<const uint32_t*>(ws + L.tile_pre);
     const uint32_t* sorted = reinterpret_cast<const uint32_t*>(ws + L.sorted);
+    const bool pow2 = hm.present && (hm.width & (hm.width - 1)) == 0 && (hm.height & (hm.height - 1)) == 0;
     for (uint32_t q = 0; q < n; ++q) {
         if (tile_pre[q + 1] == tile_pre[q]) continue;  // invalid patch
         const uint32_t p = sorted[q];
@@ -527,26 +596,29 @@ __global__ void __launch_bounds__(256) k_forward_naive(const wt_patch* __restric
                 s.sxz += Q * A * k * w.dir_x * w.dir_z * sn;
                 s.szz += Q * A * k * w.dir_z * w.dir_z * sn;
             }
-            finish_vertex(s, xl, zl, a, hm, P.out_offset + v, pos, nrm, flags);
+            finish_vertex(s, xl, zl, a, hm, pow2, P.out_offset + v, pos, nrm, flags);
         }
     }
 }
 
-template <int S, int THREADS, int MINB>
+template <int THREADS, int MINB>
 cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const HmDev& hm, float* pos,
                          float* nrm, uint32_t flags, void* ws, const WsLayout& L, cudaStream_t s) {
-    static int sms = -1;
-    static int occ = -1;
-    if (sms < 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_forward<S, THREADS, MINB>, THREADS, 0);
-        if (occ < 1) occ = 1;
+    constexpr int kMaxDev = 64;
+    static int sms[kMaxDev] = {}, occ[kMaxDev] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+    if (sms[dev] == 0) {
+        int o = 0, m = 0;
+        cudaDeviceGetAttribute(&m, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_forward<THREADS, MINB>, THREADS, 0);
+        occ[dev] = o < 1 ? 1 : o;
+        sms[dev] = m;
     }
-    int bps = cfg.blocks_per_sm > 0 ? (cfg.blocks_per_sm < occ ? cfg.blocks_per_sm : occ) : occ;
+    const int bps = cfg.blocks_per_sm > 0 ? (cfg.blocks_per_sm < occ[dev] ? cfg.blocks_per_sm : occ[dev]) : occ[dev];
     cudaLaunchConfig_t lc = {};
-    lc.gridDim = dim3((unsigned)(sms * bps));
+    lc.gridDim = dim3((unsigned)(sms[dev] * bps));
     lc.blockDim = dim3(THREADS);
     lc.dynamicSmemBytes = 0;
     lc.stream = s;
@@ -555,8 +627,9 @@ cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const Hm
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     lc.attrs = attr;
     lc.numAttrs = 1;
-    return cudaLaunchKernelEx(&lc, k_forward<S, THREADS, MINB>, patches, hm, pos, nrm, flags,
-                              static_cast<char*>(ws), L);
+    const uint32_t chunk = cfg.chunk >= 1 && cfg.chunk <= 32 ? (uint32_t)cfg.chunk : 32u;
+    return cudaLaunchKernelEx(&lc, k_forward<THREADS, MINB>, patches, hm, pos, nrm, flags, static_cast<char*>(ws), L,
+                              chunk);
 }
 
 }  // namespace
@@ -590,16 +663,17 @@ cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wa
 }
 
 bool forward_config_supported(const FwdConfig& c) {
-    return (c.s == 8 && (c.warps == 8 || c.warps == 4)) || (c.s == 4 && (c.warps == 8 || c.warps == 4));
+    return c.warps == 8 || c.warps == 6 || c.warps == 4 || c.warps == 16;
 }
 
 cudaError_t launch_forward(const FwdConfig& cfg, const wt_patch* patches, uint32_t, const HmDev& hm,
                            float* pos, float* nrm, uint32_t flags, void* ws, const WsLayout& L,
                            cudaStream_t s) {
-    if (cfg.s == 8 && cfg.warps == 8) return launch_fwd_t<8, 256, 2>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
-    if (cfg.s == 8 && cfg.warps == 4) return launch_fwd_t<8, 128, 4>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
-    if (cfg.s == 4 && cfg.warps == 8) return launch_fwd_t<4, 256, 3>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
-    if (cfg.s == 4 && cfg.warps == 4) return launch_fwd_t<4, 128, 6>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
+    // warps per block; the minimum-blocks hint sets the register budget
+    if (cfg.warps == 8) return launch_fwd_t<256, 2>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 128 regs
+    if (cfg.warps == 6) return launch_fwd_t<192, 2>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 168 regs
+    if (cfg.warps == 4) return launch_fwd_t<128, 3>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 168 regs
+    if (cfg.warps == 16) return launch_fwd_t<512, 1>(cfg, patches, hm, pos, nrm, flags, ws, L, s);  // 128 regs
     return cudaErrorInvalidValue;
 }
 
