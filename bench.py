@@ -200,7 +200,7 @@ def run_ours(args):
         surf.displace(pos, nrm, flags=flags)
 
     if args.tuning == "auto":
-        tuning = surf.autotune(pos, nrm, flags=flags, reps=3)  # launch shape, before any timing
+        tuning = surf.autotune(pos, nrm, flags=flags, reps=5)  # launch shape, before any timing
     else:
         w_, c_ = (int(x) for x in args.tuning.split(","))
         wt.set_tuning(w_, 0, c_)

@@ -294,6 +294,7 @@ wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches, cons
     float best_ms = 1e30f;
     wt::FwdConfig best_cfg = current_cfg();
     wt_status st = WT_OK;
+    for (int pass = 0; pass < 2 && st == WT_OK; ++pass)
     for (int w : warps) {
         for (int ch : chunks) {
             wt::FwdConfig c = {8, ch, w, 0};
