@@ -219,12 +219,17 @@ wt_status wt_gerstner_displace_unbatched(const wt_patch* host_patches,
                                          void* workspace, size_t workspace_bytes,
                                          wt_stream stream);
 
-/* Vector-Jacobian product of wt_gerstner_displace: given dL/dpos (float4 per
- * vertex, w ignored) and dL/dnrm (float4 per vertex or NULL), writes dL/dwave
- * for every wave (device array of n_waves).  Deterministic: per-tile partial
- * sums are reduced in a fixed order.  No reference counterpart (the reference
- * has no derivatives); the forward it differentiates is water-grid.vert:74-111. */
-wt_status wt_gerstner_adjoint(const wt_patch* patches, uint32_t n_patches,
+/* Vector-Jacobian product of wt_gerstner_displace: given dL/dpos (per
+ * vertex, the layout flag selects float4 or packed vec3; w ignored) and
+ * dL/dnrm (same layout, or NULL), writes dL/dwave for every wave (device
+ * array grad_out of n_waves; waves no patch uses get zeros; patches that share
+ * a wave add up).  The gradient is the same for world and displacement
+ * outputs.  `host_patches` is a host copy of the device patch table (the
+ * per-tile partial sums are laid out from it; wt_adjoint_workspace_size gives
+ * the workspace).  Deterministic: per-tile FP32 partial sums are reduced in
+ * FP64 in a fixed order.  No reference counterpart (the reference has no
+ * derivatives); the forward it differentiates is water-grid.vert:74-111. */
+wt_status wt_gerstner_adjoint(const wt_patch* host_patches, const wt_patch* patches, uint32_t n_patches,
                               const wt_wave* waves, uint32_t n_waves,
                               const wt_heightmap* hm,
                               const float* d_pos, const float* d_nrm, uint64_t out_capacity,

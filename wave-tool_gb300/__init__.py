@@ -83,8 +83,8 @@ def lib():
                                                    vp]
         L.wt_gerstner_displace_unbatched.argtypes = [vp, vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, u64,
                                                      u32, vp, sz, vp]
-        L.wt_gerstner_adjoint.argtypes = [vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, u64, u32, vp, vp,
-                                          sz, vp]
+        L.wt_gerstner_adjoint.argtypes = [vp, vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, u64, u32, vp,
+                                          vp, sz, vp]
         L.wt_grid_indices.argtypes = [u32, u32, u32, vp, vp]
         L.wt_noise_synth.argtypes = [vp, u32, u32, u32, vp, vp, sz, vp]
         L.wt_wave_from_reference.argtypes = [C.c_float] * 6 + [u32, C.POINTER(CWave)]
@@ -223,6 +223,28 @@ class Surface:
 
     def status(self, stream=None):
         return workspace_status(self.workspace, stream)
+
+    def adjoint(self, d_pos, d_nrm=None, flags: int = 0, grad=None, stream=None):
+        """dL/dwave (n_waves x 8 float32 tensor, the wt_wave_grad fields) for
+        upstream gradients d_pos / d_nrm laid out like the outputs."""
+        torch = _torch()
+        if getattr(self, "adj_workspace", None) is None:
+            self.adj_workspace = empty_bytes(adjoint_workspace_bytes(self.host_patches), self.patches.device)
+        if grad is None:
+            grad = torch.empty((self.n_waves, 8), dtype=torch.float32, device=self.patches.device)
+        hm = self.heightmap.cstruct() if self.heightmap is not None else None
+        check(lib().wt_gerstner_adjoint(
+            self.host_patches.ctypes.data, self.patches.data_ptr(), self.n_patches, self.waves.data_ptr(),
+            self.n_waves, C.byref(hm) if hm is not None else None, d_pos.data_ptr(), _ptr(d_nrm), d_pos.shape[0],
+            flags, grad.data_ptr(), self.adj_workspace.data_ptr(), self.adj_workspace.numel(),
+            stream_handle(stream)))
+        return grad
+
+    def set_waves(self, waves: np.ndarray) -> None:
+        """Replace the wave parameters (same count) in place on the device."""
+        assert waves.dtype == WAVE_DTYPE and len(waves) == self.n_waves
+        self.host_waves = np.ascontiguousarray(waves)
+        self.waves.copy_(to_device(self.host_waves, self.patches.device))
 
     def autotune(self, pos, nrm, flags: int = 0, reps: int = 3, stream=None) -> dict:
         """Times the candidate launch shapes on this surface and keeps the

@@ -1,0 +1,447 @@
+// wt_adjoint.cu — vector-Jacobian product of the forward path with respect
+// to every wave's parameters (no reference counterpart; the forward it
+// differentiates is water-grid.vert:74-111, see wt_displace.cu).
+//
+// After the shared prep stages (validation, LPT order, FP64 phase constants):
+//   k_adj_scan   (1 block)   rank of each patch, prefix of (tile, wave) records
+//   k_adjoint    (persistent) per tile:
+//       phase 1, one vertex per lane (as the forward): recompute the eight
+//       wave sums, the heightmap sample and the normal, and turn dL/dpos and
+//       dL/dnrm into the adjoints of the eight sums; park them with the
+//       vertex's local grid position in shared memory;
+//       phase 2, one wave per lane: walk the tile's vertices (broadcast from
+//       shared memory), regenerate the wave's sin/cos there (MUFU start +
+//       Chebyshev steps) and accumulate 11 per-wave moments; write them as
+//       the tile's record for that wave (no cross-lane reduction).
+//   k_adj_pairs  one warp per (patch, wave): FP64 sum of the patch's records
+//                in tile order, then the closed-form gradient in FP64.
+//   k_adj_waves  one thread per wave: sum over the patches that use it, in
+//                patch order.
+// Every sum has a fixed order, so the result is bitwise reproducible.
+//
+// With g_q the adjoint of sum q per vertex and (c, s) the wave's cos/sin
+// there, the records hold M_q = sum g_q c (q = dx, dz, jx, jz) or
+// sum g_q s (q = dy, sxx, sxz, szz), T0 = sum g_theta, Tx = sum g_theta x,
+// Tz = sum g_theta z, where g_theta = u_s c - u_c s is the adjoint of the
+// phase.  All parameter gradients follow from these eleven sums.
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "wt_device.cuh"
+#include "wt_internal.h"
+
+namespace wt {
+namespace {
+
+using namespace wt::dev;
+
+constexpr int kAdjWarps = 4;                 // warps per block
+constexpr int kGbufVerts = 256;              // vertices per tile (32 lanes x S <= 8)
+constexpr int kGbufF4 = 3;                   // float4 per parked vertex
+
+__global__ void __launch_bounds__(1024) k_adj_scan(const wt_patch* __restrict__ patches, uint32_t n, char* ws,
+                                                   AdjLayout L) {
+#if __CUDA_ARCH__ >= 900
+    cudaGridDependencySynchronize();
+#endif
+    WsHeader* hdr = reinterpret_cast<WsHeader*>(ws);
+    const uint32_t* sorted = reinterpret_cast<const uint32_t*>(ws + L.f.sorted);
+    const uint32_t* tile_pre = reinterpret_cast<const uint32_t*>(ws + L.f.tile_pre);
+    const uint32_t* pair_off = reinterpret_cast<const uint32_t*>(ws + L.f.pair_off);
+    uint32_t* rank = reinterpret_cast<uint32_t*>(ws + L.rank);
+    uint32_t* part_off = reinterpret_cast<uint32_t*>(ws + L.part_off);
+    for (uint32_t q = threadIdx.x; q < n; q += blockDim.x) {
+        const uint32_t p = sorted[q];
+        rank[p] = q;
+        const uint64_t rec = (uint64_t)(tile_pre[q + 1] - tile_pre[q]) * (pair_off[p + 1] - pair_off[p]);
+        part_off[q] = rec > 0xffffffffull ? 0xffffffffu : (uint32_t)rec;
+    }
+    __syncthreads();
+    const uint32_t total = block_exclusive_scan(part_off, n);
+    if (threadIdx.x == 0) {
+        part_off[n] = total;
+        if ((uint64_t)total > L.cap_records || total == 0xffffffffu) {
+            // the device patches need more records than the host copy said
+            atomicCAS(&hdr->status, 0u, (uint32_t)WT_ERR_NOMEM);
+            hdr->total_tiles = 0;
+        }
+    }
+}
+
+// Adjoints of the eight sums at one vertex.  Order: dx, dy, dz, jx, jz, sxx,
+// sxz, szz.  See oracle/gerstner_f64.c:wto_adjoint_f64 for the same algebra.
+__device__ __forceinline__ void vertex_adjoint(const VertexSums& s, float xl, float zl, const PatchAux& a,
+                                               const HmDev& hm, bool pow2, const float* __restrict__ gpos,
+                                               const float* __restrict__ gnrm, uint64_t vidx, bool vec3,
+                                               float g[8]) {
+    const float a1 = 1.0f - s.sxx, a3 = -s.sxz, b1 = -s.sxz, b3 = 1.0f - s.szz;
+    HmSample h = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (hm.present) h = hm_sample(hm, a, xl + s.dx, zl + s.dz, pow2);
+    const float px0 = a1, px1 = fmaf(h.hx, a1, fmaf(h.hz, a3, s.jx)), px2 = a3;
+    const float pz0 = b1, pz1 = fmaf(h.hx, b1, fmaf(h.hz, b3, s.jz)), pz2 = b3;
+    const float* gp = gpos + (vec3 ? 3 : 4) * vidx;
+    const float gpx_ = gp[0], gpy_ = gp[1], gpz_ = gp[2];
+    float gPx0 = 0.0f, gPx1 = 0.0f, gPx2 = 0.0f, gPz0 = 0.0f, gPz1 = 0.0f, gPz2 = 0.0f;
+    if (gnrm) {
+        const float* gn = gnrm + (vec3 ? 3 : 4) * vidx;
+        const float N0 = pz1 * px2 - pz2 * px1, N1 = pz2 * px0 - pz0 * px2, N2 = pz0 * px1 - pz1 * px0;
+        const float inv = rsqrtf(fmaf(N0, N0, fmaf(N1, N1, N2 * N2)));
+        const float n0 = N0 * inv, n1 = N1 * inv, n2 = N2 * inv;
+        const float d = fmaf(n0, gn[0], fmaf(n1, gn[1], n2 * gn[2]));
+        const float gN0 = (gn[0] - n0 * d) * inv, gN1 = (gn[1] - n1 * d) * inv, gN2 = (gn[2] - n2 * d) * inv;
+        // N = Pz x Px:  g_Pz = Px x gN,  g_Px = gN x Pz
+        gPz0 = px1 * gN2 - px2 * gN1;
+        gPz1 = px2 * gN0 - px0 * gN2;
+        gPz2 = px0 * gN1 - px1 * gN0;
+        gPx0 = gN1 * pz2 - gN2 * pz1;
+        gPx1 = gN2 * pz0 - gN0 * pz2;
+        gPx2 = gN0 * pz1 - gN1 * pz0;
+    }
+    const float g_a1 = fmaf(gPx1, h.hx, gPx0), g_a3 = fmaf(gPx1, h.hz, gPx2);
+    const float g_b1 = fmaf(gPz1, h.hx, gPz0), g_b3 = fmaf(gPz1, h.hz, gPz2);
+    const float g_hx = fmaf(gPx1, a1, gPz1 * b1), g_hz = fmaf(gPx1, a3, gPz1 * b3);
+    const float g_X = fmaf(gpy_, h.hx, g_hz * h.hxz), g_Z = fmaf(gpy_, h.hz, g_hx * h.hxz);
+    g[0] = gpx_ + g_X;        // dx
+    g[1] = gpy_;              // dy
+    g[2] = gpz_ + g_Z;        // dz
+    g[3] = gPx1;              // jx
+    g[4] = gPz1;              // jz
+    g[5] = -g_a1;             // sxx
+    g[6] = -g_a3 - g_b1;      // sxz
+    g[7] = -g_b3;             // szz
+}
+
+// Phase 2 for a compile-time S: lane = one wave; vertices l + 32 j of the tile.
+template <int S>
+__device__ __forceinline__ void wave_moments(const float4* __restrict__ gbuf, uint32_t nvalid, uint32_t t32,
+                                             uint32_t a32, float cd, float sd, const PairCoef& k, float m[11]) {
+    const float tc = 2.0f * cd;
+    for (uint32_t l = 0; l < 32; ++l) {
+        if (l >= nvalid) break;  // columns past the row end (nvalid = valid lanes of vertex 0)
+        const uint32_t tl = t32 + l * a32;
+        float s, c, cp = 0.0f, sp = 0.0f;
+        __sincosf((float)(int)tl * kTurnToRad, &s, &c);
+#pragma unroll
+        for (int j = 0; j < S; ++j) {
+            if (j == 1) {
+                const float cn = fmaf(c, cd, -s * sd), sn = fmaf(s, cd, c * sd);
+                cp = c; sp = s; c = cn; s = sn;
+            } else if (j >= 2) {
+                const float cn = fmaf(tc, c, -cp), sn = fmaf(tc, s, -sp);
+                cp = c; sp = s; c = cn; s = sn;
+            }
+            const float4* v = gbuf + kGbufF4 * (l + 32 * j);
+            const float4 g0 = v[0], g1 = v[1], g2 = v[2];  // dx dy dz jx | jz sxx sxz szz | x z - -
+            m[0] = fmaf(g0.x, c, m[0]);
+            m[1] = fmaf(g0.y, s, m[1]);
+            m[2] = fmaf(g0.z, c, m[2]);
+            m[3] = fmaf(g0.w, c, m[3]);
+            m[4] = fmaf(g1.x, c, m[4]);
+            m[5] = fmaf(g1.y, s, m[5]);
+            m[6] = fmaf(g1.z, s, m[6]);
+            m[7] = fmaf(g1.w, s, m[7]);
+            const float uc = fmaf(k.qadx, g0.x, fmaf(k.qadz, g0.z, fmaf(k.akdx, g0.w, k.akdz * g1.x)));
+            const float us = fmaf(k.a, g0.y, fmaf(k.qakxx, g1.y, fmaf(k.qakxz, g1.z, k.qakzz * g1.w)));
+            const float gth = fmaf(us, c, -uc * s);
+            m[8] += gth;
+            m[9] = fmaf(gth, g2.x, m[9]);
+            m[10] = fmaf(gth, g2.y, m[10]);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(32 * kAdjWarps)
+k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restrict__ gpos,
+          const float* __restrict__ gnrm, uint32_t flags, char* __restrict__ ws, AdjLayout L) {
+#if __CUDA_ARCH__ >= 900
+    cudaGridDependencySynchronize();
+#endif
+    extern __shared__ float4 smem[];
+    const int warp = threadIdx.x >> 5;
+    const uint32_t lane = threadIdx.x & 31;
+    float4* wst = smem + warp * (32 * kStage + kGbufVerts * kGbufF4);
+    float4* gbuf = wst + 32 * kStage;
+    WsHeader* hdr = reinterpret_cast<WsHeader*>(ws);
+    const uint32_t* sorted = reinterpret_cast<const uint32_t*>(ws + L.f.sorted);
+    const uint32_t* tile_pre = reinterpret_cast<const uint32_t*>(ws + L.f.tile_pre);
+    const PatchAux* aux = reinterpret_cast<const PatchAux*>(ws + L.f.aux);
+    const PairCoef* coef = reinterpret_cast<const PairCoef*>(ws + L.f.coef);
+    const uint32_t* part_off = reinterpret_cast<const uint32_t*>(ws + L.part_off);
+    float* partials = reinterpret_cast<float*>(ws + L.partials);
+    const uint32_t n = hdr->n_patches;
+    const uint32_t total = hdr->total_tiles;
+    const bool pow2 = hm.present && (hm.width & (hm.width - 1)) == 0 && (hm.height & (hm.height - 1)) == 0;
+    const bool vec3 = (flags & WT_LAYOUT_VEC3) != 0;
+
+    uint32_t t_next = 0;
+    if (lane == 0) t_next = atomicAdd(&hdr->tile_counter, 1u);
+    uint32_t t = __shfl_sync(0xffffffffu, t_next, 0);
+    uint32_t q = 0;
+    while (t < total) {
+        if (lane == 0) t_next = atomicAdd(&hdr->tile_counter, 1u);
+        if (tile_pre[q + 1] <= t) {
+            uint32_t step = 1, lo = q + 1, hi = q + 2;
+            while (hi <= n && tile_pre[hi] <= t) { lo = hi; step <<= 1; hi = lo + step; }
+            hi = min(hi, n + 1);
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (tile_pre[mid] <= t) lo = mid; else hi = mid;
+            }
+            q = lo;
+        }
+        const uint32_t p = sorted[q];
+        const uint32_t lt = t - tile_pre[q];
+        const uint32_t cols = patches[p].cols;
+        const uint32_t nwaves = patches[p].wave_count;
+        const uint64_t out0 = patches[p].out_offset;
+        const PatchAux a = aux[p];
+        uint32_t S, tpr;
+        row_tiling(cols, &S, &tpr);
+        const uint32_t row = lt / tpr;
+        const uint32_t c0 = (lt - row * tpr) * 32u * S;
+        if (nwaves > 0) {
+            // ---- phase 1: forward sums and vertex adjoints, vertex per lane
+            float acc[8][8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+#pragma unroll
+                for (int mm = 0; mm < 8; ++mm) acc[j][mm] = 0.0f;
+            for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
+                const uint32_t nw = min(32u, nwaves - w0);
+                __syncwarp();
+                if (lane < nw) stage_wave(coef[a.pair_offset + w0 + lane], c0, row, wst + kStage * lane);
+                __syncwarp();
+                switch (S) {
+                    case 1: wave_loop<1>(acc, wst, nw, lane); break;
+                    case 2: wave_loop<2>(acc, wst, nw, lane); break;
+                    case 3: wave_loop<3>(acc, wst, nw, lane); break;
+                    case 4: wave_loop<4>(acc, wst, nw, lane); break;
+                    case 5: wave_loop<5>(acc, wst, nw, lane); break;
+                    case 6: wave_loop<6>(acc, wst, nw, lane); break;
+                    case 7: wave_loop<7>(acc, wst, nw, lane); break;
+                    default: wave_loop<8>(acc, wst, nw, lane); break;
+                }
+            }
+            const float v = (float)row * a.inv_rm1;
+            const float gx = (a.e1x + v * a.e3x) * a.inv_cm1, gz = (a.e1z + v * a.e3z) * a.inv_cm1;
+            const float colf = (float)(c0 + lane);
+            const float xb = fmaf(colf, gx, v * a.e2x), zb = fmaf(colf, gz, v * a.e2z);
+            const uint64_t rowbase = out0 + (uint64_t)row * cols;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                if ((uint32_t)j < S) {
+                    const uint32_t col = c0 + lane + 32 * j;
+                    const float xl = fmaf(32.0f * j, gx, xb), zl = fmaf(32.0f * j, gz, zb);
+                    float g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                    if (col < cols) {
+                        VertexSums s{acc[j][0], acc[j][1], acc[j][2], acc[j][3], acc[j][4], acc[j][5], acc[j][6],
+                                     acc[j][7]};
+                        vertex_adjoint(s, xl, zl, a, hm, pow2, gpos, gnrm, rowbase + col, vec3, g);
+                    }
+                    float4* d = gbuf + kGbufF4 * (lane + 32 * j);
+                    d[0] = make_float4(g[0], g[1], g[2], g[3]);
+                    d[1] = make_float4(g[4], g[5], g[6], g[7]);
+                    d[2] = make_float4(xl, zl, 0.0f, 0.0f);
+                }
+            }
+            __syncwarp();
+            // ---- phase 2: wave per lane, records of this tile
+            const uint32_t nvalid0 = min(32u, cols - c0);  // valid lanes at j = 0
+            const uint32_t rec0 = part_off[q] + lt * nwaves;
+            for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
+                const uint32_t wi = w0 + lane;
+                const bool active = wi < nwaves;
+                const PairCoef k = coef[a.pair_offset + (active ? wi : 0)];
+                float4 st[3];
+                stage_wave(k, c0, row, st);
+                float m[11];
+#pragma unroll
+                for (int i = 0; i < 11; ++i) m[i] = 0.0f;
+                const uint32_t t32 = __float_as_uint(st[0].x), a32 = __float_as_uint(st[0].y);
+                switch (S) {
+                    case 1: wave_moments<1>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
+                    case 2: wave_moments<2>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
+                    case 3: wave_moments<3>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
+                    case 4: wave_moments<4>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
+                    case 5: wave_moments<5>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
+                    case 6: wave_moments<6>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
+                    case 7: wave_moments<7>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
+                    default: wave_moments<8>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
+                }
+                if (active) {
+                    float* r = partials + (size_t)kAdjRecord * (rec0 + wi);
+#pragma unroll
+                    for (int i = 0; i < 11; ++i) r[i] = m[i];
+                }
+            }
+            __syncwarp();
+        }
+        t = __shfl_sync(0xffffffffu, t_next, 0);
+    }
+}
+
+// One warp per (patch, wave): FP64 sum of the patch's records in tile order,
+// then the closed-form gradient (see the header comment for the moments).
+__global__ void __launch_bounds__(256) k_adj_pairs(const wt_patch* __restrict__ patches, uint32_t n,
+                                                   const wt_wave* __restrict__ waves, const char* __restrict__ ws,
+                                                   AdjLayout L) {
+#if __CUDA_ARCH__ >= 900
+    cudaGridDependencySynchronize();
+#endif
+    const uint32_t* pair_off = reinterpret_cast<const uint32_t*>(ws + L.f.pair_off);
+    const uint32_t* tile_pre = reinterpret_cast<const uint32_t*>(ws + L.f.tile_pre);
+    const uint32_t* rank = reinterpret_cast<const uint32_t*>(ws + L.rank);
+    const uint32_t* part_off = reinterpret_cast<const uint32_t*>(ws + L.part_off);
+    const float* partials = reinterpret_cast<const float*>(ws + L.partials);
+    const WsHeader* hdr = reinterpret_cast<const WsHeader*>(ws);
+    double* pair_grad = reinterpret_cast<double*>(const_cast<char*>(ws) + L.pair_grad);
+    const uint32_t total = pair_off[n];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const bool ran = hdr->total_tiles > 0 || total == 0;
+    for (uint32_t P = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < total; P += warps) {
+        uint32_t lo = 0, hi = n + 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (pair_off[mid] <= P) lo = mid + 1; else hi = mid;
+        }
+        const uint32_t p = lo - 1, j = P - pair_off[p];
+        const uint32_t nw = pair_off[p + 1] - pair_off[p];
+        const uint32_t qs = rank[p];
+        const uint32_t ntiles = tile_pre[qs + 1] - tile_pre[qs];
+        double m[11];
+#pragma unroll
+        for (int i = 0; i < 11; ++i) m[i] = 0.0;
+        if (ran)
+            for (uint32_t k = lane; k < ntiles; k += 32) {
+                const float* r = partials + (size_t)kAdjRecord * (part_off[qs] + (size_t)k * nw + j);
+#pragma unroll
+                for (int i = 0; i < 11; ++i) m[i] += (double)r[i];
+            }
+#pragma unroll
+        for (int i = 0; i < 11; ++i)
+            for (int o = 16; o > 0; o >>= 1) m[i] += __shfl_xor_sync(0xffffffffu, m[i], o);
+        if (lane == 0) {
+            const wt_patch Pt = patches[p];
+            const wt_wave w = waves[Pt.wave_offset + j];
+            const double lam = w.wavelength;
+            const double k = isinf(lam) ? 0.0 : kTwoPi / lam;
+            const double A = w.amplitude, Q = w.steepness_q, Dx = w.dir_x, Dz = w.dir_z, sp = w.speed;
+            const double t = Pt.time_s;
+            const double Mdx = m[0], Mdy = m[1], Mdz = m[2], Mjx = m[3], Mjz = m[4];
+            const double Mxx = m[5], Mxz = m[6], Mzz = m[7], T0 = m[8];
+            const double Xw = m[9] + (double)Pt.bl[0] * T0, Zw = m[10] + (double)Pt.bl[1] * T0;
+            const double P3 = Dx * Dx * Mxx + Dx * Dz * Mxz + Dz * Dz * Mzz;
+            const double gA = Q * (Dx * Mdx + Dz * Mdz) + k * (Dx * Mjx + Dz * Mjz) + Mdy + Q * k * P3;
+            const double gQ = A * (Dx * Mdx + Dz * Mdz + k * P3);
+            const double gk = A * (Dx * Mjx + Dz * Mjz + Q * P3) + Dx * Xw + Dz * Zw + sp * t * T0;
+            const double gDx = Q * A * Mdx + A * k * Mjx + Q * A * k * (2.0 * Dx * Mxx + Dz * Mxz) + k * Xw;
+            const double gDz = Q * A * Mdz + A * k * Mjz + Q * A * k * (2.0 * Dz * Mzz + Dx * Mxz) + k * Zw;
+            double* g = pair_grad + 8 * (size_t)P;
+            g[0] = gA;
+            g[1] = isinf(lam) ? 0.0 : -gk * k / lam;
+            g[2] = -Dz * gDx + Dx * gDz;
+            g[3] = gQ;
+            g[4] = T0;
+            g[5] = k * t * T0;
+            g[6] = gDx;
+            g[7] = gDz;
+        }
+    }
+}
+
+// One thread per wave: the patches that use it, in patch order.
+__global__ void __launch_bounds__(256) k_adj_waves(const wt_patch* __restrict__ patches, uint32_t n,
+                                                   uint32_t n_waves, const char* __restrict__ ws, AdjLayout L,
+                                                   wt_wave_grad* __restrict__ grad) {
+#if __CUDA_ARCH__ >= 900
+    cudaGridDependencySynchronize();
+#endif
+    const uint32_t* pair_off = reinterpret_cast<const uint32_t*>(ws + L.f.pair_off);
+    const double* pair_grad = reinterpret_cast<const double*>(ws + L.pair_grad);
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < n_waves; w += gridDim.x * blockDim.x) {
+        double g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (uint32_t p = 0; p < n; ++p) {
+            const uint32_t nw = pair_off[p + 1] - pair_off[p];  // 0 for invalid patches
+            const uint32_t off = patches[p].wave_offset;
+            if (nw > 0 && w >= off && w - off < nw) {
+                const double* s = pair_grad + 8 * (size_t)(pair_off[p] + (w - off));
+#pragma unroll
+                for (int i = 0; i < 8; ++i) g[i] += s[i];
+            }
+        }
+        wt_wave_grad o;
+        o.d_amplitude = (float)g[0];
+        o.d_wavelength = (float)g[1];
+        o.d_direction = (float)g[2];
+        o.d_steepness_q = (float)g[3];
+        o.d_phase = (float)g[4];
+        o.d_speed = (float)g[5];
+        o.d_dir_x = (float)g[6];
+        o.d_dir_z = (float)g[7];
+        grad[w] = o;
+    }
+}
+
+int device_sms() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+template <typename K, typename... Args>
+cudaError_t launch_pdl(K kernel, dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = grid;
+    lc.blockDim = block;
+    lc.dynamicSmemBytes = smem;
+    lc.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    return cudaLaunchKernelEx(&lc, kernel, args...);
+}
+
+}  // namespace
+
+uint64_t adjoint_records(const wt_patch& p) {
+    if (p.cols < 2 || p.rows < 2) return 0;
+    uint32_t S, tpr;
+    dev::row_tiling(p.cols, &S, &tpr);
+    return (uint64_t)p.rows * tpr * p.wave_count;
+}
+
+cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
+                           const HmDev& hm, const float* gpos, const float* gnrm, uint32_t flags,
+                           wt_wave_grad* grad, void* ws, const AdjLayout& L, cudaStream_t s) {
+    char* w = static_cast<char*>(ws);
+    const int sms = device_sms();
+    cudaError_t e = launch_pdl(k_adj_scan, dim3(1), dim3(1024), 0, s, patches, n_patches, w, L);
+    if (e != cudaSuccess) return e;
+    const size_t smem = sizeof(float4) * kAdjWarps * (32 * kStage + kGbufVerts * kGbufF4);
+    static bool attr_set[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+        e = cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_set[dev] = true;
+    }
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint, 32 * kAdjWarps, smem);
+    if (occ < 1) occ = 1;
+    e = launch_pdl(k_adjoint, dim3(sms * occ), dim3(32 * kAdjWarps), smem, s, patches, hm, gpos, gnrm, flags, w, L);
+    if (e != cudaSuccess) return e;
+    e = launch_pdl(k_adj_pairs, dim3(sms * 4), dim3(256), 0, s, patches, n_patches, waves,
+                   static_cast<const char*>(ws), L);
+    if (e != cudaSuccess) return e;
+    const unsigned wb = (n_waves + 255) / 256;
+    if (wb == 0) return cudaSuccess;
+    return launch_pdl(k_adj_waves, dim3(wb), dim3(256), 0, s, patches, n_patches, n_waves,
+                      static_cast<const char*>(ws), L, grad);
+}
+
+}  // namespace wt

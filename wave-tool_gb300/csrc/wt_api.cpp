@@ -149,10 +149,28 @@ wt_status wt_displace_workspace_size(uint32_t n_patches, uint64_t total_wave_slo
     return WT_OK;
 }
 
+// Wave slots and (tile, wave) records of a host patch table.
+static wt_status adjoint_sizes(const wt_patch* hp, uint32_t n, uint64_t* slots, uint64_t* records) {
+    uint64_t sl = 0, rec = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        sl += hp[i].wave_count;
+        rec += wt::adjoint_records(hp[i]);
+    }
+    if (sl > 0xffffffffull || rec >= 0xffffffffull) return fail(WT_ERR_INVALID_ARG, "adjoint: too many wave slots or tiles");
+    *slots = sl;
+    *records = rec;
+    return WT_OK;
+}
+
 wt_status wt_adjoint_workspace_size(const wt_patch* host_patches, uint32_t n_patches, size_t* bytes) {
     if (!bytes) return fail(WT_ERR_INVALID_ARG, "bytes is NULL");
     if (n_patches > 0 && !host_patches) return fail(WT_ERR_INVALID_ARG, "host_patches is NULL");
-    return fail(WT_ERR_UNSUPPORTED, "adjoint not built yet");
+    if (n_patches > kMaxPatches) return fail(WT_ERR_INVALID_ARG, "n_patches %u > %u", n_patches, kMaxPatches);
+    uint64_t slots = 0, records = 0;
+    wt_status st = adjoint_sizes(host_patches, n_patches, &slots, &records);
+    if (st != WT_OK) return st;
+    *bytes = wt::adj_layout(n_patches, slots, records).end;
+    return WT_OK;
 }
 
 wt_status wt_workspace_status(const void* workspace, wt_stream stream, uint32_t* bad_patch) {
@@ -190,13 +208,39 @@ wt_status wt_gerstner_displace_unbatched(const wt_patch* host_patches, const wt_
     return WT_OK;
 }
 
-wt_status wt_gerstner_adjoint(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
-                              uint32_t n_waves, const wt_heightmap* hm, const float* d_pos, const float* d_nrm,
-                              uint64_t out_capacity, uint32_t flags, wt_wave_grad* grad_out, void* workspace,
-                              size_t workspace_bytes, wt_stream stream) {
-    (void)patches; (void)n_patches; (void)waves; (void)n_waves; (void)hm; (void)d_pos; (void)d_nrm;
-    (void)out_capacity; (void)flags; (void)grad_out; (void)workspace; (void)workspace_bytes; (void)stream;
-    return fail(WT_ERR_UNSUPPORTED, "adjoint not built yet");
+wt_status wt_gerstner_adjoint(const wt_patch* host_patches, const wt_patch* patches, uint32_t n_patches,
+                              const wt_wave* waves, uint32_t n_waves, const wt_heightmap* hm, const float* d_pos,
+                              const float* d_nrm, uint64_t out_capacity, uint32_t flags, wt_wave_grad* grad_out,
+                              void* workspace, size_t workspace_bytes, wt_stream stream) {
+    if (n_patches > 0 && !host_patches) return fail(WT_ERR_INVALID_ARG, "host_patches is NULL");
+    Prepared P;
+    wt_status st = check_common(patches, n_patches, waves, n_waves, hm, out_capacity, flags, workspace,
+                                workspace_bytes, &P);
+    if (st != WT_OK) return st;
+    if (flags & WT_PHASE_FP32_NAIVE) return fail(WT_ERR_UNSUPPORTED, "adjoint: FP32-naive phase has no adjoint");
+    if (!d_pos || !aligned(d_pos, 4)) return fail(WT_ERR_INVALID_ARG, "d_pos NULL or not 4-byte aligned");
+    if (d_nrm && !aligned(d_nrm, 4)) return fail(WT_ERR_INVALID_ARG, "d_nrm not 4-byte aligned");
+    if (n_waves > 0 && (!grad_out || !aligned(grad_out, 4)))
+        return fail(WT_ERR_INVALID_ARG, "grad_out NULL or not 4-byte aligned");
+    uint64_t slots = 0, records = 0;
+    st = adjoint_sizes(host_patches, n_patches, &slots, &records);
+    if (st != WT_OK) return st;
+    const wt::AdjLayout L = wt::adj_layout(n_patches, slots, records);
+    if (workspace_bytes < L.end)
+        return fail(WT_ERR_NOMEM, "adjoint workspace %zu bytes < %zu needed", workspace_bytes, L.end);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n_patches == 0 || n_waves == 0) {
+        if (n_waves == 0) return WT_OK;
+        cudaError_t e = cudaMemsetAsync(grad_out, 0, sizeof(wt_wave_grad) * n_waves, s);
+        return e == cudaSuccess ? WT_OK : cuda_fail(e, "clearing grad_out");
+    }
+    const wt::FwdConfig cfg = current_cfg();
+    cudaError_t e = wt::launch_prep(patches, n_patches, waves, n_waves, P.hm, out_capacity, 32u * cfg.s, workspace,
+                                    L.f, s);
+    if (e != cudaSuccess) return cuda_fail(e, "prep launch");
+    e = wt::launch_adjoint(patches, n_patches, waves, n_waves, P.hm, d_pos, d_nrm, flags, grad_out, workspace, L, s);
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
+    return WT_OK;
 }
 
 wt_status wt_grid_indices(uint32_t cols, uint32_t rows, uint32_t base_vertex, uint32_t* idx_out, wt_stream stream) {

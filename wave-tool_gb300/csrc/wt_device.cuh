@@ -1,0 +1,253 @@
+// wt_device.cuh — device code shared by the forward (wt_displace.cu) and
+// adjoint (wt_adjoint.cu) kernels: row tiling, the per-wave staging and
+// Chebyshev wave loop, heightmap footprints, block scans.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "wt_internal.h"
+
+namespace wt {
+namespace dev {
+
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+constexpr float kTurnToRad = 1.4629180792671596e-09f;  // 2*pi / 2^32
+
+// Block-wide exclusive scan of a u32 array in global memory, in place, in
+// chunks of blockDim.x.  Returns the total.  All threads must call.
+static __device__ uint32_t block_exclusive_scan(uint32_t* a, uint32_t n) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (uint32_t base = 0; base < n; base += blockDim.x) {
+        uint32_t i = base + threadIdx.x;
+        uint32_t v = i < n ? a[i] : 0u;
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sums[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = lane < nwarps ? warp_sums[lane] : 0u;
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            warp_sums[lane] = w;  // inclusive
+        }
+        __syncthreads();
+        uint32_t excl = carry + (warp > 0 ? warp_sums[warp - 1] : 0u) + x - v;
+        if (i < n) a[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_sums[nwarps - 1];
+        __syncthreads();
+    }
+    return carry;
+}
+
+// Tiling of one patch row: tiles of 32*S columns, S in 1..8, choosing the S
+// whose tiles cover the row with the least padding, with a preference for
+// larger S (each wave's start-up costs about as much as two vertices).
+__host__ __device__ __forceinline__ void row_tiling(uint32_t cols, uint32_t* S_out, uint32_t* tpr_out) {
+    uint32_t bestS = 8, bestT = (cols + 255) / 256;
+    float best = 256.0f * bestT * (1.0f + 2.0f / 8.0f);
+    for (uint32_t S = 7; S >= 1; --S) {
+        const uint32_t t = (cols + 32 * S - 1) / (32 * S);
+        const float cost = 32.0f * S * t * (1.0f + 2.0f / (float)S);
+        if (cost < best) { best = cost; bestS = S; bestT = t; }
+    }
+    *S_out = bestS;
+    *tpr_out = bestT;
+}
+
+// ---- shared epilogue -------------------------------------------------------
+
+// Texel coordinate -> the two texel indices of the GL_LINEAR footprint and
+// the weight, with the GL wrap of integer texel indices (REPEAT: i mod n;
+// MIRRORED_REPEAT: (n-1) - mirror((i mod 2n) - n)).  The coordinate is first
+// reduced by the wrap period (exact for |x| < 2^24); indices are clamped into
+// range whatever the input (huge or NaN coordinates give garbage, never an
+// out-of-bounds read).
+struct Footprint {
+    int i0, i1;
+    float w;
+};
+
+__device__ __forceinline__ int mirror_index(int m, int n) {
+    int a = m - n;
+    return n - 1 - (a >= 0 ? a : -(1 + a));
+}
+
+__device__ __forceinline__ Footprint footprint(float x, int n, uint32_t mode, bool pow2) {
+    const bool mir = mode == WT_WRAP_MIRRORED_REPEAT;
+    const int P = mir ? 2 * n : n;
+    Footprint f;
+    int i0;
+    if (pow2) {
+        // power-of-two sizes: the wrap is a mask; the saturating conversion
+        // keeps any input (NaN -> 0) in range
+        f.w = x - floorf(x);
+        i0 = __float2int_rd(x) & (P - 1);
+    } else {
+        const float Pf = (float)P;
+        const float r = x - Pf * floorf(x * (1.0f / Pf));
+        f.w = r - floorf(r);
+        i0 = __float2int_rd(r);
+        i0 += i0 < 0 ? P : 0;
+        i0 -= i0 >= P ? P : 0;
+        i0 = min(max(i0, 0), P - 1);
+    }
+    const int i1 = i0 + 1 == P ? 0 : i0 + 1;
+    f.i0 = mir ? mirror_index(i0, n) : i0;
+    f.i1 = mir ? mirror_index(i1, n) : i1;
+    return f;
+}
+
+// Heightmap layer at the displaced local point (xl + dx, zl + dz) of a
+// patch: h = disp*2*(r - 0.5) and its derivatives with respect to world x'
+// and z' (the bilinear cross term hxz is what the adjoint of the normal needs;
+// d2h/dx'2 = d2h/dz'2 = 0 inside a texel cell).
+struct HmSample {
+    float h, hx, hz, hxz;
+};
+
+__device__ __forceinline__ HmSample hm_sample(const HmDev& hm, const PatchAux& a, float xd, float zd, bool pow2) {
+    const float ut = fmaf(a.su, xd, a.hu0);
+    const float vt = fmaf(a.sv, zd, a.hv0);
+    const int W = (int)hm.width, H = (int)hm.height;
+    const Footprint fu = footprint(ut, W, hm.wrap, pow2), fv = footprint(vt, H, hm.wrap, pow2);
+    const float al = fu.w, be = fv.w;
+    const float t00 = __ldg(hm.texels + fv.i0 * W + fu.i0), t10 = __ldg(hm.texels + fv.i0 * W + fu.i1);
+    const float t01 = __ldg(hm.texels + fv.i1 * W + fu.i0), t11 = __ldg(hm.texels + fv.i1 * W + fu.i1);
+    const float r0 = fmaf(al, t10 - t00, t00), r1 = fmaf(al, t11 - t01, t01);
+    const float r = fmaf(be, r1 - r0, r0);
+    const float dru = fmaf(be, (t11 - t01) - (t10 - t00), t10 - t00);
+    const float drv = r1 - r0;
+    const float k2 = 2.0f * hm.disp_scale;
+    HmSample o;
+    o.h = k2 * (r - 0.5f);
+    o.hx = k2 * dru * a.su;
+    o.hz = k2 * drv * a.sv;
+    o.hxz = k2 * ((t11 - t01) - (t10 - t00)) * a.su * a.sv;
+    return o;
+}
+
+struct VertexSums {
+    float dx, dy, dz, jx, jz, sxx, sxz, szz;
+};
+
+// Heightmap, bounce, normal, stores for one vertex.
+__device__ __forceinline__ void finish_vertex(const VertexSums& s, float xl, float zl, const PatchAux& a,
+                                              const HmDev& hm, bool pow2, uint64_t vidx,
+                                              float* __restrict__ pos, float* __restrict__ nrm,
+                                              uint32_t flags) {
+    float px0 = 1.0f - s.sxx, px1 = s.jx, px2 = -s.sxz;
+    float pz0 = -s.sxz, pz1 = s.jz, pz2 = 1.0f - s.szz;
+    float dy = s.dy;
+    if (hm.present) {
+        const HmSample g = hm_sample(hm, a, xl + s.dx, zl + s.dz, pow2);
+        dy += g.h;
+        px1 = fmaf(g.hx, px0, fmaf(g.hz, px2, px1));
+        pz1 = fmaf(g.hx, pz0, fmaf(g.hz, pz2, pz1));
+    }
+    dy += a.y_offset;
+    // N = dP/dz x dP/dx
+    float n0 = pz1 * px2 - pz2 * px1;
+    float n1 = pz2 * px0 - pz0 * px2;
+    float n2 = pz0 * px1 - pz1 * px0;
+    float inv = rsqrtf(fmaf(n0, n0, fmaf(n1, n1, n2 * n2)));
+    float ox, oz, ow;
+    if (flags & WT_OUT_DISPLACEMENT) { ox = s.dx; oz = s.dz; ow = 0.0f; }
+    else { ox = a.blx + (xl + s.dx); oz = a.blz + (zl + s.dz); ow = 1.0f; }
+    if (flags & WT_LAYOUT_VEC3) {
+        float* P = pos + 3 * vidx;
+        __stcs(P, ox); __stcs(P + 1, dy); __stcs(P + 2, oz);
+        if (nrm) {
+            float* N = nrm + 3 * vidx;
+            __stcs(N, n0 * inv); __stcs(N + 1, n1 * inv); __stcs(N + 2, n2 * inv);
+        }
+    } else {
+        __stcs(reinterpret_cast<float4*>(pos) + vidx, make_float4(ox, dy, oz, ow));
+        if (nrm) __stcs(reinterpret_cast<float4*>(nrm) + vidx, make_float4(n0 * inv, n1 * inv, n2 * inv, 0.0f));
+    }
+}
+
+__device__ __forceinline__ uint32_t hi32_round(unsigned long long x) {
+    return (uint32_t)((x + 0x80000000ull) >> 32);
+}
+
+// Per-wave staging in shared memory (3 float4 per wave, up to 32 waves per warp):
+//   [0] t32, a32 (fixed-point turns), cos d, sin d      d = one 32-column step
+//   [1] Q*A*Dx, A, Q*A*Dz, A*k*Dx
+//   [2] A*k*Dz, Q*A*k*Dx^2, Q*A*k*Dx*Dz, Q*A*k*Dz^2
+// Lane l's vertices j = 0..S-1 sit at columns c0 + l + 32 j.  Vertex 0 takes
+// a MUFU sincos of its exact start phase, vertex 1 an exact rotation by d, and
+// vertices j >= 2 the Chebyshev recurrence x[j] = 2 cos(d) x[j-1] - x[j-2]
+// (one FMA per value; its error grows at most linearly in j).
+constexpr int kStage = 3;
+
+// One lane's share of the staging: wave constants for the tile at (c0, row).
+__device__ __forceinline__ void stage_wave(const PairCoef& c, uint32_t c0, uint32_t row, float4* __restrict__ d) {
+    // phase of this wave at (c0, row) and its per-column step on this row
+    const unsigned long long t64 = c.t00 + (unsigned long long)c0 * c.ta + (unsigned long long)row * c.tb +
+                                   (unsigned long long)c0 * row * c.tg;
+    const unsigned long long a64 = c.ta + (unsigned long long)row * c.tg;
+    const uint32_t t32 = hi32_round(t64), a32 = hi32_round(a64), d32 = hi32_round(a64 * 32ull);
+    // rotation by the 32-column step: sincospi of the high part (exact in
+    // FP32), then a first-order turn by the low 8 bits
+    const uint32_t dhi = d32 & 0xffffff00u;
+    float sd, cd;
+    sincospif((float)(int)dhi * 4.656612873077393e-10f, &sd, &cd);  // sin(2*pi*turns)
+    const float eps = (float)(d32 - dhi) * kTurnToRad;
+    const float cdn = fmaf(-sd, eps, cd);
+    sd = fmaf(cd, eps, sd);
+    cd = cdn;
+    d[0] = make_float4(__uint_as_float(t32), __uint_as_float(a32), cd, sd);
+    d[1] = make_float4(c.qadx, c.a, c.qadz, c.akdx);
+    d[2] = make_float4(c.akdz, c.qakxx, c.qakxz, c.qakzz);
+}
+
+// The wave loop of one tile for a compile-time S: sums of nw staged waves
+// into acc[0..S-1].
+template <int S>
+__device__ __forceinline__ void wave_loop(float (&acc)[8][8], const float4* __restrict__ wst, uint32_t nw,
+                                          uint32_t lane) {
+#pragma unroll 2
+    for (uint32_t i = 0; i < nw; ++i) {
+        const float4 w0v = wst[kStage * i];
+        const float4 w1 = wst[kStage * i + 1];
+        const float4 w2 = wst[kStage * i + 2];
+        const uint32_t tl = __float_as_uint(w0v.x) + lane * __float_as_uint(w0v.y);
+        const float ang = (float)(int)tl * kTurnToRad;
+        const float cd = w0v.z, sd = w0v.w, tc = 2.0f * cd;
+        float c, s, cp = 0.0f, sp = 0.0f;
+        __sincosf(ang, &s, &c);
+#pragma unroll
+        for (int j = 0; j < S; ++j) {
+            if (j == 1) {
+                const float cn = fmaf(c, cd, -s * sd);
+                const float sn = fmaf(s, cd, c * sd);
+                cp = c; sp = s; c = cn; s = sn;
+            } else if (j >= 2) {
+                const float cn = fmaf(tc, c, -cp);
+                const float sn = fmaf(tc, s, -sp);
+                cp = c; sp = s; c = cn; s = sn;
+            }
+            acc[j][0] = fmaf(w1.x, c, acc[j][0]);
+            acc[j][1] = fmaf(w1.y, s, acc[j][1]);
+            acc[j][2] = fmaf(w1.z, c, acc[j][2]);
+            acc[j][3] = fmaf(w1.w, c, acc[j][3]);
+            acc[j][4] = fmaf(w2.x, c, acc[j][4]);
+            acc[j][5] = fmaf(w2.y, s, acc[j][5]);
+            acc[j][6] = fmaf(w2.z, s, acc[j][6]);
+            acc[j][7] = fmaf(w2.w, s, acc[j][7]);
+        }
+    }
+}
+
+}  // namespace dev
+}  // namespace wt

@@ -75,6 +75,32 @@ inline WsLayout ws_layout(uint32_t n_patches, uint64_t total_wave_slots) {
     return L;
 }
 
+// Adjoint workspace: the forward layout (prep stages are shared), then
+// rank    u32[n]      sorted position of each patch
+// partoff u32[n+1]    exclusive prefix of records (tiles x waves) over the sorted order
+// partial float[11 x records]   per-(tile, wave) FP32 partial sums
+// pairg   double[8 x wave slots] per-(patch, wave) gradient
+constexpr int kAdjRecord = 11;
+
+struct AdjLayout {
+    WsLayout f;
+    size_t rank, part_off, partials, pair_grad, end;
+    uint64_t cap_records;
+};
+
+inline AdjLayout adj_layout(uint32_t n_patches, uint64_t total_wave_slots, uint64_t records) {
+    AdjLayout A;
+    A.f = ws_layout(n_patches, total_wave_slots);
+    size_t o = A.f.end;
+    A.rank = o;      o = align_up(o + 4ull * n_patches, 16);
+    A.part_off = o;  o = align_up(o + 4ull * (n_patches + 1), 256);
+    A.partials = o;  o = align_up(o + 4ull * kAdjRecord * records, 256);
+    A.pair_grad = o; o = align_up(o + 8ull * 8 * total_wave_slots, 256);
+    A.end = o;
+    A.cap_records = records;
+    return A;
+}
+
 // Tuning of the forward launch.
 struct FwdConfig {
     int s;              // vertices per lane per tile row (tile = 32*s columns)
@@ -103,6 +129,13 @@ cudaError_t launch_forward_naive(const wt_patch* patches, uint32_t n_patches, co
                                  void* ws, const WsLayout& L, uint64_t total_vertices,
                                  cudaStream_t s);
 bool forward_config_supported(const FwdConfig& cfg);
+
+// ---- adjoint (wt_adjoint.cu) ----------------------------------------------
+// Records (tiles x waves) of one patch, as the adjoint lays them out.
+uint64_t adjoint_records(const wt_patch& p);
+cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
+                           const HmDev& hm, const float* gpos, const float* gnrm, uint32_t flags,
+                           wt_wave_grad* grad, void* ws, const AdjLayout& L, cudaStream_t s);
 
 // ---- host helpers (wt_api.cpp) ---------------------------------------------
 void set_last_error(const char* msg);  // message returned by wt_last_error() on this thread
