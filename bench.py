@@ -47,6 +47,8 @@ def parse_args():
     ap.add_argument("--patches", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
     ap.add_argument("--no-extras", action="store_true", help="skip the unbatched / single-patch side runs")
+    ap.add_argument("--mode", choices=["forward", "adjoint"], default="forward",
+                    help="'adjoint' times only wt_gerstner_adjoint on 64 uneven patches (for profiling)")
     ap.add_argument("--tuning", default="auto",
                     help="'auto' (autotune before timing) or WARPS,CHUNK to fix the launch shape")
     return ap.parse_args()
@@ -176,6 +178,74 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _event_ms(fn, reps, stream, flush=None):
+    """Mean device time of fn() over reps calls (CUDA events on `stream`,
+    optional L2 flush before each call, outside the events)."""
+    import torch
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for a, b in evs:
+        if flush is not None:
+            flush.zero_()
+        a.record(stream)
+        fn()
+        b.record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in evs) / reps
+
+
+def side_measurements(wt, workloads, surf, pos, nrm, flags, flush, stream, ms_step):
+    """Graph replay of the batched step, adjoint vs forward, the precision
+    configuration's throughput and the Adam fit (each reported, not the
+    headline)."""
+    import torch
+    from wave_tool_gb300 import fit
+    out = {}
+    # one CUDA graph holding the three launches of the batched call
+    s = torch.cuda.Stream()
+    s.wait_stream(stream)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        surf.displace(pos, nrm, flags=flags, stream=s)
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    gms = _event_ms(g.replay, 20, torch.cuda.current_stream(), flush)
+    out["graph_replay"] = {"ms_per_step": gms, "value": surf.n_terms_cache / (gms * 1e-3)}
+    # adjoint vs forward on the adjoint-fit grid and on 64 uneven patches
+    for name, w in (("adjoint_512sq_16waves", workloads.config4()[0]),
+                    ("adjoint_batched_64_uneven_patches", workloads.config5_batched_adjoint())):
+        sa = wt.Surface(w.patches, w.waves, wt.heightmap_from(w.heightmap))
+        pa, na = sa.alloc_outputs(flags)
+        gen = torch.Generator(device="cuda").manual_seed(1)
+        gp = torch.randn(pa.shape, device="cuda", generator=gen)
+        gn = torch.randn(na.shape, device="cuda", generator=gen)
+        for _ in range(3):
+            sa.displace(pa, na, flags=flags)
+            sa.adjoint(gp, gn)
+        fms = _event_ms(lambda: sa.displace(pa, na, flags=flags), 10, stream, flush)
+        ams = _event_ms(lambda: sa.adjoint(gp, gn), 10, stream, flush)
+        out[name] = {"terms": w.n_terms, "forward_ms": fms, "adjoint_ms": ams, "adjoint_over_forward": ams / fms}
+    # precision configuration: 2048^2 vertices x 128 waves at three times
+    prec = {}
+    for t in (1.0e2, 1.0e4, 1.0e6):
+        w5 = workloads.config5(time_s=t)
+        s5 = wt.Surface(w5.patches, w5.waves)
+        p5, n5 = s5.alloc_outputs(flags)
+        for _ in range(3):
+            s5.displace(p5, n5, flags=flags)
+        ms5 = _event_ms(lambda: s5.displace(p5, n5, flags=flags), 10, stream, flush)
+        prec[f"t={t:g}"] = {"ms_per_step": ms5, "value": w5.n_terms / (ms5 * 1e-3)}
+        del s5, p5, n5
+    out["precision_2048sq_128waves"] = prec
+    # the Adam fit: 500 steps of forward + adjoint on 512^2 x 16 waves
+    target, start = workloads.config4()
+    r = fit.fit_waves(target.patches, target.waves, start, steps=500, lr=1e-2)
+    out["adam_fit_512sq_16waves_500steps"] = {"ms_per_step": r["ms_per_step"], "loss_first": r["loss_first"],
+                                              "loss_last": r["loss_last"],
+                                              "param_errors": fit.parameter_errors(r["fitted"], target.waves)}
+    return out
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -191,6 +261,7 @@ def run_ours(args):
     w = workloads.config3(n_patches=args.patches, seed=2 + rank)
     hm = wt.heightmap_from(w.heightmap)
     surf = wt.Surface(w.patches, w.waves, hm)
+    surf.n_terms_cache = w.n_terms
     flags = wt.WT_OUT_DISPLACEMENT
     pos, nrm = surf.alloc_outputs(flags)
     stream = torch.cuda.current_stream()
@@ -278,6 +349,7 @@ def run_ours(args):
 
     extras = {}
     if not args.no_extras and rank == 0:
+        extras.update(side_measurements(wt, workloads, surf, pos, nrm, flags, flush, stream, ms_step))
         # 256 plain launches (one wt_gerstner_displace per patch)
         for _ in range(2):
             surf.displace(pos, nrm, flags=flags, unbatched=True)
@@ -354,8 +426,30 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_adjoint_only(args):
+    """wt_gerstner_adjoint on the 64-patch batched-adjoint workload: warmup,
+    then `steps` timed calls; prints one JSON line (not the headline)."""
+    import torch
+    wt = __graft_entry__.load_package()
+    from wave_tool_gb300 import workloads
+    w = workloads.config5_batched_adjoint()
+    surf = wt.Surface(w.patches, w.waves, wt.heightmap_from(w.heightmap))
+    pos, nrm = surf.alloc_outputs(0)
+    gen = torch.Generator(device="cuda").manual_seed(1)
+    gp = torch.randn(pos.shape, device="cuda", generator=gen)
+    gn = torch.randn(nrm.shape, device="cuda", generator=gen)
+    for _ in range(args.warmup):
+        surf.adjoint(gp, gn)
+    ms = _event_ms(lambda: surf.adjoint(gp, gn), args.steps, torch.cuda.current_stream())
+    print(json.dumps({"mode": "adjoint", "workload": w.name, "terms": w.n_terms, "ms_per_step": ms,
+                      "terms_per_s": w.n_terms / (ms * 1e-3)}), flush=True)
+
+
 def main():
     args = parse_args()
+    if args.mode == "adjoint":
+        run_adjoint_only(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
