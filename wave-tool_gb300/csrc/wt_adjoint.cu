@@ -13,10 +13,10 @@
 //       shared memory), regenerate the wave's sin/cos there (MUFU start +
 //       Chebyshev steps) and accumulate 11 per-wave moments; write them as
 //       the tile's record for that wave (no cross-lane reduction).
-//   k_adj_pairs  one warp per (patch, wave): FP64 sum of the patch's records
-//                in tile order, then the closed-form gradient in FP64.
-//   k_adj_waves  one thread per wave: sum over the patches that use it, in
-//                patch order.
+//   k_adj_cols   column sums of each patch's records over its tiles (FP32
+//                Kahan, fixed order)
+//   k_adj_waves  one warp per wave: closed-form gradient in FP64 for each
+//                patch that uses the wave, combined in a fixed order.
 // Every sum has a fixed order, so the result is bitwise reproducible.
 //
 // With g_q the adjoint of sum q per vertex and (c, s) the wave's cos/sin
@@ -37,7 +37,7 @@ using namespace wt::dev;
 
 constexpr int kAdjWarps = 4;                 // warps per block
 constexpr int kGbufVerts = 256;              // vertices per tile (32 lanes x S <= 8)
-constexpr int kGbufF4 = 3;                   // float4 per parked vertex
+constexpr int kGbufF4 = 2;                   // float4 per parked vertex
 
 __global__ void __launch_bounds__(1024) k_adj_scan(const wt_patch* __restrict__ patches, uint32_t n, char* ws,
                                                    AdjLayout L) {
@@ -111,18 +111,24 @@ __device__ __forceinline__ void vertex_adjoint(const VertexSums& s, float xl, fl
     g[7] = -g_b3;             // szz
 }
 
-// Phase 2 for a compile-time S: lane = one wave; vertices l + 32 j of the tile.
-template <int S>
-__device__ __forceinline__ void wave_moments(const float4* __restrict__ gbuf, uint32_t nvalid, uint32_t t32,
-                                             uint32_t a32, float cd, float sd, const PairCoef& k, float m[11]) {
+// Phase 2: lane = one wave; vertices l + 32 j of the tile (gbuf holds the
+// eight vertex adjoints as two float4).  The position-weighted phase sums use
+// x(l, j) = xb + l*gx + 32 j*gx: per vertex only sum(g_theta) and
+// sum(j*g_theta) are kept, and folded into Tx, Tz once per l.
+template <int SC>  // SC > 0: compile-time S; 0: runtime S
+__device__ __forceinline__ void wave_moments(const float4* __restrict__ gbuf, uint32_t S_rt, uint32_t nvalid,
+                                             uint32_t t32, uint32_t a32, float cd, float sd, const PairCoef& k,
+                                             float xb, float zb, float gx, float gz, float m[11]) {
+    const uint32_t S = SC > 0 ? (uint32_t)SC : S_rt;
     const float tc = 2.0f * cd;
-    for (uint32_t l = 0; l < 32; ++l) {
-        if (l >= nvalid) break;  // columns past the row end (nvalid = valid lanes of vertex 0)
+    for (uint32_t l = 0; l < nvalid; ++l) {
         const uint32_t tl = t32 + l * a32;
         float s, c, cp = 0.0f, sp = 0.0f;
         __sincosf((float)(int)tl * kTurnToRad, &s, &c);
+        float G0 = 0.0f, G1 = 0.0f;
 #pragma unroll
-        for (int j = 0; j < S; ++j) {
+        for (int j = 0; j < (SC > 0 ? SC : 8); ++j) {
+            if (SC == 0 && (uint32_t)j >= S) break;
             if (j == 1) {
                 const float cn = fmaf(c, cd, -s * sd), sn = fmaf(s, cd, c * sd);
                 cp = c; sp = s; c = cn; s = sn;
@@ -130,8 +136,8 @@ __device__ __forceinline__ void wave_moments(const float4* __restrict__ gbuf, ui
                 const float cn = fmaf(tc, c, -cp), sn = fmaf(tc, s, -sp);
                 cp = c; sp = s; c = cn; s = sn;
             }
-            const float4* v = gbuf + kGbufF4 * (l + 32 * j);
-            const float4 g0 = v[0], g1 = v[1], g2 = v[2];  // dx dy dz jx | jz sxx sxz szz | x z - -
+            const float4* v = gbuf + 2 * (l + 32 * j);
+            const float4 g0 = v[0], g1 = v[1];  // dx dy dz jx | jz sxx sxz szz
             m[0] = fmaf(g0.x, c, m[0]);
             m[1] = fmaf(g0.y, s, m[1]);
             m[2] = fmaf(g0.z, c, m[2]);
@@ -143,14 +149,17 @@ __device__ __forceinline__ void wave_moments(const float4* __restrict__ gbuf, ui
             const float uc = fmaf(k.qadx, g0.x, fmaf(k.qadz, g0.z, fmaf(k.akdx, g0.w, k.akdz * g1.x)));
             const float us = fmaf(k.a, g0.y, fmaf(k.qakxx, g1.y, fmaf(k.qakxz, g1.z, k.qakzz * g1.w)));
             const float gth = fmaf(us, c, -uc * s);
-            m[8] += gth;
-            m[9] = fmaf(gth, g2.x, m[9]);
-            m[10] = fmaf(gth, g2.y, m[10]);
+            G0 += gth;
+            G1 = fmaf((float)j, gth, G1);
         }
+        const float xl = fmaf((float)l, gx, xb), zl = fmaf((float)l, gz, zb);
+        m[8] += G0;
+        m[9] = fmaf(xl, G0, fmaf(32.0f * gx, G1, m[9]));
+        m[10] = fmaf(zl, G0, fmaf(32.0f * gz, G1, m[10]));
     }
 }
 
-__global__ void __launch_bounds__(32 * kAdjWarps)
+__global__ void __launch_bounds__(32 * kAdjWarps, 4)
 k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restrict__ gpos,
           const float* __restrict__ gnrm, uint32_t flags, char* __restrict__ ws, AdjLayout L) {
 #if __CUDA_ARCH__ >= 900
@@ -224,25 +233,31 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
             }
             const float v = (float)row * a.inv_rm1;
             const float gx = (a.e1x + v * a.e3x) * a.inv_cm1, gz = (a.e1z + v * a.e3z) * a.inv_cm1;
-            const float colf = (float)(c0 + lane);
-            const float xb = fmaf(colf, gx, v * a.e2x), zb = fmaf(colf, gz, v * a.e2z);
+            const float xb0 = fmaf((float)c0, gx, v * a.e2x), zb0 = fmaf((float)c0, gz, v * a.e2z);
             const uint64_t rowbase = out0 + (uint64_t)row * cols;
+            // park the eight sums of each vertex, then turn them into the
+            // vertex adjoints in a rolled loop (one copy of that code)
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 if ((uint32_t)j < S) {
-                    const uint32_t col = c0 + lane + 32 * j;
-                    const float xl = fmaf(32.0f * j, gx, xb), zl = fmaf(32.0f * j, gz, zb);
-                    float g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-                    if (col < cols) {
-                        VertexSums s{acc[j][0], acc[j][1], acc[j][2], acc[j][3], acc[j][4], acc[j][5], acc[j][6],
-                                     acc[j][7]};
-                        vertex_adjoint(s, xl, zl, a, hm, pow2, gpos, gnrm, rowbase + col, vec3, g);
-                    }
                     float4* d = gbuf + kGbufF4 * (lane + 32 * j);
-                    d[0] = make_float4(g[0], g[1], g[2], g[3]);
-                    d[1] = make_float4(g[4], g[5], g[6], g[7]);
-                    d[2] = make_float4(xl, zl, 0.0f, 0.0f);
+                    d[0] = make_float4(acc[j][0], acc[j][1], acc[j][2], acc[j][3]);
+                    d[1] = make_float4(acc[j][4], acc[j][5], acc[j][6], acc[j][7]);
                 }
+            }
+            for (uint32_t j = 0; j < S; ++j) {
+                const uint32_t vi = lane + 32 * j;
+                const uint32_t col = c0 + vi;
+                float4* d = gbuf + kGbufF4 * vi;
+                float g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                if (col < cols) {
+                    const float4 s0 = d[0], s1 = d[1];
+                    const float xl = fmaf((float)vi, gx, xb0), zl = fmaf((float)vi, gz, zb0);
+                    VertexSums sm{s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+                    vertex_adjoint(sm, xl, zl, a, hm, pow2, gpos, gnrm, rowbase + col, vec3, g);
+                }
+                d[0] = make_float4(g[0], g[1], g[2], g[3]);
+                d[1] = make_float4(g[4], g[5], g[6], g[7]);
             }
             __syncwarp();
             // ---- phase 2: wave per lane, records of this tile
@@ -258,16 +273,10 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
 #pragma unroll
                 for (int i = 0; i < 11; ++i) m[i] = 0.0f;
                 const uint32_t t32 = __float_as_uint(st[0].x), a32 = __float_as_uint(st[0].y);
-                switch (S) {
-                    case 1: wave_moments<1>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
-                    case 2: wave_moments<2>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
-                    case 3: wave_moments<3>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
-                    case 4: wave_moments<4>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
-                    case 5: wave_moments<5>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
-                    case 6: wave_moments<6>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
-                    case 7: wave_moments<7>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
-                    default: wave_moments<8>(gbuf, nvalid0, t32, a32, st[0].z, st[0].w, k, m); break;
-                }
+                if (S == 8)
+                    wave_moments<8>(gbuf, 8, nvalid0, t32, a32, st[0].z, st[0].w, k, xb0, zb0, gx, gz, m);
+                else
+                    wave_moments<0>(gbuf, S, nvalid0, t32, a32, st[0].z, st[0].w, k, xb0, zb0, gx, gz, m);
                 if (active) {
                     float* r = partials + (size_t)kAdjRecord * (rec0 + wi);
 #pragma unroll
@@ -280,106 +289,115 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
     }
 }
 
-// One warp per (patch, wave): FP64 sum of the patch's records in tile order,
-// then the closed-form gradient (see the header comment for the moments).
-__global__ void __launch_bounds__(256) k_adj_pairs(const wt_patch* __restrict__ patches, uint32_t n,
-                                                   const wt_wave* __restrict__ waves, const char* __restrict__ ws,
-                                                   AdjLayout L) {
+// Column sums of the records.  A patch's records form a [tiles][waves * 11]
+// matrix; block (x, y) sums columns 32x .. 32x+31 of patch y over its tiles:
+// 32 tile-lanes per column, each summing every 32nd tile in order with Kahan
+// compensation (FP32: this part's FP64 rate is low), combined in a fixed
+// order.  Output: colsum[pair][11] (FP32).
+constexpr int kColLanes = 32;
+
+__global__ void __launch_bounds__(32 * kColLanes) k_adj_cols(uint32_t n, const char* __restrict__ ws, AdjLayout L) {
 #if __CUDA_ARCH__ >= 900
     cudaGridDependencySynchronize();
 #endif
+    __shared__ float red[kColLanes][32];
     const uint32_t* pair_off = reinterpret_cast<const uint32_t*>(ws + L.f.pair_off);
     const uint32_t* tile_pre = reinterpret_cast<const uint32_t*>(ws + L.f.tile_pre);
     const uint32_t* rank = reinterpret_cast<const uint32_t*>(ws + L.rank);
     const uint32_t* part_off = reinterpret_cast<const uint32_t*>(ws + L.part_off);
     const float* partials = reinterpret_cast<const float*>(ws + L.partials);
     const WsHeader* hdr = reinterpret_cast<const WsHeader*>(ws);
-    double* pair_grad = reinterpret_cast<double*>(const_cast<char*>(ws) + L.pair_grad);
-    const uint32_t total = pair_off[n];
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    const bool ran = hdr->total_tiles > 0 || total == 0;
-    for (uint32_t P = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < total; P += warps) {
-        uint32_t lo = 0, hi = n + 1;
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (pair_off[mid] <= P) lo = mid + 1; else hi = mid;
-        }
-        const uint32_t p = lo - 1, j = P - pair_off[p];
+    float* colsum = reinterpret_cast<float*>(const_cast<char*>(ws) + L.pair_grad);
+    const bool ran = hdr->total_tiles > 0;
+    const uint32_t cl = threadIdx.x & 31, tl = threadIdx.x >> 5;
+    for (uint32_t p = blockIdx.y; p < n; p += gridDim.y) {
         const uint32_t nw = pair_off[p + 1] - pair_off[p];
+        const uint32_t width = nw * kAdjRecord;
+        const uint32_t col = blockIdx.x * 32 + cl;
+        if (blockIdx.x * 32 >= width) continue;  // block-uniform
         const uint32_t qs = rank[p];
         const uint32_t ntiles = tile_pre[qs + 1] - tile_pre[qs];
-        double m[11];
-#pragma unroll
-        for (int i = 0; i < 11; ++i) m[i] = 0.0;
-        if (ran)
-            for (uint32_t k = lane; k < ntiles; k += 32) {
-                const float* r = partials + (size_t)kAdjRecord * (part_off[qs] + (size_t)k * nw + j);
-#pragma unroll
-                for (int i = 0; i < 11; ++i) m[i] += (double)r[i];
+        const float* base = partials + (size_t)kAdjRecord * part_off[qs];
+        float sum = 0.0f, comp = 0.0f;
+        if (ran && col < width) {
+#pragma unroll 8
+            for (uint32_t t = tl; t < ntiles; t += kColLanes) {
+                const float y = base[(size_t)t * width + col] - comp;
+                const float tt = sum + y;
+                comp = (tt - sum) - y;
+                sum = tt;
             }
-#pragma unroll
-        for (int i = 0; i < 11; ++i)
-            for (int o = 16; o > 0; o >>= 1) m[i] += __shfl_xor_sync(0xffffffffu, m[i], o);
-        if (lane == 0) {
-            const wt_patch Pt = patches[p];
-            const wt_wave w = waves[Pt.wave_offset + j];
-            const double lam = w.wavelength;
-            const double k = isinf(lam) ? 0.0 : kTwoPi / lam;
-            const double A = w.amplitude, Q = w.steepness_q, Dx = w.dir_x, Dz = w.dir_z, sp = w.speed;
-            const double t = Pt.time_s;
-            const double Mdx = m[0], Mdy = m[1], Mdz = m[2], Mjx = m[3], Mjz = m[4];
-            const double Mxx = m[5], Mxz = m[6], Mzz = m[7], T0 = m[8];
-            const double Xw = m[9] + (double)Pt.bl[0] * T0, Zw = m[10] + (double)Pt.bl[1] * T0;
-            const double P3 = Dx * Dx * Mxx + Dx * Dz * Mxz + Dz * Dz * Mzz;
-            const double gA = Q * (Dx * Mdx + Dz * Mdz) + k * (Dx * Mjx + Dz * Mjz) + Mdy + Q * k * P3;
-            const double gQ = A * (Dx * Mdx + Dz * Mdz + k * P3);
-            const double gk = A * (Dx * Mjx + Dz * Mjz + Q * P3) + Dx * Xw + Dz * Zw + sp * t * T0;
-            const double gDx = Q * A * Mdx + A * k * Mjx + Q * A * k * (2.0 * Dx * Mxx + Dz * Mxz) + k * Xw;
-            const double gDz = Q * A * Mdz + A * k * Mjz + Q * A * k * (2.0 * Dz * Mzz + Dx * Mxz) + k * Zw;
-            double* g = pair_grad + 8 * (size_t)P;
-            g[0] = gA;
-            g[1] = isinf(lam) ? 0.0 : -gk * k / lam;
-            g[2] = -Dz * gDx + Dx * gDz;
-            g[3] = gQ;
-            g[4] = T0;
-            g[5] = k * t * T0;
-            g[6] = gDx;
-            g[7] = gDz;
+        }
+        __syncthreads();
+        red[tl][cl] = sum;
+        __syncthreads();
+        if (tl == 0 && col < width) {
+            float total = 0.0f;
+#pragma unroll 8
+            for (int i = 0; i < kColLanes; ++i) total += red[i][cl];
+            colsum[(size_t)kAdjRecord * pair_off[p] + col] = total;
         }
     }
 }
 
-// One thread per wave: the patches that use it, in patch order.
+// One warp per wave: lane l takes patches l, l+32, ... that use the wave and
+// adds their closed-form gradients (FP64, from the patch's eleven column
+// sums); the lanes are then combined by a fixed shuffle tree.
 __global__ void __launch_bounds__(256) k_adj_waves(const wt_patch* __restrict__ patches, uint32_t n,
-                                                   uint32_t n_waves, const char* __restrict__ ws, AdjLayout L,
+                                                   const wt_wave* __restrict__ waves, uint32_t n_waves,
+                                                   const char* __restrict__ ws, AdjLayout L,
                                                    wt_wave_grad* __restrict__ grad) {
 #if __CUDA_ARCH__ >= 900
     cudaGridDependencySynchronize();
 #endif
     const uint32_t* pair_off = reinterpret_cast<const uint32_t*>(ws + L.f.pair_off);
-    const double* pair_grad = reinterpret_cast<const double*>(ws + L.pair_grad);
-    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < n_waves; w += gridDim.x * blockDim.x) {
+    const float* colsum = reinterpret_cast<const float*>(ws + L.pair_grad);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < n_waves; wi += warps) {
+        const wt_wave w = waves[wi];
+        const double lam = w.wavelength;
+        const double k = isinf(lam) ? 0.0 : kTwoPi / lam;
+        const double A = w.amplitude, Q = w.steepness_q, Dx = w.dir_x, Dz = w.dir_z, sp = w.speed;
         double g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (uint32_t p = 0; p < n; ++p) {
+        for (uint32_t p = lane; p < n; p += 32) {
             const uint32_t nw = pair_off[p + 1] - pair_off[p];  // 0 for invalid patches
             const uint32_t off = patches[p].wave_offset;
-            if (nw > 0 && w >= off && w - off < nw) {
-                const double* s = pair_grad + 8 * (size_t)(pair_off[p] + (w - off));
-#pragma unroll
-                for (int i = 0; i < 8; ++i) g[i] += s[i];
-            }
+            if (nw == 0 || wi < off || wi - off >= nw) continue;
+            const float* m = colsum + (size_t)kAdjRecord * (pair_off[p] + (wi - off));
+            const double t = patches[p].time_s;
+            const double Mdx = m[0], Mdy = m[1], Mdz = m[2], Mjx = m[3], Mjz = m[4];
+            const double Mxx = m[5], Mxz = m[6], Mzz = m[7], T0 = m[8];
+            const double Xw = (double)m[9] + (double)patches[p].bl[0] * T0;
+            const double Zw = (double)m[10] + (double)patches[p].bl[1] * T0;
+            const double P3 = Dx * Dx * Mxx + Dx * Dz * Mxz + Dz * Dz * Mzz;
+            const double gk = A * (Dx * Mjx + Dz * Mjz + Q * P3) + Dx * Xw + Dz * Zw + sp * t * T0;
+            const double gDx = Q * A * Mdx + A * k * Mjx + Q * A * k * (2.0 * Dx * Mxx + Dz * Mxz) + k * Xw;
+            const double gDz = Q * A * Mdz + A * k * Mjz + Q * A * k * (2.0 * Dz * Mzz + Dx * Mxz) + k * Zw;
+            g[0] += Q * (Dx * Mdx + Dz * Mdz) + k * (Dx * Mjx + Dz * Mjz) + Mdy + Q * k * P3;
+            g[1] += isinf(lam) ? 0.0 : -gk * k / lam;
+            g[2] += -Dz * gDx + Dx * gDz;
+            g[3] += A * (Dx * Mdx + Dz * Mdz + k * P3);
+            g[4] += T0;
+            g[5] += k * t * T0;
+            g[6] += gDx;
+            g[7] += gDz;
         }
-        wt_wave_grad o;
-        o.d_amplitude = (float)g[0];
-        o.d_wavelength = (float)g[1];
-        o.d_direction = (float)g[2];
-        o.d_steepness_q = (float)g[3];
-        o.d_phase = (float)g[4];
-        o.d_speed = (float)g[5];
-        o.d_dir_x = (float)g[6];
-        o.d_dir_z = (float)g[7];
-        grad[w] = o;
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            for (int o = 16; o > 0; o >>= 1) g[i] += __shfl_xor_sync(0xffffffffu, g[i], o);
+        if (lane == 0) {
+            wt_wave_grad o;
+            o.d_amplitude = (float)g[0];
+            o.d_wavelength = (float)g[1];
+            o.d_direction = (float)g[2];
+            o.d_steepness_q = (float)g[3];
+            o.d_phase = (float)g[4];
+            o.d_speed = (float)g[5];
+            o.d_dir_x = (float)g[6];
+            o.d_dir_z = (float)g[7];
+            grad[wi] = o;
+        }
     }
 }
 
@@ -415,8 +433,8 @@ uint64_t adjoint_records(const wt_patch& p) {
 }
 
 cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
-                           const HmDev& hm, const float* gpos, const float* gnrm, uint32_t flags,
-                           wt_wave_grad* grad, void* ws, const AdjLayout& L, cudaStream_t s) {
+                           uint32_t max_waves_per_patch, const HmDev& hm, const float* gpos, const float* gnrm,
+                           uint32_t flags, wt_wave_grad* grad, void* ws, const AdjLayout& L, cudaStream_t s) {
     char* w = static_cast<char*>(ws);
     const int sms = device_sms();
     cudaError_t e = launch_pdl(k_adj_scan, dim3(1), dim3(1024), 0, s, patches, n_patches, w, L);
@@ -435,12 +453,12 @@ cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt
     if (occ < 1) occ = 1;
     e = launch_pdl(k_adjoint, dim3(sms * occ), dim3(32 * kAdjWarps), smem, s, patches, hm, gpos, gnrm, flags, w, L);
     if (e != cudaSuccess) return e;
-    e = launch_pdl(k_adj_pairs, dim3(sms * 4), dim3(256), 0, s, patches, n_patches, waves,
-                   static_cast<const char*>(ws), L);
+    const dim3 cg((max_waves_per_patch * kAdjRecord + 31) / 32, n_patches < 65535u ? n_patches : 65535u);
+    e = launch_pdl(k_adj_cols, cg, dim3(32 * kColLanes), 0, s, n_patches, static_cast<const char*>(ws), L);
     if (e != cudaSuccess) return e;
-    const unsigned wb = (n_waves + 255) / 256;
+    const unsigned wb = (n_waves + 7) / 8 < (unsigned)sms * 16 ? (n_waves + 7) / 8 : (unsigned)sms * 16;
     if (wb == 0) return cudaSuccess;
-    return launch_pdl(k_adj_waves, dim3(wb), dim3(256), 0, s, patches, n_patches, n_waves,
+    return launch_pdl(k_adj_waves, dim3(wb), dim3(256), 0, s, patches, n_patches, waves, n_waves,
                       static_cast<const char*>(ws), L, grad);
 }
 

@@ -238,7 +238,10 @@ wt_status wt_gerstner_adjoint(const wt_patch* host_patches, const wt_patch* patc
     cudaError_t e = wt::launch_prep(patches, n_patches, waves, n_waves, P.hm, out_capacity, 32u * cfg.s, workspace,
                                     L.f, s);
     if (e != cudaSuccess) return cuda_fail(e, "prep launch");
-    e = wt::launch_adjoint(patches, n_patches, waves, n_waves, P.hm, d_pos, d_nrm, flags, grad_out, workspace, L, s);
+    uint32_t maxw = 0;
+    for (uint32_t i = 0; i < n_patches; ++i) maxw = host_patches[i].wave_count > maxw ? host_patches[i].wave_count : maxw;
+    e = wt::launch_adjoint(patches, n_patches, waves, n_waves, maxw > 0 ? maxw : 1, P.hm, d_pos, d_nrm, flags, grad_out,
+                           workspace, L, s);
     if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
     return WT_OK;
 }

@@ -79,7 +79,7 @@ inline WsLayout ws_layout(uint32_t n_patches, uint64_t total_wave_slots) {
 // rank    u32[n]      sorted position of each patch
 // partoff u32[n+1]    exclusive prefix of records (tiles x waves) over the sorted order
 // partial float[11 x records]   per-(tile, wave) FP32 partial sums
-// pairg   double[8 x wave slots] per-(patch, wave) gradient
+// colsum  float[11 x wave slots] per-(patch, wave) sums of the records
 constexpr int kAdjRecord = 11;
 
 struct AdjLayout {
@@ -134,8 +134,8 @@ bool forward_config_supported(const FwdConfig& cfg);
 // Records (tiles x waves) of one patch, as the adjoint lays them out.
 uint64_t adjoint_records(const wt_patch& p);
 cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
-                           const HmDev& hm, const float* gpos, const float* gnrm, uint32_t flags,
-                           wt_wave_grad* grad, void* ws, const AdjLayout& L, cudaStream_t s);
+                           uint32_t max_waves_per_patch, const HmDev& hm, const float* gpos, const float* gnrm,
+                           uint32_t flags, wt_wave_grad* grad, void* ws, const AdjLayout& L, cudaStream_t s);
 
 // ---- host helpers (wt_api.cpp) ---------------------------------------------
 void set_last_error(const char* msg);  // message returned by wt_last_error() on this thread
