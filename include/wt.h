@@ -274,7 +274,8 @@ typedef struct wt_tuning {
     uint32_t warps_per_block; /* 4, 6, 8 or 16 (0 = default 8) */
     uint32_t blocks_per_sm;   /* 0 = as many as fit */
     uint32_t wave_chunk;      /* waves staged per warp at a time: 8, 16 or 32 (0 = 32) */
-    uint32_t reserved;        /* must be 0 */
+    uint32_t max_vertices_per_lane; /* widest tile = 32 * this; 4 or 8 (0 = 8).  4 halves
+                                       the accumulator registers for more resident warps */
 } wt_tuning;
 
 wt_status wt_set_tuning(const wt_tuning* tuning); /* NULL restores the defaults */

@@ -49,7 +49,7 @@ class CHeightmap(C.Structure):
 
 class CTuning(C.Structure):
     _fields_ = [("warps_per_block", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("wave_chunk", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("max_vertices_per_lane", C.c_uint32)]
 
 
 class CWave(C.Structure):
@@ -255,7 +255,7 @@ class Surface:
             self.patches.data_ptr(), self.n_patches, self.waves.data_ptr(), self.n_waves,
             C.byref(hm) if hm is not None else None, pos.data_ptr(), _ptr(nrm), pos.shape[0], flags,
             self.workspace.data_ptr(), self.workspace.numel(), reps, C.byref(best), stream_handle(stream)))
-        return {f: getattr(best, f) for f, _ in CTuning._fields_ if f != "reserved"}
+        return {f: getattr(best, f) for f, _ in CTuning._fields_}
 
 
 def grid_indices(cols: int, rows: int, base_vertex: int = 0, stream=None):
@@ -287,14 +287,15 @@ def wave_from_reference(amplitude_A, frequency_w, phase_constant_phi, steepness_
     return out
 
 
-def set_tuning(warps_per_block: int = 0, blocks_per_sm: int = 0, wave_chunk: int = 0) -> None:
-    check(lib().wt_set_tuning(C.byref(CTuning(warps_per_block, blocks_per_sm, wave_chunk, 0))))
+def set_tuning(warps_per_block: int = 0, blocks_per_sm: int = 0, wave_chunk: int = 0,
+               max_vertices_per_lane: int = 0) -> None:
+    check(lib().wt_set_tuning(C.byref(CTuning(warps_per_block, blocks_per_sm, wave_chunk, max_vertices_per_lane))))
 
 
 def get_tuning() -> dict:
     t = CTuning()
     check(lib().wt_get_tuning(C.byref(t)))
-    return {f: getattr(t, f) for f, _ in CTuning._fields_ if f != "reserved"}
+    return {f: getattr(t, f) for f, _ in CTuning._fields_}
 
 
 def measure_peaks(stream=None) -> tuple[float, float]:

@@ -205,7 +205,7 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
         const uint64_t out0 = patches[p].out_offset;
         const PatchAux a = aux[p];
         uint32_t S, tpr;
-        row_tiling(cols, &S, &tpr);
+        row_tiling(cols, 8, &S, &tpr);
         const uint32_t row = lt / tpr;
         const uint32_t c0 = (lt - row * tpr) * 32u * S;
         if (nwaves > 0) {
@@ -220,16 +220,7 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
                 __syncwarp();
                 if (lane < nw) stage_wave(coef[a.pair_offset + w0 + lane], c0, row, wst + kStage * lane);
                 __syncwarp();
-                switch (S) {
-                    case 1: wave_loop<1>(acc, wst, nw, lane); break;
-                    case 2: wave_loop<2>(acc, wst, nw, lane); break;
-                    case 3: wave_loop<3>(acc, wst, nw, lane); break;
-                    case 4: wave_loop<4>(acc, wst, nw, lane); break;
-                    case 5: wave_loop<5>(acc, wst, nw, lane); break;
-                    case 6: wave_loop<6>(acc, wst, nw, lane); break;
-                    case 7: wave_loop<7>(acc, wst, nw, lane); break;
-                    default: wave_loop<8>(acc, wst, nw, lane); break;
-                }
+                wave_loop_dispatch<8>(S, acc, wst, nw, lane);
             }
             const float v = (float)row * a.inv_rm1;
             const float gx = (a.e1x + v * a.e3x) * a.inv_cm1, gz = (a.e1z + v * a.e3z) * a.inv_cm1;
@@ -428,7 +419,7 @@ cudaError_t launch_pdl(K kernel, dim3 grid, dim3 block, size_t smem, cudaStream_
 uint64_t adjoint_records(const wt_patch& p) {
     if (p.cols < 2 || p.rows < 2) return 0;
     uint32_t S, tpr;
-    dev::row_tiling(p.cols, &S, &tpr);
+    dev::row_tiling(p.cols, 8, &S, &tpr);
     return (uint64_t)p.rows * tpr * p.wave_count;
 }
 

@@ -234,9 +234,7 @@ wt_status wt_gerstner_adjoint(const wt_patch* host_patches, const wt_patch* patc
         cudaError_t e = cudaMemsetAsync(grad_out, 0, sizeof(wt_wave_grad) * n_waves, s);
         return e == cudaSuccess ? WT_OK : cuda_fail(e, "clearing grad_out");
     }
-    const wt::FwdConfig cfg = current_cfg();
-    cudaError_t e = wt::launch_prep(patches, n_patches, waves, n_waves, P.hm, out_capacity, 32u * cfg.s, workspace,
-                                    L.f, s);
+    cudaError_t e = wt::launch_prep(patches, n_patches, waves, n_waves, P.hm, out_capacity, 256u, workspace, L.f, s);
     if (e != cudaSuccess) return cuda_fail(e, "prep launch");
     uint32_t maxw = 0;
     for (uint32_t i = 0; i < n_patches; ++i) maxw = host_patches[i].wave_count > maxw ? host_patches[i].wave_count : maxw;
@@ -302,11 +300,13 @@ wt_status wt_wave_from_reference(float amplitude_A, float frequency_w, float pha
 wt_status wt_set_tuning(const wt_tuning* t) {
     wt::FwdConfig c = {8, 32, 8, 0};
     if (t) {
-        if (t->reserved != 0) return fail(WT_ERR_INVALID_ARG, "tuning: reserved must be 0");
+        c.s = t->max_vertices_per_lane ? (int)t->max_vertices_per_lane : 8;
         c.warps = t->warps_per_block ? (int)t->warps_per_block : 8;
         c.blocks_per_sm = (int)t->blocks_per_sm;
         c.chunk = t->wave_chunk ? (int)t->wave_chunk : 32;
-        if (!wt::forward_config_supported(c)) return fail(WT_ERR_INVALID_ARG, "tuning: warps_per_block must be 4, 6, 8 or 16");
+        if (!wt::forward_config_supported(c))
+            return fail(WT_ERR_INVALID_ARG, "tuning: unsupported (warps_per_block, max_vertices_per_lane) = (%d, %d)",
+                        c.warps, c.s);
         if (c.chunk != 8 && c.chunk != 16 && c.chunk != 32) return fail(WT_ERR_INVALID_ARG, "tuning: wave_chunk must be 8, 16 or 32");
         if (t->blocks_per_sm > 64) return fail(WT_ERR_INVALID_ARG, "tuning: blocks_per_sm > 64");
     }
@@ -321,7 +321,7 @@ wt_status wt_get_tuning(wt_tuning* t) {
     t->warps_per_block = (uint32_t)c.warps;
     t->blocks_per_sm = (uint32_t)c.blocks_per_sm;
     t->wave_chunk = (uint32_t)c.chunk;
-    t->reserved = 0;
+    t->max_vertices_per_lane = (uint32_t)c.s;
     return WT_OK;
 }
 
@@ -336,15 +336,15 @@ wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches, cons
     if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
     e = cudaEventCreate(&e1);
     if (e != cudaSuccess) { cudaEventDestroy(e0); return cuda_fail(e, "cudaEventCreate"); }
-    const int warps[] = {4, 6, 8, 16};
-    const int chunks[] = {8, 16, 32};
+    const int shapes[][2] = {{8, 4}, {8, 6}, {8, 8}, {8, 16}, {4, 8}, {4, 16}};  // (vertices per lane, warps)
+    const int chunks[] = {16, 32};
     float best_ms = 1e30f;
     wt::FwdConfig best_cfg = current_cfg();
     wt_status st = WT_OK;
     for (int pass = 0; pass < 2 && st == WT_OK; ++pass)
-    for (int w : warps) {
+    for (const auto& sh : shapes) {
         for (int ch : chunks) {
-            wt::FwdConfig c = {8, ch, w, 0};
+            wt::FwdConfig c = {sh[0], ch, sh[1], 0};
             st = run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags,
                               workspace, workspace_bytes, s, c);
             if (st != WT_OK) break;

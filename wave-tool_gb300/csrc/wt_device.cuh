@@ -52,10 +52,11 @@ static __device__ uint32_t block_exclusive_scan(uint32_t* a, uint32_t n) {
 // Tiling of one patch row: tiles of 32*S columns, S in 1..8, choosing the S
 // whose tiles cover the row with the least padding, with a preference for
 // larger S (each wave's start-up costs about as much as two vertices).
-__host__ __device__ __forceinline__ void row_tiling(uint32_t cols, uint32_t* S_out, uint32_t* tpr_out) {
-    uint32_t bestS = 8, bestT = (cols + 255) / 256;
-    float best = 256.0f * bestT * (1.0f + 2.0f / 8.0f);
-    for (uint32_t S = 7; S >= 1; --S) {
+__host__ __device__ __forceinline__ void row_tiling(uint32_t cols, uint32_t smax, uint32_t* S_out,
+                                                    uint32_t* tpr_out) {
+    uint32_t bestS = smax, bestT = (cols + 32 * smax - 1) / (32 * smax);
+    float best = 32.0f * smax * bestT * (1.0f + 2.0f / (float)smax);
+    for (uint32_t S = smax - 1; S >= 1; --S) {
         const uint32_t t = (cols + 32 * S - 1) / (32 * S);
         const float cost = 32.0f * S * t * (1.0f + 2.0f / (float)S);
         if (cost < best) { best = cost; bestS = S; bestT = t; }
@@ -213,8 +214,8 @@ __device__ __forceinline__ void stage_wave(const PairCoef& c, uint32_t c0, uint3
 
 // The wave loop of one tile for a compile-time S: sums of nw staged waves
 // into acc[0..S-1].
-template <int S>
-__device__ __forceinline__ void wave_loop(float (&acc)[8][8], const float4* __restrict__ wst, uint32_t nw,
+template <int S, int SMAX>
+__device__ __forceinline__ void wave_loop(float (&acc)[SMAX][8], const float4* __restrict__ wst, uint32_t nw,
                                           uint32_t lane) {
 #pragma unroll 2
     for (uint32_t i = 0; i < nw; ++i) {
@@ -245,6 +246,37 @@ __device__ __forceinline__ void wave_loop(float (&acc)[8][8], const float4* __re
             acc[j][5] = fmaf(w2.y, s, acc[j][5]);
             acc[j][6] = fmaf(w2.z, s, acc[j][6]);
             acc[j][7] = fmaf(w2.w, s, acc[j][7]);
+        }
+    }
+}
+
+}  // namespace dev
+}  // namespace wt
+
+namespace wt {
+namespace dev {
+
+// The wave loop for the tile's S (warp-uniform), compile-time in each branch.
+template <int SMAX>
+__device__ __forceinline__ void wave_loop_dispatch(uint32_t S, float (&acc)[SMAX][8], const float4* __restrict__ wst,
+                                                   uint32_t nw, uint32_t lane) {
+    if (SMAX == 4) {
+        switch (S) {
+            case 1: wave_loop<1, SMAX>(acc, wst, nw, lane); break;
+            case 2: wave_loop<2, SMAX>(acc, wst, nw, lane); break;
+            case 3: wave_loop<3, SMAX>(acc, wst, nw, lane); break;
+            default: wave_loop<(SMAX >= 4 ? 4 : SMAX), SMAX>(acc, wst, nw, lane); break;
+        }
+    } else {
+        switch (S) {
+            case 1: wave_loop<1, SMAX>(acc, wst, nw, lane); break;
+            case 2: wave_loop<2, SMAX>(acc, wst, nw, lane); break;
+            case 3: wave_loop<3, SMAX>(acc, wst, nw, lane); break;
+            case 4: wave_loop<4, SMAX>(acc, wst, nw, lane); break;
+            case 5: wave_loop<(SMAX >= 5 ? 5 : SMAX), SMAX>(acc, wst, nw, lane); break;
+            case 6: wave_loop<(SMAX >= 6 ? 6 : SMAX), SMAX>(acc, wst, nw, lane); break;
+            case 7: wave_loop<(SMAX >= 7 ? 7 : SMAX), SMAX>(acc, wst, nw, lane); break;
+            default: wave_loop<SMAX, SMAX>(acc, wst, nw, lane); break;
         }
     }
 }

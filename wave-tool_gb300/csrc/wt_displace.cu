@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
         if (!ok) flag_error(hdr, WT_ERR_INVALID_ARG, p);
         pair_off[p] = ok ? P.wave_count : 0u;
         uint32_t S, tpr;
-        row_tiling(P.cols, &S, &tpr);
+        row_tiling(P.cols, tile_cols / 32, &S, &tpr);
         tiles[p] = ok ? P.rows * tpr : 0u;
         const uint32_t key = P.wave_count < kSortBins ? P.wave_count : kSortBins - 1;
         atomicAdd(&bins[kSortBins - 1 - key], 1u);  // descending wave count
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(256) k_prep_coef(const wt_patch* __restrict__ 
 }
 
 // ---- stage 3: the persistent forward kernel --------------------------------
-template <int THREADS, int MINB>
+template <int THREADS, int MINB, int SMAX>
 __global__ void __launch_bounds__(THREADS, MINB)
 k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ pos,
           float* __restrict__ nrm, uint32_t flags, char* __restrict__ ws, WsLayout L, uint32_t chunk) {
@@ -290,13 +290,13 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
         const uint64_t out0 = patches[p].out_offset;
         const PatchAux a = aux[p];
         uint32_t S, tpr;
-        row_tiling(cols, &S, &tpr);
+        row_tiling(cols, SMAX, &S, &tpr);
         const uint32_t row = lt / tpr;
         const uint32_t c0 = (lt - row * tpr) * 32u * S;
 
-        float acc[8][8];
+        float acc[SMAX][8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
+        for (int j = 0; j < SMAX; ++j)
 #pragma unroll
             for (int m = 0; m < 8; ++m) acc[j][m] = 0.0f;
 
@@ -307,16 +307,7 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
                 stage_wave(coef[a.pair_offset + w0 + lane], c0, row, wst + kStage * lane);
             }
             __syncwarp();
-            switch (S) {  // warp-uniform
-                case 1: wave_loop<1>(acc, wst, nw, lane); break;
-                case 2: wave_loop<2>(acc, wst, nw, lane); break;
-                case 3: wave_loop<3>(acc, wst, nw, lane); break;
-                case 4: wave_loop<4>(acc, wst, nw, lane); break;
-                case 5: wave_loop<5>(acc, wst, nw, lane); break;
-                case 6: wave_loop<6>(acc, wst, nw, lane); break;
-                case 7: wave_loop<7>(acc, wst, nw, lane); break;
-                default: wave_loop<8>(acc, wst, nw, lane); break;
-            }
+            wave_loop_dispatch<SMAX>(S, acc, wst, nw, lane);
         }
 
         // grid position along the row: x(col) = col * du * (e1 + v e3) + v e2
@@ -326,7 +317,7 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
         const float xb = fmaf(colf, gx, v * a.e2x), zb = fmaf(colf, gz, v * a.e2z);
         const uint64_t rowbase = out0 + (uint64_t)row * cols;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
+        for (int j = 0; j < SMAX; ++j) {
             const uint32_t col = c0 + lane + 32 * j;
             if ((uint32_t)j < S && col < cols) {
                 const float xl = fmaf(32.0f * j, gx, xb);
@@ -385,7 +376,7 @@ __global__ void __launch_bounds__(256) k_forward_naive(const wt_patch* __restric
     }
 }
 
-template <int THREADS, int MINB>
+template <int THREADS, int MINB, int SMAX>
 cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const HmDev& hm, float* pos,
                          float* nrm, uint32_t flags, void* ws, const WsLayout& L, cudaStream_t s) {
     constexpr int kMaxDev = 64;
@@ -396,7 +387,7 @@ cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const Hm
     if (sms[dev] == 0) {
         int o = 0, m = 0;
         cudaDeviceGetAttribute(&m, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_forward<THREADS, MINB>, THREADS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_forward<THREADS, MINB, SMAX>, THREADS, 0);
         occ[dev] = o < 1 ? 1 : o;
         sms[dev] = m;
     }
@@ -412,8 +403,8 @@ cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const Hm
     lc.attrs = attr;
     lc.numAttrs = 1;
     const uint32_t chunk = cfg.chunk >= 1 && cfg.chunk <= 32 ? (uint32_t)cfg.chunk : 32u;
-    return cudaLaunchKernelEx(&lc, k_forward<THREADS, MINB>, patches, hm, pos, nrm, flags, static_cast<char*>(ws), L,
-                              chunk);
+    return cudaLaunchKernelEx(&lc, k_forward<THREADS, MINB, SMAX>, patches, hm, pos, nrm, flags,
+                              static_cast<char*>(ws), L, chunk);
 }
 
 }  // namespace
@@ -447,17 +438,24 @@ cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wa
 }
 
 bool forward_config_supported(const FwdConfig& c) {
-    return c.warps == 8 || c.warps == 6 || c.warps == 4 || c.warps == 16;
+    if (c.s == 8) return c.warps == 8 || c.warps == 6 || c.warps == 4 || c.warps == 16;
+    if (c.s == 4) return c.warps == 8 || c.warps == 16;
+    return false;
 }
 
 cudaError_t launch_forward(const FwdConfig& cfg, const wt_patch* patches, uint32_t, const HmDev& hm,
                            float* pos, float* nrm, uint32_t flags, void* ws, const WsLayout& L,
                            cudaStream_t s) {
     // warps per block; the minimum-blocks hint sets the register budget
-    if (cfg.warps == 8) return launch_fwd_t<256, 2>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 128 regs
-    if (cfg.warps == 6) return launch_fwd_t<192, 2>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 168 regs
-    if (cfg.warps == 4) return launch_fwd_t<128, 3>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 168 regs
-    if (cfg.warps == 16) return launch_fwd_t<512, 1>(cfg, patches, hm, pos, nrm, flags, ws, L, s);  // 128 regs
+    if (cfg.s == 4) {
+        if (cfg.warps == 8) return launch_fwd_t<256, 3, 4>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 85 regs
+        if (cfg.warps == 16) return launch_fwd_t<512, 1, 4>(cfg, patches, hm, pos, nrm, flags, ws, L, s);  // 128 regs
+        return cudaErrorInvalidValue;
+    }
+    if (cfg.warps == 8) return launch_fwd_t<256, 2, 8>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 128 regs
+    if (cfg.warps == 6) return launch_fwd_t<192, 2, 8>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 168 regs
+    if (cfg.warps == 4) return launch_fwd_t<128, 3, 8>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 168 regs
+    if (cfg.warps == 16) return launch_fwd_t<512, 1, 8>(cfg, patches, hm, pos, nrm, flags, ws, L, s);  // 128 regs
     return cudaErrorInvalidValue;
 }
 
