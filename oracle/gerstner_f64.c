@@ -120,41 +120,58 @@ static void wave_sums(const wt_patch* p, const wt_wave* waves, double x, double 
     }
 }
 
+/* One vertex: displaced position, displacement, unit normal, texel-edge
+ * distance (any output may be NULL). */
+static void vertex_f64(const wt_patch* p, const wt_wave* waves, const wto_heightmap* hm, uint32_t row,
+                       uint32_t col, double* pos, double* disp, double* nrm, double* edge) {
+    double x, z;
+    wto_grid_xz_f64(p, row, col, &x, &z);
+    wsum s;
+    wave_sums(p, waves, x, z, &s);
+    /* dP/dx and dP/dz of the Gerstner surface */
+    double px[3] = {1.0 - s.sxx, s.jx, -s.sxz};
+    double pz[3] = {-s.sxz, s.jz, 1.0 - s.szz};
+    double dy = s.dy;
+    double e = INFINITY;
+    if (hm && hm->texels) {
+        hm_sample h = sample_hm(hm, x + s.dx, z + s.dz);
+        dy += h.h;
+        px[1] += h.hx * px[0] + h.hz * px[2];
+        pz[1] += h.hx * pz[0] + h.hz * pz[2];
+        e = h.edge;
+    }
+    dy += (double)p->y_offset;
+    if (pos) { pos[0] = x + s.dx; pos[1] = dy; pos[2] = z + s.dz; }
+    if (disp) { disp[0] = s.dx; disp[1] = dy; disp[2] = s.dz; }
+    if (nrm) {
+        double n0 = pz[1] * px[2] - pz[2] * px[1];
+        double n1 = pz[2] * px[0] - pz[0] * px[2];
+        double n2 = pz[0] * px[1] - pz[1] * px[0];
+        double inv = 1.0 / sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+        nrm[0] = n0 * inv; nrm[1] = n1 * inv; nrm[2] = n2 * inv;
+    }
+    if (edge) *edge = e;
+}
+
 void wto_displace_f64(const wt_patch* p, const wt_wave* waves, const wto_heightmap* hm,
                       uint32_t row0, uint32_t row1,
                       double* pos, double* disp, double* nrm, double* edge) {
-    for (uint32_t row = row0; row < row1 && row < p->rows; ++row) {
+    for (uint32_t row = row0; row < row1 && row < p->rows; ++row)
         for (uint32_t col = 0; col < p->cols; ++col) {
             size_t v = (size_t)row * p->cols + col;
-            double x, z;
-            wto_grid_xz_f64(p, row, col, &x, &z);
-            wsum s;
-            wave_sums(p, waves, x, z, &s);
-            /* dP/dx and dP/dz of the Gerstner surface */
-            double px[3] = {1.0 - s.sxx, s.jx, -s.sxz};
-            double pz[3] = {-s.sxz, s.jz, 1.0 - s.szz};
-            double dy = s.dy;
-            double e = INFINITY;
-            if (hm && hm->texels) {
-                hm_sample h = sample_hm(hm, x + s.dx, z + s.dz);
-                dy += h.h;
-                px[1] += h.hx * px[0] + h.hz * px[2];
-                pz[1] += h.hx * pz[0] + h.hz * pz[2];
-                e = h.edge;
-            }
-            dy += (double)p->y_offset;
-            if (pos) { pos[3 * v] = x + s.dx; pos[3 * v + 1] = dy; pos[3 * v + 2] = z + s.dz; }
-            if (disp) { disp[3 * v] = s.dx; disp[3 * v + 1] = dy; disp[3 * v + 2] = s.dz; }
-            if (nrm) {
-                double n0 = pz[1] * px[2] - pz[2] * px[1];
-                double n1 = pz[2] * px[0] - pz[0] * px[2];
-                double n2 = pz[0] * px[1] - pz[1] * px[0];
-                double inv = 1.0 / sqrt(n0 * n0 + n1 * n1 + n2 * n2);
-                nrm[3 * v] = n0 * inv; nrm[3 * v + 1] = n1 * inv; nrm[3 * v + 2] = n2 * inv;
-            }
-            if (edge) edge[v] = e;
+            vertex_f64(p, waves, hm, row, col, pos ? pos + 3 * v : NULL, disp ? disp + 3 * v : NULL,
+                       nrm ? nrm + 3 * v : NULL, edge ? edge + v : NULL);
         }
-    }
+}
+
+void wto_displace_f64_rows(const wt_patch* p, const wt_wave* waves, const wto_heightmap* hm,
+                           const uint32_t* rows, uint32_t n_rows, double* pos, double* disp, double* nrm) {
+    for (uint32_t k = 0; k < n_rows; ++k)
+        for (uint32_t col = 0; col < p->cols; ++col) {
+            size_t v = (size_t)k * p->cols + col;
+            vertex_f64(p, waves, hm, rows[k], col, pos ? pos + 3 * v : NULL, disp ? disp + 3 * v : NULL,
+                       nrm ? nrm + 3 * v : NULL, NULL);
+        }
 }
 
 /* Reverse mode by hand.  Per vertex the loss touches the wave sums through

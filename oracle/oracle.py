@@ -62,6 +62,7 @@ def lib():
         vp = C.c_void_p
         _lib.wto_displace_f64.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp, vp, vp, vp]
         _lib.wto_adjoint_f64.argtypes = [vp, vp, vp, vp, vp, vp]
+        _lib.wto_displace_f64_rows.argtypes = [vp, vp, vp, vp, C.c_uint32, vp, vp, vp]
         _lib.wto_reference_vertex.argtypes = [C.POINTER(RefUniforms), C.c_uint32, C.c_uint32,
                                               C.POINTER(RefOutputs)]
         for f in (_lib.wto_cpu_reference, _lib.wto_cpu_analytic):
@@ -120,6 +121,19 @@ def displace_f64(patches, waves, texels=None, hm_params=None, rows=None):
                            _ptr(pos[o:o + nv]), _ptr(disp[o:o + nv]), _ptr(nrm[o:o + nv]),
                            _ptr(edge[o:o + nv]))
     return pos, disp, nrm, edge
+
+
+def displace_f64_rows(patch, waves, rows, texels=None, hm_params=None):
+    """FP64 truth on selected rows of one patch: (disp, nrm), row k at k*cols."""
+    L = lib()
+    rows = np.ascontiguousarray(rows, dtype=np.uint32)
+    cols = int(patch["cols"])
+    disp = np.zeros((len(rows) * cols, 3)); nrm = np.zeros((len(rows) * cols, 3))
+    hm = make_hm(texels, hm_params.sample_scale, hm_params.disp_scale, hm_params.wrap) if texels is not None else None
+    pp = np.array(patch).copy()
+    L.wto_displace_f64_rows(_ptr(pp), _ptr(waves), C.byref(hm) if hm else None, _ptr(rows), len(rows), None,
+                            _ptr(disp), _ptr(nrm))
+    return disp, nrm
 
 
 def adjoint_f64(patches, waves, gpos, gnrm=None, texels=None, hm_params=None):

@@ -54,6 +54,11 @@ void wto_displace_f64(const wt_patch* p, const wt_wave* waves, const wto_heightm
                       uint32_t row0, uint32_t row1,
                       double* pos, double* disp, double* nrm, double* edge);
 
+/* The same for an explicit list of rows, written compactly (row k of the
+ * list at k*cols). */
+void wto_displace_f64_rows(const wt_patch* p, const wt_wave* waves, const wto_heightmap* hm,
+                           const uint32_t* rows, uint32_t n_rows, double* pos, double* disp, double* nrm);
+
 /* Undisplaced grid position (x, z) of vertex (row, col), water-grid.vert:87-91
  * and :123-125 in FP64. */
 void wto_grid_xz_f64(const wt_patch* p, uint32_t row, uint32_t col, double* x, double* z);

@@ -186,3 +186,36 @@ def test_reference_default_waves_through_conversion(wt, oracle, gpu):
                                         texels=None, disp_scale=0.0)
     ref = oracle.reference_vertex(U, 0, L * L)["position"][:, :3]
     assert np.abs(pos[:, :3] - ref).max() < 2e-5
+
+
+@pytest.mark.parametrize("t", [1.0e2, 1.0e4, 1.0e6])
+def test_precision_stress_2048sq_128waves(wt, oracle, gpu, t):
+    """The precision configuration at full size (2048^2 vertices, 128 waves,
+    t = 1e2 / 1e4 / 1e6 s): every vertex through the GPU in both phase modes,
+    32 rows spread over the patch against FP64.  FP64-reduced phase stays
+    within 1e-5; the FP32-naive phase of the reference (water-grid.vert:78)
+    degrades with t.  Prints max / RMS displacement error and max normal angle."""
+    import torch
+    from wave_tool_gb300 import workloads
+    w = workloads.config5(time_s=t)
+    surf = wt.Surface(w.patches, w.waves)
+    rows = np.linspace(0, 2047, 32).astype(int)
+    cols = 2048
+    res = {}
+    for mode, flags in (("fp64_phase", wt.WT_OUT_DISPLACEMENT),
+                        ("fp32_naive", wt.WT_OUT_DISPLACEMENT | wt.WT_PHASE_FP32_NAIVE)):
+        pos, nrm = surf.displace(flags=flags)
+        torch.cuda.synchronize()
+        idx = (rows[:, None] * cols + np.arange(cols)[None, :]).ravel()
+        res[mode] = (pos[torch.from_numpy(idx).cuda()].cpu().numpy(), nrm[torch.from_numpy(idx).cuda()].cpu().numpy())
+        del pos, nrm
+    disp64, nrm64 = oracle.displace_f64_rows(w.patches[0], w.waves, rows)
+    out = {}
+    for mode, (p, n) in res.items():
+        e = np.abs(p[:, :3].astype(np.float64) - disp64)
+        out[mode] = (e.max() / np.abs(disp64).max(), np.sqrt((e ** 2).mean()) / np.abs(disp64).max(),
+                     angle_deg(n[:, :3].astype(np.float64), nrm64).max())
+    print(f"t={t:g}: " + "; ".join(f"{m} max {a:.2e} rms {b:.2e} normal {c:.2e} deg" for m, (a, b, c) in out.items()))
+    assert out["fp64_phase"][0] <= DISP_TOL
+    if t >= 1e4:
+        assert out["fp32_naive"][0] > 10 * out["fp64_phase"][0]
