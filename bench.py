@@ -50,7 +50,7 @@ def parse_args():
     ap.add_argument("--mode", choices=["forward", "adjoint"], default="forward",
                     help="'adjoint' times only wt_gerstner_adjoint on 64 uneven patches (for profiling)")
     ap.add_argument("--tuning", default="auto",
-                    help="'auto' (autotune before timing) or WARPS,CHUNK to fix the launch shape")
+                    help="'auto' (autotune before timing) or WARPS,CHUNK[,VPL,EPI] to fix the launch shape")
     return ap.parse_args()
 
 
@@ -216,6 +216,7 @@ def side_measurements(wt, workloads, surf, pos, nrm, flags, flush, stream, ms_st
                     ("adjoint_batched_64_uneven_patches", workloads.config5_batched_adjoint())):
         sa = wt.Surface(w.patches, w.waves, wt.heightmap_from(w.heightmap))
         pa, na = sa.alloc_outputs(flags)
+        sa.autotune(pa, na, flags=flags, reps=5)
         gen = torch.Generator(device="cuda").manual_seed(1)
         gp = torch.randn(pa.shape, device="cuda", generator=gen)
         gn = torch.randn(na.shape, device="cuda", generator=gen)
@@ -231,6 +232,8 @@ def side_measurements(wt, workloads, surf, pos, nrm, flags, flush, stream, ms_st
         w5 = workloads.config5(time_s=t)
         s5 = wt.Surface(w5.patches, w5.waves)
         p5, n5 = s5.alloc_outputs(flags)
+        if t == 1.0e2:
+            prec["tuning"] = s5.autotune(p5, n5, flags=flags, reps=5)
         for _ in range(3):
             s5.displace(p5, n5, flags=flags)
         ms5 = _event_ms(lambda: s5.displace(p5, n5, flags=flags), 10, stream, flush)
@@ -273,8 +276,8 @@ def run_ours(args):
     if args.tuning == "auto":
         tuning = surf.autotune(pos, nrm, flags=flags, reps=5)  # launch shape, before any timing
     else:
-        w_, c_ = (int(x) for x in args.tuning.split(","))
-        wt.set_tuning(w_, 0, c_)
+        vals = [int(x) for x in args.tuning.split(",")] + [8, 1]
+        wt.set_tuning(vals[0], 0, vals[1], vals[2], vals[3])
         tuning = wt.get_tuning()
     for _ in range(args.warmup):
         step()

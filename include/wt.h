@@ -267,7 +267,9 @@ wt_status wt_wave_from_reference(float amplitude_A, float frequency_w,
 
 /* ---- launch tuning ------------------------------------------------------- */
 
-/* Launch shape of the persistent forward kernel.  Process-wide; applies to
+/* Launch shape of the persistent forward kernel (supported: 8 vertices per
+ * lane with 8 or 16 warps and either epilogue; 4 vertices per lane with 8 warps
+ * and the register epilogue).  Process-wide; applies to
  * launches issued after it is set.  No reference counterpart (the reference
  * has one fixed draw call). */
 typedef struct wt_tuning {
@@ -276,15 +278,21 @@ typedef struct wt_tuning {
     uint32_t wave_chunk;      /* waves staged per warp at a time: 8, 16 or 32 (0 = 32) */
     uint32_t max_vertices_per_lane; /* widest tile = 32 * this; 4 or 8 (0 = 8).  4 halves
                                        the accumulator registers for more resident warps */
+    uint32_t epilogue_in_shared;    /* 1: per-vertex epilogue as one rolled loop over sums
+                                       parked in shared memory; 0: unrolled from registers */
 } wt_tuning;
 
-wt_status wt_set_tuning(const wt_tuning* tuning); /* NULL restores the defaults */
+/* The default shape (used where the autotuner has not run); setting it also
+ * drops the autotuned shapes.  NULL restores the built-in default. */
+wt_status wt_set_tuning(const wt_tuning* tuning);
 wt_status wt_get_tuning(wt_tuning* tuning);
 
 /* Times every candidate launch shape on the given (device-resident) workload
- * with `reps` launches each (CUDA events on `stream`, synchronising it),
- * makes the fastest the process-wide tuning and returns it in *best (may be
- * NULL).  Arguments as wt_gerstner_displace; the outputs are overwritten. */
+ * with `reps` launches each (CUDA events on `stream`, synchronising it) and
+ * caches the fastest for the workload's shape bucket (the bit lengths of
+ * n_patches and n_waves): later wt_gerstner_displace calls in that bucket use
+ * it.  Returns it in *best (may be NULL).  Arguments as wt_gerstner_displace;
+ * the outputs are overwritten. */
 wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches,
                                const wt_wave* waves, uint32_t n_waves,
                                const wt_heightmap* hm,

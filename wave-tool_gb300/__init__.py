@@ -49,7 +49,7 @@ class CHeightmap(C.Structure):
 
 class CTuning(C.Structure):
     _fields_ = [("warps_per_block", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("wave_chunk", C.c_uint32),
-                ("max_vertices_per_lane", C.c_uint32)]
+                ("max_vertices_per_lane", C.c_uint32), ("epilogue_in_shared", C.c_uint32)]
 
 
 class CWave(C.Structure):
@@ -288,8 +288,9 @@ def wave_from_reference(amplitude_A, frequency_w, phase_constant_phi, steepness_
 
 
 def set_tuning(warps_per_block: int = 0, blocks_per_sm: int = 0, wave_chunk: int = 0,
-               max_vertices_per_lane: int = 0) -> None:
-    check(lib().wt_set_tuning(C.byref(CTuning(warps_per_block, blocks_per_sm, wave_chunk, max_vertices_per_lane))))
+               max_vertices_per_lane: int = 0, epilogue_in_shared: int = 1) -> None:
+    check(lib().wt_set_tuning(C.byref(CTuning(warps_per_block, blocks_per_sm, wave_chunk, max_vertices_per_lane,
+                                              epilogue_in_shared))))
 
 
 def get_tuning() -> dict:

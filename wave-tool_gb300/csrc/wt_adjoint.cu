@@ -116,12 +116,13 @@ __device__ __forceinline__ void vertex_adjoint(const VertexSums& s, float xl, fl
 // x(l, j) = xb + l*gx + 32 j*gx: per vertex only sum(g_theta) and
 // sum(j*g_theta) are kept, and folded into Tx, Tz once per l.
 template <int SC>  // SC > 0: compile-time S; 0: runtime S
-__device__ __forceinline__ void wave_moments(const float4* __restrict__ gbuf, uint32_t S_rt, uint32_t nvalid,
-                                             uint32_t t32, uint32_t a32, float cd, float sd, const PairCoef& k,
-                                             float xb, float zb, float gx, float gz, float m[11]) {
+__device__ __forceinline__ void wave_moments(const float4* __restrict__ gbuf, uint32_t S_rt, uint32_t l0,
+                                             uint32_t lstep, uint32_t nvalid, uint32_t t32, uint32_t a32, float cd,
+                                             float sd, const PairCoef& k, float xb, float zb, float gx, float gz,
+                                             float m[11]) {
     const uint32_t S = SC > 0 ? (uint32_t)SC : S_rt;
     const float tc = 2.0f * cd;
-    for (uint32_t l = 0; l < nvalid; ++l) {
+    for (uint32_t l = l0; l < nvalid; l += lstep) {
         const uint32_t tl = t32 + l * a32;
         float s, c, cp = 0.0f, sp = 0.0f;
         __sincosf((float)(int)tl * kTurnToRad, &s, &c);
@@ -255,9 +256,18 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
             const uint32_t nvalid0 = min(32u, cols - c0);  // valid lanes at j = 0
             const uint32_t rec0 = part_off[q] + lt * nwaves;
             for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
-                const uint32_t wi = w0 + lane;
-                const bool active = wi < nwaves;
-                const PairCoef k = coef[a.pair_offset + (active ? wi : 0)];
+                // a chunk of nwc <= 32 waves: lanes form 32 / P groups of P
+                // lanes (P = nwc rounded up to a power of two); group g walks
+                // the vertex lanes l = g, g + G, ... and the groups' moments
+                // are combined by a fixed shuffle tree
+                const uint32_t nwc = min(32u, nwaves - w0);
+                uint32_t P = 1;
+                while (P < nwc) P <<= 1;
+                const uint32_t G = 32u / P;
+                const uint32_t wl = lane & (P - 1), grp = lane / P;
+                const uint32_t wi = w0 + wl;
+                const bool active = wl < nwc;
+                const PairCoef k = coef[a.pair_offset + (active ? wi : w0)];
                 float4 st[3];
                 stage_wave(k, c0, row, st);
                 float m[11];
@@ -265,10 +275,14 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
                 for (int i = 0; i < 11; ++i) m[i] = 0.0f;
                 const uint32_t t32 = __float_as_uint(st[0].x), a32 = __float_as_uint(st[0].y);
                 if (S == 8)
-                    wave_moments<8>(gbuf, 8, nvalid0, t32, a32, st[0].z, st[0].w, k, xb0, zb0, gx, gz, m);
+                    wave_moments<8>(gbuf, 8, grp, G, nvalid0, t32, a32, st[0].z, st[0].w, k, xb0, zb0, gx, gz, m);
                 else
-                    wave_moments<0>(gbuf, S, nvalid0, t32, a32, st[0].z, st[0].w, k, xb0, zb0, gx, gz, m);
-                if (active) {
+                    wave_moments<0>(gbuf, S, grp, G, nvalid0, t32, a32, st[0].z, st[0].w, k, xb0, zb0, gx, gz, m);
+                for (uint32_t o = P; o < 32; o <<= 1) {
+#pragma unroll
+                    for (int i = 0; i < 11; ++i) m[i] += __shfl_down_sync(0xffffffffu, m[i], o);
+                }
+                if (active && grp == 0) {
                     float* r = partials + (size_t)kAdjRecord * (rec0 + wi);
 #pragma unroll
                     for (int i = 0; i < 11; ++i) r[i] = m[i];

@@ -9,6 +9,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 
@@ -35,9 +36,19 @@ wt_status cuda_fail(cudaError_t e, const char* what) {
 
 bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
 
-// Forward launch tuning, chosen by the autotuner or the defaults.
+// Forward launch tuning: a default (wt_set_tuning) and the autotuner's
+// winners cached per shape bucket (bit lengths of the patch and wave counts).
 std::mutex g_tune_mu;
-wt::FwdConfig g_fwd_cfg = {8, 32, 8, 0};
+wt::FwdConfig g_fwd_cfg = {8, 32, 16, 0, 1};
+std::map<uint32_t, wt::FwdConfig> g_tuned;
+
+uint32_t bit_length(uint32_t x) {
+    uint32_t b = 0;
+    while (x) { ++b; x >>= 1; }
+    return b;
+}
+
+uint32_t shape_bucket(uint32_t n_patches, uint32_t n_waves) { return (bit_length(n_patches) << 8) | bit_length(n_waves); }
 
 constexpr uint32_t kKnownFlags = WT_OUT_DISPLACEMENT | WT_LAYOUT_VEC3 | WT_PHASE_FP32_NAIVE;
 constexpr uint32_t kMaxPatches = 1u << 24;
@@ -109,6 +120,12 @@ wt::FwdConfig current_cfg() {
     return g_fwd_cfg;
 }
 
+wt::FwdConfig cfg_for(uint32_t n_patches, uint32_t n_waves) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tuned.find(shape_bucket(n_patches, n_waves));
+    return it != g_tuned.end() ? it->second : g_fwd_cfg;
+}
+
 wt_status run_displace(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
                        const wt_heightmap* hm, float* pos, float* nrm, uint64_t cap, uint32_t flags, void* ws,
                        size_t ws_bytes, cudaStream_t s, const wt::FwdConfig& cfg) {
@@ -132,7 +149,7 @@ wt_status run_displace(const wt_patch* patches, uint32_t n_patches, const wt_wav
 
 namespace wt {
 void set_last_error(const char* msg) { g_last_error = msg; }
-FwdConfig forward_config() { return current_cfg(); }
+FwdConfig forward_config(uint32_t n_patches, uint32_t n_waves) { return cfg_for(n_patches, n_waves); }
 }  // namespace wt
 
 extern "C" {
@@ -190,7 +207,7 @@ wt_status wt_gerstner_displace(const wt_patch* patches, uint32_t n_patches, cons
                                uint64_t out_capacity, uint32_t flags, void* workspace, size_t workspace_bytes,
                                wt_stream stream) {
     return run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags,
-                        workspace, workspace_bytes, (cudaStream_t)stream, current_cfg());
+                        workspace, workspace_bytes, (cudaStream_t)stream, cfg_for(n_patches, n_waves));
 }
 
 wt_status wt_gerstner_displace_unbatched(const wt_patch* host_patches, const wt_patch* patches,
@@ -199,7 +216,7 @@ wt_status wt_gerstner_displace_unbatched(const wt_patch* host_patches, const wt_
                                          uint64_t out_capacity, uint32_t flags, void* workspace,
                                          size_t workspace_bytes, wt_stream stream) {
     if (n_patches > 0 && !host_patches) return fail(WT_ERR_INVALID_ARG, "host_patches is NULL");
-    wt::FwdConfig cfg = current_cfg();
+    const wt::FwdConfig cfg = cfg_for(1, n_waves);
     for (uint32_t i = 0; i < n_patches; ++i) {
         wt_status st = run_displace(patches + i, 1, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags,
                                     workspace, workspace_bytes, (cudaStream_t)stream, cfg);
@@ -298,20 +315,23 @@ wt_status wt_wave_from_reference(float amplitude_A, float frequency_w, float pha
 }
 
 wt_status wt_set_tuning(const wt_tuning* t) {
-    wt::FwdConfig c = {8, 32, 8, 0};
+    wt::FwdConfig c = {8, 32, 16, 0, 1};
     if (t) {
         c.s = t->max_vertices_per_lane ? (int)t->max_vertices_per_lane : 8;
-        c.warps = t->warps_per_block ? (int)t->warps_per_block : 8;
+        c.warps = t->warps_per_block ? (int)t->warps_per_block : 16;
+        c.epi = (int)t->epilogue_in_shared;
         c.blocks_per_sm = (int)t->blocks_per_sm;
         c.chunk = t->wave_chunk ? (int)t->wave_chunk : 32;
         if (!wt::forward_config_supported(c))
-            return fail(WT_ERR_INVALID_ARG, "tuning: unsupported (warps_per_block, max_vertices_per_lane) = (%d, %d)",
-                        c.warps, c.s);
+            return fail(WT_ERR_INVALID_ARG,
+                        "tuning: unsupported (warps_per_block, max_vertices_per_lane, epilogue_in_shared) = (%d, %d, %d)",
+                        c.warps, c.s, c.epi);
         if (c.chunk != 8 && c.chunk != 16 && c.chunk != 32) return fail(WT_ERR_INVALID_ARG, "tuning: wave_chunk must be 8, 16 or 32");
         if (t->blocks_per_sm > 64) return fail(WT_ERR_INVALID_ARG, "tuning: blocks_per_sm > 64");
     }
     std::lock_guard<std::mutex> g(g_tune_mu);
     g_fwd_cfg = c;
+    g_tuned.clear();  // an explicit shape replaces the autotuned ones
     return WT_OK;
 }
 
@@ -322,6 +342,7 @@ wt_status wt_get_tuning(wt_tuning* t) {
     t->blocks_per_sm = (uint32_t)c.blocks_per_sm;
     t->wave_chunk = (uint32_t)c.chunk;
     t->max_vertices_per_lane = (uint32_t)c.s;
+    t->epilogue_in_shared = (uint32_t)c.epi;
     return WT_OK;
 }
 
@@ -336,7 +357,7 @@ wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches, cons
     if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
     e = cudaEventCreate(&e1);
     if (e != cudaSuccess) { cudaEventDestroy(e0); return cuda_fail(e, "cudaEventCreate"); }
-    const int shapes[][2] = {{8, 4}, {8, 6}, {8, 8}, {8, 16}, {4, 8}, {4, 16}};  // (vertices per lane, warps)
+    const int shapes[][3] = {{8, 8, 0}, {8, 16, 0}, {8, 8, 1}, {8, 16, 1}, {4, 8, 0}};  // (vertices/lane, warps, epi)
     const int chunks[] = {16, 32};
     float best_ms = 1e30f;
     wt::FwdConfig best_cfg = current_cfg();
@@ -344,7 +365,7 @@ wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches, cons
     for (int pass = 0; pass < 2 && st == WT_OK; ++pass)
     for (const auto& sh : shapes) {
         for (int ch : chunks) {
-            wt::FwdConfig c = {sh[0], ch, sh[1], 0};
+            wt::FwdConfig c = {sh[0], ch, sh[1], 0, sh[2]};
             st = run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags,
                               workspace, workspace_bytes, s, c);
             if (st != WT_OK) break;
@@ -367,9 +388,15 @@ wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches, cons
     if (st != WT_OK) return st;
     {
         std::lock_guard<std::mutex> g(g_tune_mu);
-        g_fwd_cfg = best_cfg;
+        g_tuned[shape_bucket(n_patches, n_waves)] = best_cfg;
     }
-    if (best) return wt_get_tuning(best);
+    if (best) {
+        best->warps_per_block = (uint32_t)best_cfg.warps;
+        best->blocks_per_sm = (uint32_t)best_cfg.blocks_per_sm;
+        best->wave_chunk = (uint32_t)best_cfg.chunk;
+        best->max_vertices_per_lane = (uint32_t)best_cfg.s;
+        best->epilogue_in_shared = (uint32_t)best_cfg.epi;
+    }
     return WT_OK;
 }
 

@@ -245,21 +245,28 @@ __global__ void __launch_bounds__(256) k_prep_coef(const wt_patch* __restrict__ 
 }
 
 // ---- stage 3: the persistent forward kernel --------------------------------
-template <int THREADS, int MINB, int SMAX>
+// EPI = 0: epilogue unrolled over the lane's vertices straight from the
+// accumulator registers; EPI = 1: the sums are parked in shared memory and a
+// single rolled copy of the epilogue runs (smaller code, larger smem carve-out).
+template <int THREADS, int MINB, int SMAX, int EPI>
 __global__ void __launch_bounds__(THREADS, MINB)
 k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ pos,
           float* __restrict__ nrm, uint32_t flags, char* __restrict__ ws, WsLayout L, uint32_t chunk) {
 #if __CUDA_ARCH__ >= 900
     cudaGridDependencySynchronize();
 #endif
-    __shared__ float4 stage[THREADS / 32][32 * kStage];
+    // per warp: wave staging (32 x kStage float4), then the parked sums of
+    // the tile's vertices ([j][half][lane] float4, conflict-free)
+    extern __shared__ float4 fwd_smem[];
+    float4* const wbase = fwd_smem + (threadIdx.x >> 5) * (32 * kStage + EPI * SMAX * 2 * 32);
     WsHeader* hdr = reinterpret_cast<WsHeader*>(ws);
     const uint32_t* sorted = reinterpret_cast<const uint32_t*>(ws + L.sorted);
     const uint32_t* tile_pre = reinterpret_cast<const uint32_t*>(ws + L.tile_pre);
     const PatchAux* aux = reinterpret_cast<const PatchAux*>(ws + L.aux);
     const PairCoef* coef = reinterpret_cast<const PairCoef*>(ws + L.coef);
     const int lane = threadIdx.x & 31;
-    float4* wst = stage[threadIdx.x >> 5];
+    float4* wst = wbase;
+    float4* ebuf = wbase + 32 * kStage;
     const uint32_t n = hdr->n_patches;
     const uint32_t total = hdr->total_tiles;
     const bool pow2 = hm.present && (hm.width & (hm.width - 1)) == 0 && (hm.height & (hm.height - 1)) == 0;
@@ -316,14 +323,38 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
         const float colf = (float)(c0 + lane);
         const float xb = fmaf(colf, gx, v * a.e2x), zb = fmaf(colf, gz, v * a.e2z);
         const uint64_t rowbase = out0 + (uint64_t)row * cols;
+        if (EPI == 1) {
+            // park the sums, then one rolled copy of the per-vertex epilogue
+            // (each lane reads back only its own slots)
 #pragma unroll
-        for (int j = 0; j < SMAX; ++j) {
-            const uint32_t col = c0 + lane + 32 * j;
-            if ((uint32_t)j < S && col < cols) {
-                const float xl = fmaf(32.0f * j, gx, xb);
-                const float zl = fmaf(32.0f * j, gz, zb);
-                VertexSums s{acc[j][0], acc[j][1], acc[j][2], acc[j][3], acc[j][4], acc[j][5], acc[j][6], acc[j][7]};
-                finish_vertex(s, xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags);
+            for (int j = 0; j < SMAX; ++j) {
+                if ((uint32_t)j < S) {
+                    ebuf[(2 * j) * 32 + lane] = make_float4(acc[j][0], acc[j][1], acc[j][2], acc[j][3]);
+                    ebuf[(2 * j + 1) * 32 + lane] = make_float4(acc[j][4], acc[j][5], acc[j][6], acc[j][7]);
+                }
+            }
+#pragma unroll 1
+            for (uint32_t j = 0; j < S; ++j) {
+                const uint32_t col = c0 + lane + 32 * j;
+                if (col < cols) {
+                    const float4 s0 = ebuf[(2 * j) * 32 + lane], s1 = ebuf[(2 * j + 1) * 32 + lane];
+                    const float xl = fmaf(32.0f * (float)j, gx, xb);
+                    const float zl = fmaf(32.0f * (float)j, gz, zb);
+                    VertexSums s{s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+                    finish_vertex(s, xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < SMAX; ++j) {
+                const uint32_t col = c0 + lane + 32 * j;
+                if ((uint32_t)j < S && col < cols) {
+                    const float xl = fmaf(32.0f * j, gx, xb);
+                    const float zl = fmaf(32.0f * j, gz, zb);
+                    VertexSums s{acc[j][0], acc[j][1], acc[j][2], acc[j][3],
+                                 acc[j][4], acc[j][5], acc[j][6], acc[j][7]};
+                    finish_vertex(s, xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags);
+                }
             }
         }
         t = __shfl_sync(0xffffffffu, t_next, 0);
@@ -376,7 +407,7 @@ __global__ void __launch_bounds__(256) k_forward_naive(const wt_patch* __restric
     }
 }
 
-template <int THREADS, int MINB, int SMAX>
+template <int THREADS, int MINB, int SMAX, int EPI>
 cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const HmDev& hm, float* pos,
                          float* nrm, uint32_t flags, void* ws, const WsLayout& L, cudaStream_t s) {
     constexpr int kMaxDev = 64;
@@ -384,10 +415,14 @@ cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const Hm
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+    constexpr size_t smem = sizeof(float4) * (THREADS / 32) * (32 * kStage + EPI * SMAX * 2 * 32);
     if (sms[dev] == 0) {
         int o = 0, m = 0;
+        cudaError_t e = cudaFuncSetAttribute(k_forward<THREADS, MINB, SMAX, EPI>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
         cudaDeviceGetAttribute(&m, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_forward<THREADS, MINB, SMAX>, THREADS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_forward<THREADS, MINB, SMAX, EPI>, THREADS, smem);
         occ[dev] = o < 1 ? 1 : o;
         sms[dev] = m;
     }
@@ -395,7 +430,7 @@ cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const Hm
     cudaLaunchConfig_t lc = {};
     lc.gridDim = dim3((unsigned)(sms[dev] * bps));
     lc.blockDim = dim3(THREADS);
-    lc.dynamicSmemBytes = 0;
+    lc.dynamicSmemBytes = smem;
     lc.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -403,7 +438,7 @@ cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const Hm
     lc.attrs = attr;
     lc.numAttrs = 1;
     const uint32_t chunk = cfg.chunk >= 1 && cfg.chunk <= 32 ? (uint32_t)cfg.chunk : 32u;
-    return cudaLaunchKernelEx(&lc, k_forward<THREADS, MINB, SMAX>, patches, hm, pos, nrm, flags,
+    return cudaLaunchKernelEx(&lc, k_forward<THREADS, MINB, SMAX, EPI>, patches, hm, pos, nrm, flags,
                               static_cast<char*>(ws), L, chunk);
 }
 
@@ -438,8 +473,9 @@ cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wa
 }
 
 bool forward_config_supported(const FwdConfig& c) {
-    if (c.s == 8) return c.warps == 8 || c.warps == 6 || c.warps == 4 || c.warps == 16;
-    if (c.s == 4) return c.warps == 8 || c.warps == 16;
+    if (c.epi != 0 && c.epi != 1) return false;
+    if (c.s == 8) return c.warps == 8 || c.warps == 16;
+    if (c.s == 4) return c.warps == 8 && c.epi == 0;
     return false;
 }
 
@@ -447,15 +483,16 @@ cudaError_t launch_forward(const FwdConfig& cfg, const wt_patch* patches, uint32
                            float* pos, float* nrm, uint32_t flags, void* ws, const WsLayout& L,
                            cudaStream_t s) {
     // warps per block; the minimum-blocks hint sets the register budget
-    if (cfg.s == 4) {
-        if (cfg.warps == 8) return launch_fwd_t<256, 3, 4>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 85 regs
-        if (cfg.warps == 16) return launch_fwd_t<512, 1, 4>(cfg, patches, hm, pos, nrm, flags, ws, L, s);  // 128 regs
-        return cudaErrorInvalidValue;
+    if (cfg.s == 4 && cfg.warps == 8 && cfg.epi == 0)
+        return launch_fwd_t<256, 3, 4, 0>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 85 regs
+    if (cfg.s == 8 && cfg.epi == 0) {
+        if (cfg.warps == 8) return launch_fwd_t<256, 2, 8, 0>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
+        if (cfg.warps == 16) return launch_fwd_t<512, 1, 8, 0>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
     }
-    if (cfg.warps == 8) return launch_fwd_t<256, 2, 8>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 128 regs
-    if (cfg.warps == 6) return launch_fwd_t<192, 2, 8>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 168 regs
-    if (cfg.warps == 4) return launch_fwd_t<128, 3, 8>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 168 regs
-    if (cfg.warps == 16) return launch_fwd_t<512, 1, 8>(cfg, patches, hm, pos, nrm, flags, ws, L, s);  // 128 regs
+    if (cfg.s == 8 && cfg.epi == 1) {
+        if (cfg.warps == 8) return launch_fwd_t<256, 2, 8, 1>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
+        if (cfg.warps == 16) return launch_fwd_t<512, 1, 8, 1>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
+    }
     return cudaErrorInvalidValue;
 }
 

@@ -107,6 +107,7 @@ struct FwdConfig {
     int chunk;          // waves staged per warp at a time (<= 32)
     int warps;          // warps per block
     int blocks_per_sm;  // persistent grid = SMs * blocks_per_sm (0 = occupancy max)
+    int epi;            // 0: epilogue from registers, 1: through shared memory
 };
 
 struct HmDev {
@@ -139,7 +140,7 @@ cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt
 
 // ---- host helpers (wt_api.cpp) ---------------------------------------------
 void set_last_error(const char* msg);  // message returned by wt_last_error() on this thread
-FwdConfig forward_config();            // the forward launch tuning in effect
+FwdConfig forward_config(uint32_t n_patches, uint32_t n_waves);  // tuning in effect for this shape
 
 // ---- misc kernels (wt_misc.cu) --------------------------------------------
 cudaError_t launch_indices(uint32_t cols, uint32_t rows, uint32_t base, uint32_t* out, cudaStream_t s);

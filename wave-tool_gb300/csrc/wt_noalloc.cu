@@ -97,7 +97,7 @@ extern "C" wt_status wt_gerstner_displace_noalloc(const wt_patch* patches, uint3
     const wt::WsLayout L = wt::ws_layout(n_patches, (kScratchBytes - L0.coef) / sizeof(wt::PairCoef) - 4);
     if (L.end > kScratchBytes || (L.end - L.coef) / sizeof(wt::PairCoef) < WT_NOALLOC_MAX_WAVE_SLOTS)
         return fail(WT_ERR_UNSUPPORTED, "no-alloc scratch smaller than its stated limits");
-    const wt::FwdConfig cfg = wt::forward_config();
+    const wt::FwdConfig cfg = wt::forward_config(n_patches, n_waves);
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = wt::launch_prep(patches, n_patches, waves, n_waves, h, out_capacity, 32u * cfg.s, ws, L, s);
     if (e != cudaSuccess) return cuda_fail(e, "prep launch");
