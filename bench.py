@@ -193,6 +193,58 @@ def _event_ms(fn, reps, stream, flush=None):
     return sum(a.elapsed_time(b) for a, b in evs) / reps
 
 
+def frame_pipeline(wt, workloads, stream, flush):
+    """One rendered frame of the water grid as the reference's render loop
+    does it (render-engine.cpp:797-1115 + water-grid.vert), on a 1024^2 grid
+    with the 32 waves and noise heightmap of the 1024^2 workload: camera ->
+    projected-grid corners (one-thread FP64 kernel) -> displacement + normals
+    -> clip / NDC-at-height-0 / view vector / facing normal / yaw-only normal,
+    replayed as one CUDA graph.  Also the vertex stage alone against HBM."""
+    import torch
+    w = workloads.config2()
+    amp = wt.displaceable_amplitude(w.waves, w.heightmap.disp_scale)
+    cam = wt.camera(position=(0.0, 4.0, 70.0), pitch_deg=-20.0, aspect=16 / 9, displaceable_amplitude=amp)
+    patch, view, st = wt.projected_grid(cam, w.patches)
+    surf = wt.Surface(patch, w.waves, wt.heightmap_from(w.heightmap))
+    cam_dev, view_dev = wt.to_device(cam), wt.to_device(view)
+    pos, nrm = surf.alloc_outputs(wt.WT_OUT_WORLD)
+    n = pos.shape[0]
+    outs = {k: torch.empty((n, 2 if k == "ndc0" else 4), device="cuda")
+            for k in ("clip", "ndc0", "view", "facing", "nrm_yaw")}
+
+    def frame(s=None):
+        wt.projected_grid_async(cam_dev, surf.patches, view_dev, stream=s)
+        surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD, stream=s)
+        wt.vertex_stage(view_dev, pos, nrm, out=outs, stream=s)
+
+    for _ in range(3):
+        frame()
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    side.wait_stream(stream)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side):
+        frame(side)
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    fms = _event_ms(g.replay, 20, stream, flush)
+    gms = _event_ms(lambda: wt.projected_grid_async(cam_dev, surf.patches, view_dev), 20, stream, flush)
+    dms = _event_ms(lambda: surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD), 20, stream, flush)
+    vms = _event_ms(lambda: wt.vertex_stage(view_dev, pos, nrm, out=outs), 20, stream, flush)
+    stage_bytes = n * (2 * 16 + 16 + 8 + 3 * 16)  # reads pos + nrm, writes clip, ndc0, view, facing, nrm_yaw
+    try:
+        hbm_peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+        peak_src = "MEASURED_PEAKS.json hbm_gbs (copy, measured)"
+    except (OSError, KeyError, ValueError):
+        hbm_peak, peak_src = 6800.0, "fallback 6.8 TB/s"
+    return {"vertices": n, "terms": n * len(w.waves), "frame_graph_ms": fms,
+            "frames_per_s": 1e3 / fms, "projected_grid_kernel_ms": gms, "displace_ms": dms,
+            "vertex_stage_ms": vms, "vertex_stage_bytes": stage_bytes,
+            "vertex_stage_gbs": stage_bytes / (vms * 1e-3) / 1e9,
+            "vertex_stage_hbm_frac": stage_bytes / (vms * 1e-3) / 1e9 / hbm_peak, "hbm_peak_source": peak_src}
+
+
 def side_measurements(wt, workloads, surf, pos, nrm, flags, flush, stream, ms_step):
     """Graph replay of the batched step, adjoint vs forward, the precision
     configuration's throughput and the Adam fit (each reported, not the
@@ -240,6 +292,7 @@ def side_measurements(wt, workloads, surf, pos, nrm, flags, flush, stream, ms_st
         prec[f"t={t:g}"] = {"ms_per_step": ms5, "value": w5.n_terms / (ms5 * 1e-3)}
         del s5, p5, n5
     out["precision_2048sq_128waves"] = prec
+    out["frame_1024sq_32waves_noise"] = frame_pipeline(wt, workloads, stream, flush)
     # the Adam fit: 500 steps of forward + adjoint on 512^2 x 16 waves
     target, start = workloads.config4()
     r = fit.fit_waves(target.patches, target.waves, start, steps=500, lr=1e-2)

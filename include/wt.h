@@ -252,6 +252,105 @@ wt_status wt_noise_synth(const wt_noise_term* terms, uint32_t n_terms,
                          uint32_t width, uint32_t height, float* texels_out,
                          void* workspace, size_t workspace_bytes, wt_stream stream);
 
+/* ---- frame set-up and the rest of the vertex stage ----------------------- */
+
+/* The reference's fly camera (src/camera.cpp:47-146, src/camera.h) as the
+ * projected grid needs it.  forward = (cos yaw cos pitch, sin pitch,
+ * sin yaw cos pitch), world up +y, right-handed look-at view, OpenGL
+ * perspective with depth in [-1, 1].  The reference's camera starts at
+ * yaw -90 (looking along -z), fov 72, near 0.1, far 100, position (0, 4, 70)
+ * (src/render-engine.cpp:52, src/render-engine.h:213-215).  80 bytes. */
+typedef struct wt_camera {
+    double position[3];
+    double yaw_deg;        /* taken mod 360 (Camera::setRotation) */
+    double pitch_deg;      /* clamped to [-89, 89] (Camera::rotate / setRotation) */
+    double fov_deg;        /* vertical field of view, in (0, 180) */
+    double aspect;         /* width / height, > 0 */
+    double z_near;         /* 0 < z_near < z_far */
+    double z_far;
+    /* half height of the displaceable slab |y| <= this: the sum of the wave
+     * amplitudes + the heightmap displacement scale + the bounce amplitude
+     * (DISPLACEABLE_AMPLITUDE, src/render-engine.cpp:803), >= 0 */
+    double displaceable_amplitude;
+} wt_camera;
+
+enum {
+    WT_VIEW_EMPTY = 0,          /* the frustum misses the slab: the reference draws no water */
+    WT_VIEW_VISIBLE = 1,
+    WT_VIEW_INVALID_CAMERA = 2  /* wt_projected_grid_async only: the device camera failed validation */
+};
+
+/* Per-frame uniforms of the vertex stage (water-grid.vert:24-33 and the values
+ * src/render-engine.cpp:277-286 derives from the camera).  Matrices are
+ * column-major (element (row r, column c) at [4*c + r], OpenGL order).
+ * 144 bytes. */
+typedef struct wt_view {
+    float view_projection[16]; /* clip = M * (x, y, z, 1) */
+    float view_only_yaw[16];   /* view matrix of the camera with its pitch set to 0 */
+    float camera_position[3];
+    uint32_t status;           /* WT_VIEW_* */
+} wt_view;
+
+/* The projected grid (src/render-engine.cpp:797-1042, after the projective
+ * grid of Johanson 2004): intersects the camera frustum (x and y widened by
+ * 1.2) with the slab |y| <= displaceable_amplitude, aims a projector placed
+ * at least displaceable_amplitude + 1 above the base plane at a point blended
+ * between the camera's bird's-eye and horizon aim points, bounds the
+ * intersection points in the projector's NDC, and casts the four corners of
+ * that range onto y = 0.  Host only, FP64 throughout (the reference computes
+ * in FP32 with GLM).
+ *   patch : host; bl, br, tl, tr are written (the rest is left as it is); left
+ *           untouched when the view is empty
+ *   view  : host or NULL; the camera's view-projection, yaw-only view matrix
+ *           and position, rounded to FP32, and the status
+ *   status: host or NULL; WT_VIEW_VISIBLE or WT_VIEW_EMPTY
+ * The reference's result is undefined where the projector looks straight
+ * down (it normalises a zero vector); here the projector pitch is then -89
+ * degrees, the clamp the reference applies to every pitch. */
+wt_status wt_projected_grid(const wt_camera* camera, wt_patch* patch, wt_view* view, uint32_t* status);
+
+/* The same computation as one single-thread kernel on `stream`, reading the
+ * camera from device memory and writing the corners of the device patch and
+ * the device wt_view, so a camera -> vertices frame (this, then
+ * wt_gerstner_displace, then wt_vertex_stage) can be captured and replayed as
+ * one CUDA graph.  An invalid camera gives status WT_VIEW_INVALID_CAMERA and
+ * leaves the patch untouched. */
+wt_status wt_projected_grid_async(const wt_camera* camera, wt_patch* patch, wt_view* view,
+                                  wt_stream stream);
+
+/* The vertex-stage outputs other than position and normal
+ * (water-grid.vert:150-158, 190-193), from the displaced world positions and
+ * normals wt_gerstner_displace wrote with WT_OUT_WORLD:
+ *   clip_out      float4  view_projection * (p, 1)              (gl_Position)
+ *   ndc0_out      float2  xy / w of view_projection * (p.x, 0, p.z, 1)
+ *                         (xyPositionNDCSpaceHeight0)
+ *   view_out      layout  camera_position - p                   (viewVecRaw)
+ *   facing_out    layout  the normal, negated where it faces away from the
+ *                         camera (dot(n, view) < 0); may be nrm itself
+ *   nrm_yaw_out   layout  normalize(view_only_yaw * (n_facing, 0))
+ *                         (normalVecInViewSpaceOnlyYaw)
+ * Every output may be NULL; nrm may be NULL when facing_out and nrm_yaw_out
+ * are.  `layout` (flags: WT_LAYOUT_FLOAT4 or WT_LAYOUT_VEC3) applies to pos,
+ * nrm, view_out, facing_out and nrm_yaw_out; float4 outputs get w = 0.
+ * view: device (e.g. written by wt_projected_grid_async). */
+wt_status wt_vertex_stage(const wt_view* view, const float* pos, const float* nrm, uint64_t n_vertices,
+                          uint32_t flags, float* clip_out, float* ndc0_out, float* view_out,
+                          float* facing_out, float* nrm_yaw_out, wt_stream stream);
+
+/* Heightmap texels from an 8-bit image already decoded into device memory,
+ * as the reference loads its heightmap (src/render-engine.cpp:1308-1322):
+ * stbi_load with vertical flip on load, forced to RGBA8, then sampled as a
+ * UNORM8 texture whose red channel is used (water-grid.vert:106).
+ *   texel (i, j) = pixels[src_row * row_stride_bytes + i * channels] / 255
+ * with src_row = height - 1 - j when flip_vertically (the reference's
+ * setting), else j: channel 0 is the red of RGB/RGBA pixels and the grey
+ * of grey / grey-alpha pixels, which stb's RGBA conversion copies to red.
+ * pixels: device, channels in [1, 4]; texels_out: device, width*height floats,
+ * ready for wt_heightmap.texels. */
+wt_status wt_heightmap_from_unorm8(const uint8_t* pixels, uint32_t width, uint32_t height, uint32_t channels,
+                                   uint64_t row_stride_bytes, uint32_t flip_vertically, float* texels_out,
+                                   wt_stream stream);
+
 /* ---- reference parameter conversion (host only) ------------------------- */
 
 /* Converts one reference GerstnerWave (render-engine.h:137-141) into a

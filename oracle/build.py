@@ -1,7 +1,7 @@
 """Build recipe of the CPU oracle (test infrastructure only).
 
 ``build_oracle()`` compiles the C restatement (gerstner_f64.c,
-reference_mode.c, indices_noise.c) into ``oracle/_build/liboracle.so``.
+reference_mode.c, indices_noise.c, projgrid.c) into ``oracle/_build/liboracle.so``.
 ``build_ref()`` compiles the reference's own vertex shader
 (``assets/shaders/water-grid.vert`` under the reference checkout) as C++ over
 ``glsl_shim.hpp`` into ``oracle/_ref/libwgvert_ref.so``; it needs the
@@ -19,7 +19,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-SOURCES = ["gerstner_f64.c", "reference_mode.c", "indices_noise.c"]
+SOURCES = ["gerstner_f64.c", "reference_mode.c", "indices_noise.c", "projgrid.c"]
 LIB = BUILD / "liboracle.so"
 REF_LIB = REF_OUT / "libwgvert_ref.so"
 CFLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-std=c11", "-Wall"]
@@ -38,7 +38,8 @@ def _stale(out: Path, deps) -> bool:
 
 def build_oracle(force: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
-    deps = [HERE / s for s in SOURCES] + [HERE / "wt_oracle.h", HERE.parent / "include" / "wt.h"]
+    deps = [HERE / s for s in SOURCES] + [HERE / "wt_oracle.h", HERE / "projgrid_body.inc",
+                                          HERE.parent / "include" / "wt.h"]
     if force or _stale(LIB, deps):
         cmd = ["gcc", *CFLAGS, "-shared", "-o", str(LIB), *[str(HERE / s) for s in SOURCES],
                "-lm", "-lpthread"]

@@ -71,6 +71,10 @@ def lib():
         _lib.wto_grid_indices.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, vp]
         _lib.wto_noise_f64.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, vp]
         _lib.wto_wave_to_reference.argtypes = [vp, C.POINTER(RefWave)]
+        for f in (_lib.wto_projected_grid_f32, _lib.wto_projected_grid_f64):
+            f.argtypes = [vp, vp, vp, vp, C.POINTER(C.c_uint32)]
+            f.restype = C.c_int
+        _lib.wto_vertex_stage_f64.argtypes = [vp, vp, vp, C.c_uint64, vp, vp, vp, vp, vp]
     return _lib
 
 
@@ -205,6 +209,44 @@ def reference_shader_vertex(U, id0, id1):
         raise ValueError("uniforms not expressible by the reference shader")
     del o["position"]
     return o
+
+
+def projected_grid(cam, fp64=True):
+    """src/render-engine.cpp:797-1042 for one wt_camera record: (status,
+    corners (4, 2) in the order BL, BR, TL, TR, view-projection (16,),
+    yaw-only view (16,), both column-major, number of slab points)."""
+    dt = np.float64 if fp64 else np.float32
+    corners = np.zeros((4, 2), dt); vp = np.zeros(16, dt); vy = np.zeros(16, dt)
+    n = C.c_uint32()
+    c = np.ascontiguousarray(cam.reshape(1))
+    f = lib().wto_projected_grid_f64 if fp64 else lib().wto_projected_grid_f32
+    st = f(_ptr(c), _ptr(corners), _ptr(vp), _ptr(vy), C.byref(n))
+    return st, corners, vp, vy, n.value
+
+
+def vertex_stage_f64(view, pos4, nrm4):
+    """water-grid.vert:150-158, 190-193 in FP64 on float4 positions/normals."""
+    n = len(pos4)
+    out = {"clip": np.zeros((n, 4)), "ndc0": np.zeros((n, 2)), "view": np.zeros((n, 3)),
+           "facing": np.zeros((n, 3)), "nrm_yaw": np.zeros((n, 3))}
+    v = np.ascontiguousarray(view.reshape(1))
+    p = np.ascontiguousarray(pos4, dtype=np.float32)
+    q = np.ascontiguousarray(nrm4, dtype=np.float32)
+    lib().wto_vertex_stage_f64(_ptr(v), _ptr(p), _ptr(q), n, *[_ptr(out[k]) for k in
+                                                                ("clip", "ndc0", "view", "facing", "nrm_yaw")])
+    return out
+
+
+def heightmap_from_unorm8(pixels, flip=True):
+    """(h, w, channels) uint8 pixels -> (h, w) float32 texels as the reference
+    uploads them: stbi_set_flip_vertically_on_load(true) + stbi_load forced to
+    RGBA (src/render-engine.cpp:1310-1311; grey is copied to red), a GL_RGBA8
+    texture (src/texture.cpp:66) whose red channel the shader samples
+    (water-grid.vert:106), UNORM8 -> float as c / 255."""
+    red = np.asarray(pixels, np.uint8)[..., 0]
+    if flip:
+        red = red[::-1]
+    return np.ascontiguousarray(red.astype(np.float32) / np.float32(255.0))
 
 
 def grid_indices(cols, rows, base=0):

@@ -143,6 +143,25 @@ void wto_grid_indices(uint32_t cols, uint32_t rows, uint32_t base_vertex, uint32
 void wto_noise_f64(const wt_noise_term* terms, uint32_t n_terms, uint32_t width,
                    uint32_t height, double* out);
 
+
+/* ---- per-frame set-up and the rest of the vertex stage (projgrid.c) ------ */
+
+/* src/render-engine.cpp:797-1042 for one camera: corners (x, z) in the order
+ * BL, BR, TL, TR; the camera's view-projection and yaw-only view matrices
+ * (column-major); the number of frustum points inside the slab.  Returns 1
+ * (visible), 0 (the frustum misses the slab) or -1 (a corner ray parallel to
+ * the base plane). */
+int wto_projected_grid_f32(const wt_camera* cam, float corners[4][2], float vp[16], float view_yaw[16],
+                           uint32_t* n_points);
+int wto_projected_grid_f64(const wt_camera* cam, double corners[4][2], double vp[16], double view_yaw[16],
+                           uint32_t* n_points);
+
+/* water-grid.vert:150-158, 190-193 in FP64 on float4 positions and normals;
+ * outputs may be NULL: clip (4), ndc0 (2), view (3), facing normal (3),
+ * yaw-only view-space normal (3) doubles per vertex. */
+void wto_vertex_stage_f64(const wt_view* v, const float* pos4, const float* nrm4, uint64_t n, double* clip4,
+                          double* ndc2, double* view3, double* facing3, double* nyaw3);
+
 #ifdef __cplusplus
 }
 #endif

@@ -40,7 +40,7 @@ def test_struct_layouts_match_c(wt, tmp_path):
     numpy dtypes the host layer uploads."""
     from wave_tool_gb300 import abi
     checks = {"wt_wave": abi.WAVE_DTYPE, "wt_patch": abi.PATCH_DTYPE, "wt_noise_term": abi.NOISE_TERM_DTYPE,
-              "wt_wave_grad": abi.WAVE_GRAD_DTYPE}
+              "wt_wave_grad": abi.WAVE_GRAD_DTYPE, "wt_camera": abi.CAMERA_DTYPE, "wt_view": abi.VIEW_DTYPE}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void) {"]
     for s, dt in checks.items():
         lines.append(f'printf("{s} sizeof %zu\\n", sizeof({s}));')

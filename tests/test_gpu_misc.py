@@ -107,3 +107,54 @@ def test_host_side_validation(wt, gpu):
         a[i] = v
         assert L.wt_gerstner_displace(*a) == code, (i, v)
         assert L.wt_last_error()
+
+
+@pytest.mark.parametrize("channels", [1, 2, 3, 4])
+def test_heightmap_from_unorm8_bit_exact(wt, oracle, gpu, channels):
+    """Pixels -> texels (flip on load, red/grey channel, c / 255) bit for bit,
+    with a padded row stride and without the flip."""
+    import ctypes as C
+    import torch
+    rng = np.random.default_rng(channels)
+    h, w = 37, 53
+    stride = w * channels + 5
+    buf = rng.integers(0, 256, (h, stride), dtype=np.uint8)
+    buf.reshape(-1)[:256] = np.arange(256, dtype=np.uint8)  # every code appears somewhere
+    px = buf[:, :w * channels].reshape(h, w, channels)
+    dev = torch.from_numpy(buf.reshape(-1).copy()).cuda()
+    for flip in (1, 0):
+        out = torch.empty((h, w), dtype=torch.float32, device="cuda")
+        wt.check(wt.lib().wt_heightmap_from_unorm8(dev.data_ptr(), w, h, channels, stride, flip, out.data_ptr(),
+                                                   wt.stream_handle()))
+        torch.cuda.synchronize()
+        want = oracle.heightmap_from_unorm8(px, bool(flip))
+        assert np.array_equal(out.cpu().numpy().view(np.uint32), want.view(np.uint32))
+    with pytest.raises(wt.WtError):
+        wt.check(wt.lib().wt_heightmap_from_unorm8(dev.data_ptr(), w, h, channels, w * channels - 1, 1,
+                                                   out.data_ptr(), wt.stream_handle()))
+
+
+def test_png_heightmap_end_to_end(wt, oracle, gpu, tmp_path):
+    """A grey PNG on disk -> device heightmap (wave_tool_gb300.png) equals
+    the oracle's texels, and displaces a grid like the same texels given
+    directly."""
+    import sys
+    from pathlib import Path
+    import torch
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    from test_png import encode
+    from wave_tool_gb300 import png, workloads
+    rng = np.random.default_rng(21)
+    img = rng.integers(0, 256, (64, 96, 1))
+    f = tmp_path / "hm.png"
+    f.write_bytes(encode(img, 8, 0, rng))
+    hm = png.load_heightmap(f, sample_scale=0.05, disp_scale=0.5, wrap=wt.WT_WRAP_MIRRORED_REPEAT)
+    torch.cuda.synchronize()
+    want = oracle.heightmap_from_unorm8(img.astype(np.uint8))
+    assert np.array_equal(hm.texels.cpu().numpy(), want)
+    w = workloads.config1()
+    a = wt.Surface(w.patches, w.waves, hm).displace()[0]
+    b = wt.Surface(w.patches, w.waves, wt.DeviceHeightmap(torch.from_numpy(want).cuda(), 0.05, 0.5,
+                                                          wt.WT_WRAP_MIRRORED_REPEAT)).displace()[0]
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)

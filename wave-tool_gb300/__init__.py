@@ -18,7 +18,8 @@ from pathlib import Path
 import numpy as np
 
 from . import abi
-from .abi import (NOISE_TERM_DTYPE, PATCH_DTYPE, WAVE_DTYPE, WAVE_GRAD_DTYPE, WT_LAYOUT_FLOAT4,
+from . import build as _build_recipe  # bound before build() below, which must not be shadowed by the submodule
+from .abi import (CAMERA_DTYPE, NOISE_TERM_DTYPE, PATCH_DTYPE, VIEW_DTYPE, WAVE_DTYPE, WAVE_GRAD_DTYPE, WT_LAYOUT_FLOAT4,
                   WT_LAYOUT_VEC3, WT_OUT_DISPLACEMENT, WT_OUT_WORLD, WT_PHASE_FP32_NAIVE, WT_PHASE_FP64,
                   WT_WRAP_MIRRORED_REPEAT, WT_WRAP_REPEAT)
 
@@ -32,6 +33,7 @@ EXPORTED = [
     "wt_gerstner_displace_unbatched",
     "wt_gerstner_adjoint", "wt_grid_indices", "wt_noise_synth", "wt_wave_from_reference",
     "wt_measure_peaks", "wt_set_tuning", "wt_get_tuning", "wt_autotune_displace",
+    "wt_projected_grid", "wt_projected_grid_async", "wt_vertex_stage", "wt_heightmap_from_unorm8",
 ]
 
 
@@ -60,8 +62,7 @@ _lib = None
 
 
 def build(force: bool = False) -> Path:
-    from .build import build as _b
-    return _b(force=force)
+    return _build_recipe.build(force=force)
 
 
 def lib():
@@ -93,6 +94,10 @@ def lib():
         L.wt_get_tuning.argtypes = [C.POINTER(CTuning)]
         L.wt_autotune_displace.argtypes = [vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, u64, u32, vp, sz, u32,
                                            C.POINTER(CTuning), vp]
+        L.wt_projected_grid.argtypes = [vp, vp, vp, C.POINTER(u32)]
+        L.wt_projected_grid_async.argtypes = [vp, vp, vp, vp]
+        L.wt_vertex_stage.argtypes = [vp, vp, vp, u64, u32, vp, vp, vp, vp, vp, vp]
+        L.wt_heightmap_from_unorm8.argtypes = [vp, u32, u32, u32, u64, u32, vp, vp]
         for name in EXPORTED:
             if name not in ("wt_version", "wt_last_error"):
                 getattr(L, name).restype = C.c_int
@@ -307,6 +312,63 @@ def measure_peaks(stream=None) -> tuple[float, float]:
     return f.value, s.value
 
 
+# ---- frame set-up and the rest of the vertex stage ---------------------------
+
+def camera(position=(0.0, 4.0, 70.0), yaw_deg=-90.0, pitch_deg=0.0, fov_deg=72.0, aspect=16.0 / 9.0,
+           z_near=0.1, z_far=100.0, displaceable_amplitude=0.0) -> np.ndarray:
+    """A wt_camera (defaults: the reference's start camera, render-engine.cpp:52)."""
+    c = np.zeros(1, CAMERA_DTYPE)
+    c["position"] = position
+    for k, v in (("yaw_deg", yaw_deg), ("pitch_deg", pitch_deg), ("fov_deg", fov_deg), ("aspect", aspect),
+                 ("z_near", z_near), ("z_far", z_far), ("displaceable_amplitude", displaceable_amplitude)):
+        c[k] = v
+    return c
+
+
+def displaceable_amplitude(waves: np.ndarray, heightmap_disp_scale: float = 0.0, bounce_amplitude: float = 0.0):
+    """DISPLACEABLE_AMPLITUDE of render-engine.cpp:803: total wave amplitude
+    + heightmap displacement scale + vertical bounce amplitude."""
+    return float(np.sum(np.abs(waves["amplitude"].astype(np.float64)))) + abs(heightmap_disp_scale) + \
+        abs(bounce_amplitude)
+
+
+def projected_grid(cam: np.ndarray, patch: np.ndarray | None = None):
+    """Host FP64 projected grid: (patch with corners set, wt_view, status).
+    `patch` (one PATCH_DTYPE record) keeps its other fields."""
+    assert cam.dtype == CAMERA_DTYPE
+    cam = np.ascontiguousarray(cam.reshape(1))
+    p = np.zeros(1, PATCH_DTYPE) if patch is None else np.ascontiguousarray(patch.reshape(1)).copy()
+    v = np.zeros(1, VIEW_DTYPE)
+    st = C.c_uint32()
+    check(lib().wt_projected_grid(cam.ctypes.data, p.ctypes.data, v.ctypes.data, C.byref(st)))
+    return p, v, st.value
+
+
+def projected_grid_async(cam_dev, patch_dev, view_dev, stream=None) -> None:
+    """Device projected grid: camera (device bytes of a wt_camera) -> corners
+    of the device patch and the device wt_view."""
+    check(lib().wt_projected_grid_async(cam_dev.data_ptr(), patch_dev.data_ptr(), view_dev.data_ptr(),
+                                        stream_handle(stream)))
+
+
+def vertex_stage(view_dev, pos, nrm=None, flags: int = 0, clip=True, ndc0=True, view=True, facing=True,
+                 nrm_yaw=True, out=None, stream=None) -> dict:
+    """water-grid.vert's remaining outputs for world positions/normals of
+    wt_gerstner_displace.  Returns the dict of (new or given) output tensors."""
+    torch = _torch()
+    n = pos.shape[0]
+    w = 3 if flags & WT_LAYOUT_VEC3 else 4
+    out = dict(out or {})
+    want = {"clip": (clip, 4), "ndc0": (ndc0, 2), "view": (view, w), "facing": (facing, w), "nrm_yaw": (nrm_yaw, w)}
+    for k, (on, width) in want.items():
+        if on and k not in out:
+            out[k] = torch.empty((n, width), dtype=torch.float32, device=pos.device)
+    check(lib().wt_vertex_stage(view_dev.data_ptr(), pos.data_ptr(), _ptr(nrm), n, flags, _ptr(out.get("clip")),
+                                _ptr(out.get("ndc0")), _ptr(out.get("view")), _ptr(out.get("facing")),
+                                _ptr(out.get("nrm_yaw")), stream_handle(stream)))
+    return out
+
+
 def heightmap_from(workload_hm, texels=None) -> DeviceHeightmap | None:
     """Device heightmap of a workloads.Heightmap: synthesised on the GPU
     unless texels are given."""
@@ -323,5 +385,6 @@ __all__ = [
     "adjoint_workspace_bytes", "workspace_status", "heightmap_from", "PATCH_DTYPE", "WAVE_DTYPE",
     "NOISE_TERM_DTYPE", "WAVE_GRAD_DTYPE", "WT_OUT_WORLD", "WT_OUT_DISPLACEMENT", "WT_LAYOUT_FLOAT4",
     "WT_LAYOUT_VEC3", "WT_PHASE_FP64", "WT_PHASE_FP32_NAIVE", "WT_WRAP_REPEAT", "WT_WRAP_MIRRORED_REPEAT",
-    "EXPORTED", "math",
+    "EXPORTED", "math", "CAMERA_DTYPE", "VIEW_DTYPE", "camera", "displaceable_amplitude", "projected_grid",
+    "projected_grid_async", "vertex_stage",
 ]

@@ -58,10 +58,36 @@ WAVE_GRAD_DTYPE = np.dtype(
     align=True,
 )
 
+CAMERA_DTYPE = np.dtype(
+    [
+        ("position", "<f8", (3,)),
+        ("yaw_deg", "<f8"),
+        ("pitch_deg", "<f8"),
+        ("fov_deg", "<f8"),
+        ("aspect", "<f8"),
+        ("z_near", "<f8"),
+        ("z_far", "<f8"),
+        ("displaceable_amplitude", "<f8"),
+    ],
+    align=True,
+)
+
+VIEW_DTYPE = np.dtype(
+    [
+        ("view_projection", "<f4", (16,)),
+        ("view_only_yaw", "<f4", (16,)),
+        ("camera_position", "<f4", (3,)),
+        ("status", "<u4"),
+    ],
+    align=True,
+)
+
 assert WAVE_DTYPE.itemsize == 32
 assert PATCH_DTYPE.itemsize == 72
 assert NOISE_TERM_DTYPE.itemsize == 16
 assert WAVE_GRAD_DTYPE.itemsize == 32
+assert CAMERA_DTYPE.itemsize == 80
+assert VIEW_DTYPE.itemsize == 144
 
 # status codes (wt_status)
 WT_OK = 0
@@ -88,6 +114,11 @@ WT_LAYOUT_FLOAT4 = 0
 WT_LAYOUT_VEC3 = 2
 WT_PHASE_FP64 = 0
 WT_PHASE_FP32_NAIVE = 4
+
+# wt_view.status
+WT_VIEW_EMPTY = 0
+WT_VIEW_VISIBLE = 1
+WT_VIEW_INVALID_CAMERA = 2
 
 
 def patch_vertices(patches: np.ndarray) -> np.ndarray:

@@ -42,7 +42,7 @@ def _stale(out: Path, deps) -> bool:
 
 def build(force: bool = False, verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
-    headers = list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h"))
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
     srcs = sources()
     objs = [BUILD / (s.name + ".o") for s in srcs]
 

@@ -285,6 +285,24 @@ wt_status wt_noise_synth(const wt_noise_term* terms, uint32_t n_terms, uint32_t 
     return WT_OK;
 }
 
+wt_status wt_heightmap_from_unorm8(const uint8_t* pixels, uint32_t width, uint32_t height, uint32_t channels,
+                                   uint64_t row_stride_bytes, uint32_t flip_vertically, float* texels_out,
+                                   wt_stream stream) {
+    if (width < 1 || height < 1 || width > 32768 || height > 32768)
+        return fail(WT_ERR_INVALID_ARG, "image size %ux%u outside [1, 32768]", width, height);
+    if (channels < 1 || channels > 4) return fail(WT_ERR_INVALID_ARG, "channels %u outside [1, 4]", channels);
+    if (row_stride_bytes < (uint64_t)width * channels)
+        return fail(WT_ERR_INVALID_ARG, "row stride %llu below width * channels",
+                    (unsigned long long)row_stride_bytes);
+    if (flip_vertically > 1) return fail(WT_ERR_INVALID_ARG, "flip_vertically must be 0 or 1");
+    if (!pixels) return fail(WT_ERR_INVALID_ARG, "pixels is NULL");
+    if (!texels_out || !aligned(texels_out, 4)) return fail(WT_ERR_INVALID_ARG, "texels_out NULL or misaligned");
+    cudaError_t e = wt::launch_unorm8(pixels, width, height, channels, row_stride_bytes, flip_vertically, texels_out,
+                                      (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "heightmap ingestion launch");
+    return WT_OK;
+}
+
 wt_status wt_wave_from_reference(float amplitude_A, float frequency_w, float phase_constant_phi, float steepness_Q,
                                  float dir_x, float dir_z, uint32_t wave_count, wt_wave* out) {
     if (!out) return fail(WT_ERR_INVALID_ARG, "out is NULL");

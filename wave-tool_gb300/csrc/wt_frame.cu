@@ -1,0 +1,419 @@
+// wt_frame.cu — per-frame set-up of the projected grid, and the vertex-stage
+// outputs that follow the displacement.
+//
+// projected_grid() restates src/render-engine.cpp:797-1042 in FP64.  It is
+// one __host__ __device__ function: wt_projected_grid runs it on the host,
+// wt_projected_grid_async in a single-thread kernel that reads the camera
+// from device memory, so that camera -> corners -> displaced vertices is one
+// stream of kernels a CUDA graph can replay with a new camera every frame.
+//
+// k_vertex_stage computes the rest of water-grid.vert's outputs
+// (:150-158, :190-193) from the displaced positions and exact normals: a
+// streaming, HBM-bound kernel (reads 2 x 16 B, writes up to 72 B per vertex).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "wt_internal.h"
+
+namespace {
+
+#define WT_HD __host__ __device__ inline
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kDeg = kPi / 180.0;
+
+// Constants of the reference's projected grid (src/render-engine.cpp).
+constexpr double kFrustumPad = 1.2;          // SAFETY_PADDING_SCALAR, :826
+constexpr double kProjectorElevation = 1.0;  // PROJECTOR_ELEVATION_FROM_CAMERA, :915
+constexpr double kHorizonEpsilon = 0.001;    // SAFE_EPSILON, :925
+constexpr double kPitchLimit = 89.0;         // Camera::setRotation clamp, src/camera.cpp:100
+
+struct D3 {
+    double x, y, z;
+};
+WT_HD D3 operator+(D3 a, D3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+WT_HD D3 operator-(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+WT_HD D3 operator*(double s, D3 a) { return {s * a.x, s * a.y, s * a.z}; }
+WT_HD double dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+WT_HD D3 cross(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+WT_HD D3 unit(D3 a) { return (1.0 / sqrt(dot(a, a))) * a; }
+
+// 4x4 matrix in OpenGL (column-major) order: m[c][r] is row r of column c.
+struct M4 {
+    double m[4][4];
+};
+
+WT_HD M4 identity() {
+    M4 r;
+    for (int c = 0; c < 4; ++c)
+        for (int k = 0; k < 4; ++k) r.m[c][k] = (c == k) ? 1.0 : 0.0;
+    return r;
+}
+
+WT_HD M4 mul(const M4& a, const M4& b) {
+    M4 r;
+    for (int c = 0; c < 4; ++c)
+        for (int k = 0; k < 4; ++k) {
+            double s = 0.0;
+            for (int j = 0; j < 4; ++j) s += a.m[j][k] * b.m[c][j];
+            r.m[c][k] = s;
+        }
+    return r;
+}
+
+// The camera's basis (Camera::updateBasisVectors, src/camera.cpp:130-137)
+// for a yaw given by its cosine and sine: pitch clamped, world up +y.  The
+// right vector normalize(cross(forward, +y)) is (-sin yaw, 0, cos yaw) for
+// every pitch.
+struct Basis {
+    D3 pos, fwd, right, up;
+};
+
+WT_HD Basis camera_basis(D3 pos, double cy, double sy, double pitch_deg) {
+    double sp, cp;
+    sincos(fmin(fmax(pitch_deg, -kPitchLimit), kPitchLimit) * kDeg, &sp, &cp);
+    Basis b;
+    b.pos = pos;
+    b.fwd = unit(D3{cy * cp, sp, sy * cp});
+    b.right = D3{-sy, 0.0, cy};
+    b.up = unit(cross(b.right, b.fwd));
+    return b;
+}
+
+// Right-handed look-at along the basis' forward vector (glm::lookAt, whose
+// side vector normalize(cross(forward, up)) is the basis' right vector).
+WT_HD M4 view_matrix(const Basis& b) {
+    const D3 s = b.right, u = b.up;
+    M4 v = identity();
+    v.m[0][0] = s.x; v.m[1][0] = s.y; v.m[2][0] = s.z; v.m[3][0] = -dot(s, b.pos);
+    v.m[0][1] = u.x; v.m[1][1] = u.y; v.m[2][1] = u.z; v.m[3][1] = -dot(u, b.pos);
+    v.m[0][2] = -b.fwd.x; v.m[1][2] = -b.fwd.y; v.m[2][2] = -b.fwd.z; v.m[3][2] = dot(b.fwd, b.pos);
+    return v;
+}
+
+// OpenGL perspective, depth mapped to [-1, 1] (glm::perspective).
+WT_HD M4 perspective(double tan_half_fov, double aspect, double zn, double zf) {
+    const double f = 1.0 / tan_half_fov;
+    M4 p;
+    for (int c = 0; c < 4; ++c)
+        for (int k = 0; k < 4; ++k) p.m[c][k] = 0.0;
+    p.m[0][0] = f / aspect;
+    p.m[1][1] = f;
+    p.m[2][2] = -(zf + zn) / (zf - zn);
+    p.m[2][3] = -1.0;
+    p.m[3][2] = -2.0 * zf * zn / (zf - zn);
+    return p;
+}
+
+WT_HD bool camera_ok(const wt_camera& c) {
+    const double v[10] = {c.position[0], c.position[1], c.position[2], c.yaw_deg, c.pitch_deg,
+                          c.fov_deg, c.aspect, c.z_near, c.z_far, c.displaceable_amplitude};
+    for (double x : v)
+        if (!isfinite(x)) return false;
+    return c.fov_deg > 0.0 && c.fov_deg < 180.0 && c.aspect > 0.0 && c.z_near > 0.0 && c.z_far > c.z_near &&
+           c.displaceable_amplitude >= 0.0;
+}
+
+struct Grid {
+    double corner[4][2];  // world (x, z) of BL, BR, TL, TR
+    M4 view_projection, view_only_yaw;
+    bool visible;
+};
+
+// src/render-engine.cpp:797-1042.  The view-projection inverses the
+// reference forms with glm::inverse are used in closed form: NDC (X, Y) at
+// view depth d is pos + d * (X*tx*right + Y*ty*up + fwd), tx = tan(fov/2) *
+// aspect, ty = tan(fov/2).  The slab points only enter through their x and z
+// (they are flattened onto y = 0 before projection, :989-991) and only
+// through the bounds of their projector NDC, so they are bounded as they are
+// found; the projector does not depend on them.
+WT_HD void projected_grid(const wt_camera& c, Grid* g) {
+    const double amp = c.displaceable_amplitude;
+    const D3 eye{c.position[0], c.position[1], c.position[2]};
+    const double yaw = (c.yaw_deg - 360.0 * floor(c.yaw_deg / 360.0)) * kDeg;
+    double sy, cy;
+    sincos(yaw, &sy, &cy);
+    const Basis cam = camera_basis(eye, cy, sy, c.pitch_deg);
+    const double ty = tan(0.5 * c.fov_deg * kDeg), tx = ty * c.aspect;
+    const M4 proj = perspective(ty, c.aspect, c.z_near, c.z_far);
+    g->view_projection = mul(proj, view_matrix(cam));
+    g->view_only_yaw = view_matrix(Basis{eye, D3{cy, 0.0, sy}, D3{-sy, 0.0, cy}, D3{0.0, 1.0, 0.0}});
+    g->visible = false;
+
+    // the projector: the camera raised out of the slab and pitched down at
+    // an aim point blended between the bird's-eye and horizon aims (:897-984)
+    const bool underwater = eye.y < 0.0;
+    const double min_height = amp + kProjectorElevation;
+    D3 ppos = eye;
+    if (eye.y < min_height) ppos.y = underwater ? min_height - eye.y : min_height;
+    D3 fs = cam.fwd;
+    if (fabs(fs.y) < kHorizonEpsilon) fs.y = (fs.y >= 0.0) ? kHorizonEpsilon : -kHorizonEpsilon;
+    const bool looking_down = fs.y < 0.0;
+    const D3 ray = (looking_down != underwater) ? fs : D3{fs.x, -fs.y, fs.z};
+    const D3 aim1 = eye + (-eye.y / ray.y) * ray;
+    D3 aim2 = eye + cam.fwd;
+    aim2.y = 0.0;
+    const double a = fabs(fs.y);
+    const D3 aim = (1.0 - a) * aim2 + a * aim1;
+    const D3 d = unit(aim - ppos);
+    // angle below the horizon of the unit aim direction; the reference's
+    // acos(d . normalize(d.x, 0, d.z)) is the same angle
+    const double pitch = -atan2(fabs(d.y), sqrt(d.x * d.x + d.z * d.z)) / kDeg;
+    const Basis pj = camera_basis(ppos, cy, sy, pitch);
+
+    // frustum corners, NDC x and y widened (:815-838); bit 2 = right,
+    // bit 1 = top, bit 0 = far
+    D3 fc[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const double depth = (i & 1) ? c.z_far : c.z_near;
+        const double X = ((i & 4) ? kFrustumPad : -kFrustumPad) * tx * depth;
+        const double Y = ((i & 2) ? kFrustumPad : -kFrustumPad) * ty * depth;
+        fc[i] = eye + X * cam.right + Y * cam.up + depth * cam.fwd;
+    }
+
+    // points of the frustum inside the slab |y| <= amp (the 12 edges cut by
+    // the planes y = +-amp, then the corners, :857-893), flattened and
+    // bounded in the projector's NDC (:993-1005)
+    double x0 = 0.0, x1 = 0.0, y0 = 0.0, y1 = 0.0;
+    bool any = false;
+    auto add = [&](double px, double pz) {
+        const D3 q = D3{px, 0.0, pz} - ppos;
+        const double w = dot(pj.fwd, q);
+        const double X = dot(pj.right, q) / (tx * w), Y = dot(pj.up, q) / (ty * w);
+        x0 = any ? fmin(x0, X) : X;
+        x1 = any ? fmax(x1, X) : X;
+        y0 = any ? fmin(y0, Y) : Y;
+        y1 = any ? fmax(y1, Y) : Y;
+        any = true;
+    };
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int bit = 1; bit < 8; bit <<= 1) {
+            if (i & bit) continue;
+            const D3 e0 = fc[i], e1 = fc[i | bit];
+            if (e0.y == e1.y) continue;  // parallel to the planes: no single crossing
+            const double lo = fmin(e0.y, e1.y), hi = fmax(e0.y, e1.y);
+#pragma unroll
+            for (int sgn = 0; sgn < 2; ++sgn) {
+                const double h = sgn ? -amp : amp;
+                if (lo <= h && h <= hi) {
+                    const double t = (h - e0.y) / (e1.y - e0.y);
+                    add(e0.x + t * (e1.x - e0.x), e0.z + t * (e1.z - e0.z));
+                }
+            }
+        }
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+        if (-amp <= fc[i].y && fc[i].y <= amp) add(fc[i].x, fc[i].z);
+    if (!any) return;
+
+    // cast the rays through the corners of that NDC range onto y = 0
+    // (:1007-1036): ray (X, Y) from the projector along X*tx*right + Y*ty*up + fwd
+    const double uv[4][2] = {{0.0, 0.0}, {1.0, 0.0}, {0.0, 1.0}, {1.0, 1.0}};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const double X = x0 + uv[k][0] * (x1 - x0), Y = y0 + uv[k][1] * (y1 - y0);
+        const D3 dir = (X * tx) * pj.right + (Y * ty) * pj.up + pj.fwd;
+        if (dir.y == 0.0) return;
+        const double t = -ppos.y / dir.y;
+        g->corner[k][0] = ppos.x + t * dir.x;
+        g->corner[k][1] = ppos.z + t * dir.z;
+        if (!isfinite(g->corner[k][0]) || !isfinite(g->corner[k][1])) return;
+    }
+    g->visible = true;
+}
+
+WT_HD void store_result(const wt_camera& c, const Grid& g, wt_patch* patch, wt_view* view) {
+    if (view) {
+        for (int col = 0; col < 4; ++col)
+            for (int r = 0; r < 4; ++r) {
+                view->view_projection[4 * col + r] = (float)g.view_projection.m[col][r];
+                view->view_only_yaw[4 * col + r] = (float)g.view_only_yaw.m[col][r];
+            }
+        for (int k = 0; k < 3; ++k) view->camera_position[k] = (float)c.position[k];
+        view->status = g.visible ? WT_VIEW_VISIBLE : WT_VIEW_EMPTY;
+    }
+    if (patch && g.visible) {
+        float* dst[4] = {patch->bl, patch->br, patch->tl, patch->tr};
+        for (int k = 0; k < 4; ++k) {
+            dst[k][0] = (float)g.corner[k][0];
+            dst[k][1] = (float)g.corner[k][1];
+        }
+    }
+}
+
+__global__ void k_projected_grid(const wt_camera* __restrict__ camera, wt_patch* patch, wt_view* view) {
+    const wt_camera c = *camera;
+    if (!camera_ok(c)) {
+        view->status = WT_VIEW_INVALID_CAMERA;
+        return;
+    }
+    Grid g;
+    projected_grid(c, &g);
+    store_result(c, g, patch, view);
+}
+
+// ---- vertex-stage outputs ---------------------------------------------------
+
+constexpr int kStageThreads = 256;
+
+struct StageOut {
+    float* clip;    // float4
+    float* ndc0;    // float2
+    float* view;    // layout
+    float* facing;  // layout
+    float* nyaw;    // layout
+};
+
+template <bool VEC3>
+__device__ __forceinline__ float3 load3(const float* p, uint64_t i) {
+    if (VEC3) return make_float3(p[3 * i], p[3 * i + 1], p[3 * i + 2]);
+    const float4 v = reinterpret_cast<const float4*>(p)[i];
+    return make_float3(v.x, v.y, v.z);
+}
+
+template <bool VEC3>
+__device__ __forceinline__ void store3(float* p, uint64_t i, float3 v) {
+    if (VEC3) {
+        p[3 * i] = v.x;
+        p[3 * i + 1] = v.y;
+        p[3 * i + 2] = v.z;
+    } else {
+        reinterpret_cast<float4*>(p)[i] = make_float4(v.x, v.y, v.z, 0.0f);
+    }
+}
+
+// One vertex per thread per iteration of a grid-stride loop.  The 36 floats
+// of wt_view are staged once per block in shared memory.
+template <bool VEC3>
+__global__ void __launch_bounds__(kStageThreads) k_vertex_stage(const wt_view* __restrict__ view, const float* pos,
+                                                                 const float* nrm, uint64_t n, StageOut o) {
+    __shared__ float u[36];
+    if (threadIdx.x < 36) u[threadIdx.x] = reinterpret_cast<const float*>(view)[threadIdx.x];
+    __syncthreads();
+    const float* M = u;       // view_projection, column-major
+    const float* Y = u + 16;  // view_only_yaw
+    const float cx = u[32], cy = u[33], cz = u[34];
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float3 p = load3<VEC3>(pos, i);
+        if (o.clip) {
+            float4 c;
+            c.x = fmaf(M[0], p.x, fmaf(M[4], p.y, fmaf(M[8], p.z, M[12])));
+            c.y = fmaf(M[1], p.x, fmaf(M[5], p.y, fmaf(M[9], p.z, M[13])));
+            c.z = fmaf(M[2], p.x, fmaf(M[6], p.y, fmaf(M[10], p.z, M[14])));
+            c.w = fmaf(M[3], p.x, fmaf(M[7], p.y, fmaf(M[11], p.z, M[15])));
+            reinterpret_cast<float4*>(o.clip)[i] = c;
+        }
+        if (o.ndc0) {
+            const float x = fmaf(M[0], p.x, fmaf(M[8], p.z, M[12]));
+            const float y = fmaf(M[1], p.x, fmaf(M[9], p.z, M[13]));
+            const float w = fmaf(M[3], p.x, fmaf(M[11], p.z, M[15]));
+            reinterpret_cast<float2*>(o.ndc0)[i] = make_float2(x / w, y / w);
+        }
+        const float3 v = make_float3(cx - p.x, cy - p.y, cz - p.z);
+        if (o.view) store3<VEC3>(o.view, i, v);
+        if (o.facing || o.nyaw) {
+            float3 nv = load3<VEC3>(nrm, i);
+            // the sign of dot(n, normalize(v)) is the sign of dot(n, v)
+            if (fmaf(nv.x, v.x, fmaf(nv.y, v.y, nv.z * v.z)) < 0.0f) nv = make_float3(-nv.x, -nv.y, -nv.z);
+            if (o.facing) store3<VEC3>(o.facing, i, nv);
+            if (o.nyaw) {
+                float3 q;
+                q.x = fmaf(Y[0], nv.x, fmaf(Y[4], nv.y, Y[8] * nv.z));
+                q.y = fmaf(Y[1], nv.x, fmaf(Y[5], nv.y, Y[9] * nv.z));
+                q.z = fmaf(Y[2], nv.x, fmaf(Y[6], nv.y, Y[10] * nv.z));
+                const float s = 1.0f / sqrtf(fmaf(q.x, q.x, fmaf(q.y, q.y, q.z * q.z)));
+                store3<VEC3>(o.nyaw, i, make_float3(q.x * s, q.y * s, q.z * s));
+            }
+        }
+    }
+}
+
+wt_status fail(wt_status s, const char* msg) {
+    wt::set_last_error(msg);
+    return s;
+}
+
+wt_status cuda_fail(cudaError_t e, const char* what) {
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+    wt::set_last_error(buf);
+    return WT_ERR_CUDA;
+}
+
+bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+
+int g_stage_blocks[64] = {};
+
+}  // namespace
+
+extern "C" wt_status wt_projected_grid(const wt_camera* camera, wt_patch* patch, wt_view* view, uint32_t* status) {
+    if (!camera) return fail(WT_ERR_INVALID_ARG, "wt_projected_grid: camera is NULL");
+    if (!camera_ok(*camera))
+        return fail(WT_ERR_INVALID_ARG,
+                    "wt_projected_grid: camera needs finite values, 0 < fov < 180, aspect > 0, "
+                    "0 < z_near < z_far, displaceable_amplitude >= 0");
+    Grid g;
+    projected_grid(*camera, &g);
+    store_result(*camera, g, patch, view);
+    if (status) *status = g.visible ? WT_VIEW_VISIBLE : WT_VIEW_EMPTY;
+    return WT_OK;
+}
+
+extern "C" wt_status wt_projected_grid_async(const wt_camera* camera, wt_patch* patch, wt_view* view,
+                                             wt_stream stream) {
+    if (!camera || !aligned(camera, 8)) return fail(WT_ERR_INVALID_ARG, "wt_projected_grid_async: camera NULL or misaligned");
+    if (!patch || !aligned(patch, 8)) return fail(WT_ERR_INVALID_ARG, "wt_projected_grid_async: patch NULL or misaligned");
+    if (!view || !aligned(view, 4)) return fail(WT_ERR_INVALID_ARG, "wt_projected_grid_async: view NULL or misaligned");
+    k_projected_grid<<<1, 1, 0, (cudaStream_t)stream>>>(camera, patch, view);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? WT_OK : cuda_fail(e, "wt_projected_grid_async launch");
+}
+
+extern "C" wt_status wt_vertex_stage(const wt_view* view, const float* pos, const float* nrm, uint64_t n_vertices,
+                                     uint32_t flags, float* clip_out, float* ndc0_out, float* view_out,
+                                     float* facing_out, float* nrm_yaw_out, wt_stream stream) {
+    if (flags & ~(uint32_t)WT_LAYOUT_VEC3) return fail(WT_ERR_INVALID_ARG, "wt_vertex_stage: flags other than WT_LAYOUT_VEC3");
+    const bool vec3 = (flags & WT_LAYOUT_VEC3) != 0;
+    const size_t la = vec3 ? 4 : 16;
+    if (!view || !aligned(view, 4)) return fail(WT_ERR_INVALID_ARG, "wt_vertex_stage: view NULL or misaligned");
+    if (!pos || !aligned(pos, la)) return fail(WT_ERR_INVALID_ARG, "wt_vertex_stage: pos NULL or misaligned");
+    const bool need_nrm = facing_out || nrm_yaw_out;
+    if (need_nrm && (!nrm || !aligned(nrm, la)))
+        return fail(WT_ERR_INVALID_ARG, "wt_vertex_stage: nrm NULL or misaligned while normal outputs are asked for");
+    if (clip_out && !aligned(clip_out, 16)) return fail(WT_ERR_INVALID_ARG, "wt_vertex_stage: clip_out not 16-byte aligned");
+    if (ndc0_out && !aligned(ndc0_out, 8)) return fail(WT_ERR_INVALID_ARG, "wt_vertex_stage: ndc0_out not 8-byte aligned");
+    float* lay[3] = {view_out, facing_out, nrm_yaw_out};
+    for (float* p : lay)
+        if (p && !aligned(p, la)) return fail(WT_ERR_INVALID_ARG, "wt_vertex_stage: output misaligned for its layout");
+    if (n_vertices == 0) return WT_OK;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= 64) return fail(WT_ERR_UNSUPPORTED, "device ordinal beyond 63");
+    if (!g_stage_blocks[dev]) {
+        int sms = 0, occ = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+        e = vec3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_vertex_stage<true>, kStageThreads, 0)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_vertex_stage<false>, kStageThreads, 0);
+        if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
+        g_stage_blocks[dev] = sms * (occ > 0 ? occ : 1);
+    }
+    const uint64_t need = (n_vertices + kStageThreads - 1) / kStageThreads;
+    const unsigned blocks = (unsigned)(need < (uint64_t)g_stage_blocks[dev] ? need : (uint64_t)g_stage_blocks[dev]);
+    const StageOut o{clip_out, ndc0_out, view_out, facing_out, nrm_yaw_out};
+    cudaStream_t s = (cudaStream_t)stream;
+    if (vec3)
+        k_vertex_stage<true><<<blocks, kStageThreads, 0, s>>>(view, pos, nrm, n_vertices, o);
+    else
+        k_vertex_stage<false><<<blocks, kStageThreads, 0, s>>>(view, pos, nrm, n_vertices, o);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? WT_OK : cuda_fail(e, "wt_vertex_stage launch");
+}

@@ -144,6 +144,8 @@ FwdConfig forward_config(uint32_t n_patches, uint32_t n_waves);  // tuning in ef
 
 // ---- misc kernels (wt_misc.cu) --------------------------------------------
 cudaError_t launch_indices(uint32_t cols, uint32_t rows, uint32_t base, uint32_t* out, cudaStream_t s);
+cudaError_t launch_unorm8(const uint8_t* px, uint32_t w, uint32_t h, uint32_t channels, uint64_t stride,
+                          uint32_t flip, float* out, cudaStream_t s);
 cudaError_t launch_noise(const wt_noise_term* terms, uint32_t n_terms, uint32_t w, uint32_t h,
                          float* out, void* ws, cudaStream_t s);
 cudaError_t measure_peaks(void* scratch, size_t bytes, double* fma, double* sin, cudaStream_t s);

@@ -29,6 +29,22 @@ __global__ void __launch_bounds__(256) k_indices(uint32_t cols, uint32_t rows, u
     }
 }
 
+// ---- 8-bit heightmap ingestion -------------------------------------------
+// texel (i, j) = R of pixel (i, row j counted from the bottom when flipped)
+// as UNORM8 -> float: c / 255, correctly rounded (GL's conversion of an
+// RGBA8 texel's red channel, sampled by water-grid.vert:106).
+__global__ void __launch_bounds__(256) k_unorm8(const uint8_t* __restrict__ px, uint32_t w, uint32_t h,
+                                                uint32_t channels, uint64_t stride, uint32_t flip,
+                                                float* __restrict__ out) {
+    const uint64_t n = (uint64_t)w * h;
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t j = (uint32_t)(k / w);
+        const uint32_t i = (uint32_t)(k - (uint64_t)j * w);
+        const uint32_t src = flip ? h - 1 - j : j;
+        out[k] = (float)px[(uint64_t)src * stride + (uint64_t)i * channels] / 255.0f;
+    }
+}
+
 // ---- noise heightmap -------------------------------------------------------
 __device__ __forceinline__ uint32_t ordered(float f) {
     uint32_t b = __float_as_uint(f);
@@ -143,6 +159,15 @@ cudaError_t launch_indices(uint32_t cols, uint32_t rows, uint32_t base, uint32_t
     uint64_t want = (total + 255) / 256;
     unsigned blocks = (unsigned)(want < (uint64_t)device_sms() * 16 ? want : (uint64_t)device_sms() * 16);
     k_indices<<<blocks, 256, 0, s>>>(cols, rows, base, out, total);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unorm8(const uint8_t* px, uint32_t w, uint32_t h, uint32_t channels, uint64_t stride,
+                          uint32_t flip, float* out, cudaStream_t s) {
+    const uint64_t n = (uint64_t)w * h;
+    const uint64_t want = (n + 255) / 256;
+    const unsigned blocks = (unsigned)(want < (uint64_t)device_sms() * 16 ? want : (uint64_t)device_sms() * 16);
+    k_unorm8<<<blocks, 256, 0, s>>>(px, w, h, channels, stride, flip, out);
     return cudaGetLastError();
 }
 
