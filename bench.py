@@ -195,11 +195,12 @@ def _event_ms(fn, reps, stream, flush=None):
 
 def frame_pipeline(wt, workloads, stream, flush):
     """One rendered frame of the water grid as the reference's render loop
-    does it (render-engine.cpp:797-1115 + water-grid.vert), on a 1024^2 grid
-    with the 32 waves and noise heightmap of the 1024^2 workload: camera ->
-    projected-grid corners (one-thread FP64 kernel) -> displacement + normals
-    -> clip / NDC-at-height-0 / view vector / facing normal / yaw-only normal,
-    replayed as one CUDA graph.  Also the vertex stage alone against HBM."""
+    does it (render-engine.cpp:797-1135, water-grid.vert, water-grid.frag), on
+    a 1024^2 grid with the 32 waves and noise heightmap of the 1024^2 workload:
+    camera -> projected-grid corners (one-thread FP64 kernel) -> displacement
+    + normals -> clip / NDC-at-height-0 / view vector / facing normal /
+    yaw-only normal -> rasterisation at 1920 x 1080 -> water shading, replayed
+    as one CUDA graph.  Also each stage alone, the vertex stage against HBM."""
     import torch
     w = workloads.config2()
     amp = wt.displaceable_amplitude(w.waves, w.heightmap.disp_scale)
@@ -212,10 +213,32 @@ def frame_pipeline(wt, workloads, stream, flush):
     outs = {k: torch.empty((n, 2 if k == "ndc0" else 4), device="cuda")
             for k in ("clip", "ndc0", "view", "facing", "nrm_yaw")}
 
+    # the fragment stage at 1920 x 1080: seeded sky box and local reflection /
+    # refraction targets, nothing drawn behind the water
+    VW, VH = 1920, 1080
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    sky = torch.randint(0, 256, (6, 256, 256, 4), dtype=torch.uint8, device="cuda", generator=gen)
+    lrefl = torch.randint(0, 256, (VH, VW, 4), dtype=torch.uint8, device="cuda", generator=gen)
+    lrefr = torch.randint(0, 256, (VH, VW, 4), dtype=torch.uint8, device="cuda", generator=gen)
+    idx = wt.grid_indices(int(patch["cols"][0]), int(patch["rows"][0]))
+    frags = torch.empty((VH, VW), dtype=torch.int64, device="cuda")
+    colour = torch.empty((VH, VW, 4), dtype=torch.float32, device="cuda")
+    shading = wt.water_shading(sun_position=(0.6, 0.8, 0.0))
+
+    def raster():
+        wt.water_raster(outs["clip"], idx, VW, VH, fragments=frags)
+
+    def shade():
+        wt.water_shade(frags, outs["clip"], idx, outs, VW, VH, shading, sky, local_reflections=lrefl,
+                       local_refractions=lrefr, colour=colour)
+
     def frame(s=None):
         wt.projected_grid_async(cam_dev, surf.patches, view_dev, stream=s)
         surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD, stream=s)
         wt.vertex_stage(view_dev, pos, nrm, out=outs, stream=s)
+        wt.water_raster(outs["clip"], idx, VW, VH, fragments=frags, stream=s)
+        wt.water_shade(frags, outs["clip"], idx, outs, VW, VH, shading, sky, local_reflections=lrefl,
+                       local_refractions=lrefr, colour=colour, stream=s)
 
     for _ in range(3):
         frame()
@@ -232,13 +255,17 @@ def frame_pipeline(wt, workloads, stream, flush):
     gms = _event_ms(lambda: wt.projected_grid_async(cam_dev, surf.patches, view_dev), 20, stream, flush)
     dms = _event_ms(lambda: surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD), 20, stream, flush)
     vms = _event_ms(lambda: wt.vertex_stage(view_dev, pos, nrm, out=outs), 20, stream, flush)
+    rms = _event_ms(raster, 20, stream, flush)
+    sms = _event_ms(shade, 20, stream, flush)
+    covered = float(((frags & 0xffffffff) != 0).float().mean())
     stage_bytes = n * (2 * 16 + 16 + 8 + 3 * 16)  # reads pos + nrm, writes clip, ndc0, view, facing, nrm_yaw
     try:
         hbm_peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
         peak_src = "MEASURED_PEAKS.json hbm_gbs (copy, measured)"
     except (OSError, KeyError, ValueError):
         hbm_peak, peak_src = 6800.0, "fallback 6.8 TB/s"
-    return {"vertices": n, "terms": n * len(w.waves), "frame_graph_ms": fms,
+    return {"vertices": n, "terms": n * len(w.waves), "viewport": [VW, VH], "water_pixels_frac": covered,
+            "frame_graph_ms": fms, "raster_ms": rms, "shade_ms": sms,
             "frames_per_s": 1e3 / fms, "projected_grid_kernel_ms": gms, "displace_ms": dms,
             "vertex_stage_ms": vms, "vertex_stage_bytes": stage_bytes,
             "vertex_stage_gbs": stage_bytes / (vms * 1e-3) / 1e9,

@@ -337,6 +337,75 @@ wt_status wt_vertex_stage(const wt_view* view, const float* pos, const float* nr
                           uint32_t flags, float* clip_out, float* ndc0_out, float* view_out,
                           float* facing_out, float* nrm_yaw_out, wt_stream stream);
 
+/* ---- water shading (the fragment stage) ---------------------------------- */
+
+/* Uniforms of the water fragment shader (assets/shaders/water-grid.frag:34-53),
+ * with the reference's defaults (src/render-engine.h:221-235,
+ * src/render-engine.cpp:288-296, 1061-1111).  72 bytes. */
+typedef struct wt_water_shading {
+    float sun_position[3];      /* sunPosition: world-space direction towards the sun, (cos a, sin a, 0) */
+    float sun_shininess;        /* 50 */
+    float sun_strength;         /* 1 */
+    float water_clarity;        /* 0.3 */
+    float soft_edges_threshold; /* softEdgesDeltaDepthThreshold, 0.05 */
+    float tint_threshold;       /* tintDeltaDepthThreshold, 0.1 */
+    float fog_colour[4];        /* fogColourFarAtCurrentTime: rgb, a = density at the far radius */
+    float fog_radius_near;      /* fogDepthRadiusNear, 0 */
+    float fog_radius_far;       /* fogDepthRadiusFar, 1 */
+    float z_near;               /* 0.1 */
+    float z_far;                /* 100 */
+} wt_water_shading;
+
+/* The render targets the water pass samples, at the viewport's size (device
+ * memory; row 0 is the bottom row, as GL stores them).  40 bytes. */
+typedef struct wt_water_textures {
+    const float* scene_depth;          /* depthTexture2D: width*height window depths in [0, 1] of what
+                                          was drawn before the water; NULL = cleared (1.0) */
+    const uint8_t* local_reflections;  /* localReflectionsTexture2D, width*height RGBA8; NULL = (0,0,0,0) */
+    const uint8_t* local_refractions;  /* localRefractionsTexture2D, width*height RGBA8; NULL = (0,0,0,0) */
+    const uint8_t* skybox;             /* the sky cube map: 6 faces (+X, -X, +Y, -Y, +Z, -Z) of
+                                          skybox_size^2 RGBA8, face row 0 at t = 0 */
+    uint32_t skybox_size;
+    uint32_t _pad;
+} wt_water_textures;
+
+/* Rasterises the grid's triangles (the glDrawElements of
+ * src/render-engine.cpp:1120, triangle list from wt_grid_indices) into a
+ * visibility buffer: fragments[y*width + x] = (window depth bits << 32) |
+ * (triangle + 1) of the nearest water fragment at pixel centre (x+0.5, y+0.5)
+ * that passes GL_LESS against scene_depth, or (scene depth bits << 32) | 0
+ * where none does.  Vertices are the clip positions wt_vertex_stage wrote
+ * (float4).  Window coordinates are snapped to 1/256 pixel and covered
+ * with exact integer edge functions (pixel centres on an edge belong to the
+ * triangle whose edge is a left or top edge); triangles reaching behind the
+ * near plane or far outside the viewport are clipped in clip space first.
+ * Ties in depth go to the lower triangle index (the first one drawn, as
+ * GL_LESS keeps it).  Independent of launch order: bitwise reproducible.
+ * Needs no workspace; fragments: device, width*height uint64. */
+wt_status wt_water_raster(const float* clip, uint64_t n_vertices, const uint32_t* indices, uint64_t n_triangles,
+                          uint32_t width, uint32_t height, const float* scene_depth, uint64_t* fragments,
+                          wt_stream stream);
+
+/* Shades every water pixel of a visibility buffer with the arithmetic of
+ * water-grid.frag:65-151: perspective-correct varyings (facing normal, yaw-only
+ * normal, view vector, NDC at height 0 from wt_vertex_stage, float4 / float2
+ * layouts), sky-box reflection plus sun highlight, Schlick Fresnel, distorted
+ * local reflection / refraction look-ups, depth tint, soft edges and fog.
+ *   colour_out : device RGBA float per pixel or NULL: the water fragment's
+ *                colour (alpha = edge hardness), (0, 0, 0, 0) where no water
+ *   composite  : device RGBA float per pixel or NULL: blended over in place with
+ *                glBlendFunc(GL_SRC_ALPHA, GL_ONE_MINUS_SRC_ALPHA)
+ *                (src/render-engine.cpp:302-303)
+ * Pixels whose triangle or vertices lie outside n_triangles / n_vertices are
+ * treated as showing no water.
+ * shading, textures: host structs (texture pointers are device memory). */
+wt_status wt_water_shade(const uint64_t* fragments, const float* clip, uint64_t n_vertices,
+                         const uint32_t* indices, uint64_t n_triangles,
+                         const float* facing, const float* nrm_yaw, const float* view, const float* ndc0,
+                         uint32_t width, uint32_t height, const wt_water_shading* shading,
+                         const wt_water_textures* textures, float* colour_out, float* composite,
+                         wt_stream stream);
+
 /* Heightmap texels from an 8-bit image already decoded into device memory,
  * as the reference loads its heightmap (src/render-engine.cpp:1308-1322):
  * stbi_load with vertical flip on load, forced to RGBA8, then sampled as a

@@ -19,9 +19,10 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-SOURCES = ["gerstner_f64.c", "reference_mode.c", "indices_noise.c", "projgrid.c"]
+SOURCES = ["gerstner_f64.c", "reference_mode.c", "indices_noise.c", "projgrid.c", "water.c"]
 LIB = BUILD / "liboracle.so"
 REF_LIB = REF_OUT / "libwgvert_ref.so"
+REF_FRAG_LIB = REF_OUT / "libwgfrag_ref.so"
 CFLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-std=c11", "-Wall"]
 
 
@@ -48,29 +49,39 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def build_ref(force: bool = False) -> Path | None:
-    """Compile the reference shader where it lies; None if it is absent."""
-    src = reference_dir() / "assets" / "shaders" / "water-grid.vert"
+    """Compile the reference vertex shader where it lies; None if it is absent."""
+    return _build_shader("water-grid.vert", "glsl_shim.hpp", "ref_driver.inc", REF_LIB, force)
+
+
+def build_ref_frag(force: bool = False) -> Path | None:
+    """Compile the reference water fragment shader where it lies; None if absent."""
+    return _build_shader("water-grid.frag", "glsl_frag_shim.hpp", "ref_frag_driver.inc", REF_FRAG_LIB, force)
+
+
+def _build_shader(name: str, shim: str, driver: str, out: Path, force: bool) -> Path | None:
+    src = reference_dir() / "assets" / "shaders" / name
     if not src.exists():
         return None
     REF_OUT.mkdir(exist_ok=True)
-    deps = [src, HERE / "glsl_shim.hpp", HERE / "ref_driver.inc", HERE / "wt_oracle.h"]
-    if not (force or _stale(REF_LIB, deps)):
-        return REF_LIB
+    deps = [src, HERE / shim, HERE / driver, HERE / "wt_oracle.h", HERE.parent / "include" / "wt.h"]
+    if not (force or _stale(out, deps)):
+        return out
     text = src.read_text()
     first, _, body = text.partition("\n")
     if not first.startswith("#version"):
         raise RuntimeError(f"unexpected first line in {src}: {first!r}")
     # The GLSL '#version' line is the only line that is not C++; it is dropped
     # and the rest is compiled unchanged between the shim and the driver.
-    tu = ('#include "glsl_shim.hpp"\n'
+    tu = (f'#include "{shim}"\n'
           f'#line 2 "{src}"\n' + body +
-          '\n#include "ref_driver.inc"\n')
+          f'\n#include "{driver}"\n')
     cmd = ["g++", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
-           "-std=gnu++17", "-w", "-I", str(HERE), "-x", "c++", "-", "-o", str(REF_LIB)]
+           "-std=gnu++17", "-w", "-I", str(HERE), "-x", "c++", "-", "-o", str(out)]
     subprocess.run(cmd, input=tu.encode(), check=True)
-    return REF_LIB
+    return out
 
 
 if __name__ == "__main__":
     print(build_oracle(force=True))
     print(build_ref(force=True))
+    print(build_ref_frag(force=True))

@@ -44,6 +44,26 @@ class RefOutputs(C.Structure):
                 ("position", "clip", "ndc0", "view", "normal", "normal_yaw", "colour")]
 
 
+class WaterShading(C.Structure):
+    _fields_ = [("sun_position", C.c_float * 3), ("sun_shininess", C.c_float), ("sun_strength", C.c_float),
+                ("water_clarity", C.c_float), ("soft_edges_threshold", C.c_float), ("tint_threshold", C.c_float),
+                ("fog_colour", C.c_float * 4), ("fog_radius_near", C.c_float), ("fog_radius_far", C.c_float),
+                ("z_near", C.c_float), ("z_far", C.c_float)]
+
+
+class WaterTextures(C.Structure):
+    _fields_ = [("scene_depth", C.c_void_p), ("local_reflections", C.c_void_p), ("local_refractions", C.c_void_p),
+                ("skybox", C.c_void_p), ("skybox_size", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+class FragUniforms(C.Structure):
+    _fields_ = [("s", WaterShading), ("tex", WaterTextures), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+FRAG_IN_DTYPE = np.dtype([("frag_coord", "<f4", (4,)), ("normal", "<f4", (3,)), ("normal_yaw", "<f4", (3,)),
+                          ("view", "<f4", (3,)), ("ndc0", "<f4", (2,))])
+
+
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
@@ -75,6 +95,9 @@ def lib():
             f.argtypes = [vp, vp, vp, vp, C.POINTER(C.c_uint32)]
             f.restype = C.c_int
         _lib.wto_vertex_stage_f64.argtypes = [vp, vp, vp, C.c_uint64, vp, vp, vp, vp, vp]
+        _lib.wto_water_fragment.argtypes = [C.POINTER(FragUniforms), vp, C.c_uint64, vp]
+        _lib.wto_water_raster.argtypes = [vp, C.c_uint64, vp, C.c_uint64, C.c_uint32, C.c_uint32, vp, vp]
+        _lib.wto_water_shade.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.POINTER(FragUniforms), vp, vp]
     return _lib
 
 
@@ -247,6 +270,87 @@ def heightmap_from_unorm8(pixels, flip=True):
     if flip:
         red = red[::-1]
     return np.ascontiguousarray(red.astype(np.float32) / np.float32(255.0))
+
+
+_ref_frag = None
+
+
+def ref_frag_lib():
+    """The reference's water fragment shader compiled from its own source, or
+    None when the reference checkout is not on this machine."""
+    global _ref_frag
+    if _ref_frag is None:
+        path = _build.REF_FRAG_LIB
+        if not path.exists():
+            if _build.build_ref_frag() is None:
+                return None
+        _ref_frag = C.CDLL(str(path))
+        _ref_frag.wtref_fragment.argtypes = [C.POINTER(FragUniforms), C.c_void_p, C.c_uint64, C.c_void_p]
+        _ref_frag.wtref_fragment.restype = C.c_int
+    return _ref_frag
+
+
+def frag_uniforms(shading: dict, width, height, scene_depth=None, local_reflections=None, local_refractions=None,
+                  skybox=None):
+    """A wto_frag_uniforms over host arrays; returns (uniforms, keepalive).
+    skybox: (6, S, S, 4) uint8; local textures (H, W, 4) uint8; depth (H, W) float32."""
+    U = FragUniforms()
+    for k, v in shading.items():
+        f = getattr(U.s, k)
+        if hasattr(f, "__len__"):
+            f[:] = list(v)
+        else:
+            setattr(U.s, k, float(v))
+    keep = []
+    for name, arr, dt in (("scene_depth", scene_depth, np.float32), ("local_reflections", local_reflections, np.uint8),
+                          ("local_refractions", local_refractions, np.uint8), ("skybox", skybox, np.uint8)):
+        if arr is not None:
+            a = np.ascontiguousarray(arr, dtype=dt)
+            keep.append(a)
+            setattr(U.tex, name, a.ctypes.data)
+    U.tex.skybox_size = 0 if skybox is None else int(np.asarray(skybox).shape[1])
+    U.width, U.height = width, height
+    return U, keep
+
+
+def water_fragment(U, frags):
+    """The FP32 restatement of water-grid.frag (oracle/water.c)."""
+    f = np.ascontiguousarray(frags, dtype=FRAG_IN_DTYPE)
+    out = np.zeros((len(f), 4), np.float32)
+    lib().wto_water_fragment(C.byref(U), _ptr(f), len(f), _ptr(out))
+    return out
+
+
+def reference_water_fragment(U, frags):
+    """water-grid.frag itself compiled as C++ (oracle/_ref), or None."""
+    r = ref_frag_lib()
+    if r is None:
+        return None
+    f = np.ascontiguousarray(frags, dtype=FRAG_IN_DTYPE)
+    out = np.zeros((len(f), 4), np.float32)
+    if r.wtref_fragment(C.byref(U), _ptr(f), len(f), _ptr(out)) != 0:
+        raise ValueError("fragment uniforms need a sky box")
+    return out
+
+
+def water_raster(clip4, idx, width, height, scene_depth=None):
+    c = np.ascontiguousarray(clip4, dtype=np.float32)
+    i = np.ascontiguousarray(idx, dtype=np.uint32)
+    out = np.zeros(width * height, np.uint64)
+    d = None if scene_depth is None else np.ascontiguousarray(scene_depth, dtype=np.float32)
+    lib().wto_water_raster(_ptr(c), len(c), _ptr(i), len(i) // 3, width, height, _ptr(d), _ptr(out))
+    return out
+
+
+def water_shade(frags, clip4, idx, facing4, nyaw4, view4, ndc0, U, composite=None):
+    arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (clip4, facing4, nyaw4, view4, ndc0)]
+    fr = np.ascontiguousarray(frags, dtype=np.uint64)
+    i = np.ascontiguousarray(idx, dtype=np.uint32)
+    out = np.zeros((U.width * U.height, 4), np.float32)
+    comp = None if composite is None else np.ascontiguousarray(composite, dtype=np.float32).copy()
+    lib().wto_water_shade(_ptr(fr), _ptr(arrs[0]), _ptr(i), _ptr(arrs[1]), _ptr(arrs[2]), _ptr(arrs[3]),
+                          _ptr(arrs[4]), C.byref(U), _ptr(out), _ptr(comp))
+    return out, comp
 
 
 def grid_indices(cols, rows, base=0):

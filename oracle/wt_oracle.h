@@ -162,6 +162,40 @@ int wto_projected_grid_f64(const wt_camera* cam, double corners[4][2], double vp
 void wto_vertex_stage_f64(const wt_view* v, const float* pos4, const float* nrm4, uint64_t n, double* clip4,
                           double* ndc2, double* view3, double* facing3, double* nyaw3);
 
+
+/* ---- the water fragment stage (water.c) ---------------------------------- */
+
+/* Inputs of one fragment of water-grid.frag: gl_FragCoord and the varyings. */
+typedef struct wto_frag_in {
+    float frag_coord[4];  /* window x, y (pixel centre), depth z, 1/w (unused) */
+    float normal[3];
+    float normal_yaw[3];
+    float view[3];
+    float ndc0[2];
+} wto_frag_in;
+
+/* Its uniforms: the shading parameters, the textures (host memory here) and
+ * the viewport size. */
+typedef struct wto_frag_uniforms {
+    wt_water_shading s;
+    wt_water_textures tex;
+    uint32_t width, height;
+} wto_frag_uniforms;
+
+/* water-grid.frag:65-151 for n fragments -> RGBA colour (FP32 restatement). */
+void wto_water_fragment(const wto_frag_uniforms* u, const wto_frag_in* f, uint64_t n, float* colour4);
+
+/* The rasteriser of wt_water_raster, restated: fragments[width*height]. */
+void wto_water_raster(const float* clip4, uint64_t n_vertices, const uint32_t* idx, uint64_t n_triangles,
+                      uint32_t width, uint32_t height, const float* scene_depth, uint64_t* fragments);
+
+/* wt_water_shade restated: perspective-correct varyings of each pixel's
+ * fragment, then wto_water_fragment; colour_out / composite as there (either
+ * may be NULL).  Vertex arrays are float4 (ndc0: float2). */
+void wto_water_shade(const uint64_t* fragments, const float* clip4, const uint32_t* idx, const float* facing4,
+                     const float* nyaw4, const float* view4, const float* ndc0, const wto_frag_uniforms* u,
+                     float* colour_out, float* composite);
+
 #ifdef __cplusplus
 }
 #endif

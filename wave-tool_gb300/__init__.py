@@ -34,6 +34,7 @@ EXPORTED = [
     "wt_gerstner_adjoint", "wt_grid_indices", "wt_noise_synth", "wt_wave_from_reference",
     "wt_measure_peaks", "wt_set_tuning", "wt_get_tuning", "wt_autotune_displace",
     "wt_projected_grid", "wt_projected_grid_async", "wt_vertex_stage", "wt_heightmap_from_unorm8",
+    "wt_water_raster", "wt_water_shade",
 ]
 
 
@@ -52,6 +53,25 @@ class CHeightmap(C.Structure):
 class CTuning(C.Structure):
     _fields_ = [("warps_per_block", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("wave_chunk", C.c_uint32),
                 ("max_vertices_per_lane", C.c_uint32), ("epilogue_in_shared", C.c_uint32)]
+
+
+class CWaterShading(C.Structure):
+    _fields_ = [("sun_position", C.c_float * 3), ("sun_shininess", C.c_float), ("sun_strength", C.c_float),
+                ("water_clarity", C.c_float), ("soft_edges_threshold", C.c_float), ("tint_threshold", C.c_float),
+                ("fog_colour", C.c_float * 4), ("fog_radius_near", C.c_float), ("fog_radius_far", C.c_float),
+                ("z_near", C.c_float), ("z_far", C.c_float)]
+
+
+class CWaterTextures(C.Structure):
+    _fields_ = [("scene_depth", C.c_void_p), ("local_reflections", C.c_void_p), ("local_refractions", C.c_void_p),
+                ("skybox", C.c_void_p), ("skybox_size", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+# the reference's water shading defaults (render-engine.h:221-235, Z_NEAR / Z_FAR)
+WATER_SHADING_DEFAULTS = dict(sun_position=(0.0, 1.0, 0.0), sun_shininess=50.0, sun_strength=1.0,
+                              water_clarity=0.3, soft_edges_threshold=0.05, tint_threshold=0.1,
+                              fog_colour=(1.0, 1.0, 1.0, 0.1), fog_radius_near=0.0, fog_radius_far=1.0,
+                              z_near=0.1, z_far=100.0)
 
 
 class CWave(C.Structure):
@@ -98,6 +118,9 @@ def lib():
         L.wt_projected_grid_async.argtypes = [vp, vp, vp, vp]
         L.wt_vertex_stage.argtypes = [vp, vp, vp, u64, u32, vp, vp, vp, vp, vp, vp]
         L.wt_heightmap_from_unorm8.argtypes = [vp, u32, u32, u32, u64, u32, vp, vp]
+        L.wt_water_raster.argtypes = [vp, u64, vp, u64, u32, u32, vp, vp, vp]
+        L.wt_water_shade.argtypes = [vp, vp, u64, vp, u64, vp, vp, vp, vp, u32, u32, C.POINTER(CWaterShading),
+                                     C.POINTER(CWaterTextures), vp, vp, vp]
         for name in EXPORTED:
             if name not in ("wt_version", "wt_last_error"):
                 getattr(L, name).restype = C.c_int
@@ -369,6 +392,55 @@ def vertex_stage(view_dev, pos, nrm=None, flags: int = 0, clip=True, ndc0=True, 
     return out
 
 
+# ---- water shading (the fragment stage) --------------------------------------
+
+def water_shading(**kw) -> CWaterShading:
+    """A wt_water_shading: the reference's defaults, overridden by kw."""
+    vals = dict(WATER_SHADING_DEFAULTS, **kw)
+    s = CWaterShading()
+    for k, v in vals.items():
+        f = getattr(s, k)
+        if hasattr(f, "__len__"):
+            f[:] = [float(x) for x in v]
+        else:
+            setattr(s, k, float(v))
+    return s
+
+
+def water_raster(clip, indices, width: int, height: int, scene_depth=None, fragments=None, stream=None):
+    """Visibility buffer (int64 tensor of height x width keys) of the
+    triangles `indices` over float4 clip positions."""
+    torch = _torch()
+    if fragments is None:
+        fragments = torch.empty((height, width), dtype=torch.int64, device=clip.device)
+    check(lib().wt_water_raster(clip.data_ptr(), clip.shape[0], indices.data_ptr(), indices.numel() // 3, width,
+                                height, _ptr(scene_depth), fragments.data_ptr(), stream_handle(stream)))
+    return fragments
+
+
+def water_shade(fragments, clip, indices, stage: dict, width: int, height: int, shading: CWaterShading, skybox,
+                scene_depth=None, local_reflections=None, local_refractions=None, colour=None, composite=None,
+                stream=None):
+    """Shades the water pixels of a visibility buffer.  `stage` holds the
+    vertex-stage outputs (facing, nrm_yaw, view, ndc0); skybox: (6, S, S, 4)
+    uint8 device tensor; local textures (H, W, 4) uint8; scene depth (H, W)
+    float32.  Returns the (H, W, 4) float32 colour tensor (colour=False: none,
+    for a call that only blends into `composite`)."""
+    torch = _torch()
+    if colour is None:
+        colour = torch.empty((height, width, 4), dtype=torch.float32, device=clip.device)
+    elif colour is False:
+        colour = None
+    tex = CWaterTextures(_ptr(scene_depth), _ptr(local_reflections), _ptr(local_refractions), skybox.data_ptr(),
+                         int(skybox.shape[1]), 0)
+    check(lib().wt_water_shade(fragments.data_ptr(), clip.data_ptr(), clip.shape[0], indices.data_ptr(),
+                               indices.numel() // 3, stage["facing"].data_ptr(),
+                               stage["nrm_yaw"].data_ptr(), stage["view"].data_ptr(), stage["ndc0"].data_ptr(),
+                               width, height, C.byref(shading), C.byref(tex), _ptr(colour), _ptr(composite),
+                               stream_handle(stream)))
+    return colour
+
+
 def heightmap_from(workload_hm, texels=None) -> DeviceHeightmap | None:
     """Device heightmap of a workloads.Heightmap: synthesised on the GPU
     unless texels are given."""
@@ -386,5 +458,6 @@ __all__ = [
     "NOISE_TERM_DTYPE", "WAVE_GRAD_DTYPE", "WT_OUT_WORLD", "WT_OUT_DISPLACEMENT", "WT_LAYOUT_FLOAT4",
     "WT_LAYOUT_VEC3", "WT_PHASE_FP64", "WT_PHASE_FP32_NAIVE", "WT_WRAP_REPEAT", "WT_WRAP_MIRRORED_REPEAT",
     "EXPORTED", "math", "CAMERA_DTYPE", "VIEW_DTYPE", "camera", "displaceable_amplitude", "projected_grid",
-    "projected_grid_async", "vertex_stage",
+    "projected_grid_async", "vertex_stage", "water_shading", "water_raster", "water_shade",
+    "WATER_SHADING_DEFAULTS",
 ]

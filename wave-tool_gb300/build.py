@@ -22,6 +22,11 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-Wal
                      "--expt-relaxed-constexpr", "-I", str(INCLUDE), "-I", str(CSRC)]
 
 
+# per-file extra flags: the water fragment stage rounds every FP32 operation
+# once, in source order (no fused multiply-add), like its CPU restatement
+FILE_FLAGS = {"wt_water.cu": ["-fmad=false"]}
+
+
 def nvcc() -> str:
     for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
         if c and (Path(c).exists() or c == "nvcc"):
@@ -50,7 +55,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         src, obj = pair
         if not force and not _stale(obj, [src, *headers]):
             return None
-        cmd = [nvcc(), *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+        cmd = [nvcc(), *NVCC_FLAGS, *FILE_FLAGS.get(src.name, []), "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             return f"{' '.join(cmd)}\n{r.stdout}\n{r.stderr}"

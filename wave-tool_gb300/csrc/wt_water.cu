@@ -1,0 +1,551 @@
+// wt_water.cu — the water fragment stage: rasterisation of the grid's
+// triangles into a visibility buffer, then per-pixel shading with the
+// arithmetic of assets/shaders/water-grid.frag:65-151.
+//
+// This file is compiled with -fmad=false: every FP32 operation rounds once,
+// in source order, so coverage, depth and all but the transcendental-bearing
+// colour terms reproduce a scalar CPU restatement bit for bit.
+//
+// Rasterisation (k_water_raster): one lane per triangle.  Window coordinates
+// are snapped to 1/256 pixel and covered with exact 64-bit integer edge
+// functions at pixel centres (left/top fill rule); the window depth is
+// interpolated linearly in screen space and folded with the triangle index
+// into one 64-bit key, (depth bits << 32) | (triangle + 1), kept per pixel by
+// atomicMin: nearest fragment wins, ties go to the lower index, and the
+// result does not depend on launch order.  Triangles with more than
+// kSmallPixels pixels in their box, and triangles that reach behind the near
+// plane or past a guard band of 64 viewports (clipped in clip space first),
+// are rasterised by their whole warp, one after another, lanes striding over
+// the pixels.
+//
+// Shading (k_water_shade): one thread per pixel; perspective-correct
+// barycentrics from the triangle's three clip-space vertices (2D homogeneous
+// form), varyings, then the fragment shader's terms.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+
+#include "wt_internal.h"
+
+namespace {
+
+constexpr float kSub = 256.0f;   // sub-pixel steps per pixel
+constexpr float kGuard = 64.0f;  // guard band, in NDC units
+constexpr int kSmallPixels = 16;
+constexpr unsigned kFull = 0xffffffffu;
+
+struct CV4 {
+    float x, y, z, w;
+};
+
+struct WinTri {
+    int32_t X[3], Y[3];
+    float Z[3];
+};
+
+__device__ __forceinline__ void to_window(const CV4& c, float hw, float hh, int32_t& X, int32_t& Y, float& Z) {
+    const float xw = (c.x / c.w + 1.0f) * hw;
+    const float yw = (c.y / c.w + 1.0f) * hh;
+    X = __float2int_rn(xw * kSub);
+    Y = __float2int_rn(yw * kSub);
+    Z = (c.z / c.w) * 0.5f + 0.5f;
+}
+
+__device__ __forceinline__ bool inside_guard(const CV4& c) {
+    return c.w > 0.0f && fabsf(c.x) <= kGuard * c.w && fabsf(c.y) <= kGuard * c.w;
+}
+
+__device__ __forceinline__ float plane_dist(int p, const CV4& c) {
+    switch (p) {
+        case 0: return c.z + c.w;              // near: z >= -w
+        case 1: return kGuard * c.w - c.x;
+        case 2: return kGuard * c.w + c.x;
+        case 3: return kGuard * c.w - c.y;
+        default: return kGuard * c.w + c.y;
+    }
+}
+
+// Sutherland-Hodgman against the near plane and the guard band; <= 8 vertices.
+__device__ int clip_polygon(CV4* poly, int n) {
+    CV4 tmp[8];
+    for (int p = 0; p < 5 && n > 0; ++p) {
+        int m = 0;
+        for (int i = 0; i < n; ++i) {
+            const CV4 a = poly[i], b = poly[i + 1 < n ? i + 1 : 0];
+            const float da = plane_dist(p, a), db = plane_dist(p, b);
+            if (da >= 0.0f && m < 8) tmp[m++] = a;
+            if ((da >= 0.0f) != (db >= 0.0f) && m < 8) {
+                const float t = da / (da - db);
+                tmp[m++] = CV4{a.x + t * (b.x - a.x), a.y + t * (b.y - a.y), a.z + t * (b.z - a.z),
+                               a.w + t * (b.w - a.w)};
+            }
+        }
+        for (int i = 0; i < m; ++i) poly[i] = tmp[i];
+        n = m;
+    }
+    return n;
+}
+
+// Oriented triangle with its pixel box and fill-rule flags.
+struct Setup {
+    int32_t x[3], y[3];
+    float z[3];
+    float area_f;
+    int32_t px0, px1, py0, py1;
+    int incl;  // bit k: edge k (vertex k+1 -> k+2) owns pixel centres exactly on it
+};
+
+__device__ __forceinline__ bool setup_tri(const WinTri& w, uint32_t W, uint32_t H, Setup& s) {
+    int64_t area = (int64_t)(w.X[1] - w.X[0]) * (w.Y[2] - w.Y[0]) - (int64_t)(w.Y[1] - w.Y[0]) * (w.X[2] - w.X[0]);
+    if (area == 0) return false;
+    const int a = area > 0 ? 1 : 2, b = area > 0 ? 2 : 1;  // counter-clockwise order
+    s.x[0] = w.X[0]; s.y[0] = w.Y[0]; s.z[0] = w.Z[0];
+    s.x[1] = w.X[a]; s.y[1] = w.Y[a]; s.z[1] = w.Z[a];
+    s.x[2] = w.X[b]; s.y[2] = w.Y[b]; s.z[2] = w.Z[b];
+    if (area < 0) area = -area;
+    s.area_f = (float)area;
+    const int32_t xmin = min(s.x[0], min(s.x[1], s.x[2])), xmax = max(s.x[0], max(s.x[1], s.x[2]));
+    const int32_t ymin = min(s.y[0], min(s.y[1], s.y[2])), ymax = max(s.y[0], max(s.y[1], s.y[2]));
+    int64_t px0 = -((128 - (int64_t)xmin) >> 8), px1 = ((int64_t)xmax - 128) >> 8;
+    int64_t py0 = -((128 - (int64_t)ymin) >> 8), py1 = ((int64_t)ymax - 128) >> 8;
+    px0 = px0 < 0 ? 0 : px0;
+    py0 = py0 < 0 ? 0 : py0;
+    px1 = px1 > (int64_t)W - 1 ? (int64_t)W - 1 : px1;
+    py1 = py1 > (int64_t)H - 1 ? (int64_t)H - 1 : py1;
+    if (px0 > px1 || py0 > py1) return false;
+    s.px0 = (int32_t)px0; s.px1 = (int32_t)px1; s.py0 = (int32_t)py0; s.py1 = (int32_t)py1;
+    s.incl = 0;
+    for (int k = 0; k < 3; ++k) {
+        const int i = k == 2 ? 0 : k + 1, j = k == 0 ? 2 : (k == 1 ? 0 : 1);
+        const int32_t dx = s.x[j] - s.x[i], dy = s.y[j] - s.y[i];
+        if (dy < 0 || (dy == 0 && dx < 0)) s.incl |= 1 << k;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void raster_pixel(const Setup& s, int32_t px, int32_t py, uint32_t tri, uint32_t W,
+                                             unsigned long long* frag) {
+    const int64_t cx = (int64_t)px * 256 + 128, cy = (int64_t)py * 256 + 128;
+    int64_t e[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int i = k == 2 ? 0 : k + 1, j = k == 0 ? 2 : (k == 1 ? 0 : 1);
+        e[k] = (int64_t)(s.x[j] - s.x[i]) * (cy - s.y[i]) - (int64_t)(s.y[j] - s.y[i]) * (cx - s.x[i]);
+        if (!(e[k] > 0 || (e[k] == 0 && ((s.incl >> k) & 1)))) return;
+    }
+    float d = ((float)e[0] * s.z[0] + (float)e[1] * s.z[1] + (float)e[2] * s.z[2]) / s.area_f;
+    if (!(d >= 0.0f && d <= 1.0f)) return;
+    d = d + 0.0f;  // -0 -> +0
+    const unsigned long long key = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned long long)(tri + 1u);
+    unsigned long long* slot = frag + (size_t)py * W + px;
+    if (key < *slot) atomicMin(slot, key);
+}
+
+__device__ __forceinline__ void raster_own(const Setup& s, uint32_t tri, uint32_t W, unsigned long long* frag) {
+    for (int32_t py = s.py0; py <= s.py1; ++py)
+        for (int32_t px = s.px0; px <= s.px1; ++px) raster_pixel(s, px, py, tri, W, frag);
+}
+
+__device__ __forceinline__ void raster_warp(const Setup& s, uint32_t tri, uint32_t W, unsigned long long* frag,
+                                            int lane) {
+    const int64_t bw = (int64_t)s.px1 - s.px0 + 1;
+    const int64_t n = bw * ((int64_t)s.py1 - s.py0 + 1);
+    for (int64_t p = lane; p < n; p += 32) {
+        const int64_t r = p / bw;
+        raster_pixel(s, (int32_t)(s.px0 + (p - r * bw)), (int32_t)(s.py0 + r), tri, W, frag);
+    }
+}
+
+__device__ __forceinline__ WinTri shfl_tri(const WinTri& w, int src) {
+    WinTri o;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        o.X[k] = __shfl_sync(kFull, w.X[k], src);
+        o.Y[k] = __shfl_sync(kFull, w.Y[k], src);
+        o.Z[k] = __shfl_sync(kFull, w.Z[k], src);
+    }
+    return o;
+}
+
+__global__ void __launch_bounds__(256) k_water_clear(const float* __restrict__ scene_depth, uint64_t n,
+                                                     unsigned long long* __restrict__ frag) {
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n; p += (uint64_t)gridDim.x * blockDim.x) {
+        const float d = scene_depth ? scene_depth[p] : 1.0f;
+        frag[p] = (unsigned long long)__float_as_uint(d) << 32;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_water_raster(const float4* __restrict__ clip, uint64_t n_vertices,
+                                                      const uint32_t* __restrict__ idx, uint64_t n_tri, uint32_t W,
+                                                      uint32_t H, unsigned long long* frag) {
+    const int lane = threadIdx.x & 31;
+    const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); base < n_tri; base += stride) {
+        const uint64_t t = base + lane;
+        int kind = 0;  // 0 nothing, 2 warp-rasterised window triangle, 3 clip first
+        CV4 v[3];
+        WinTri w;
+        if (t < n_tri) {
+            bool ok = true;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t i = idx[3 * t + k];
+                if (i >= n_vertices) {
+                    ok = false;
+                    break;
+                }
+                const float4 c = clip[i];
+                v[k] = CV4{c.x, c.y, c.z, c.w};
+            }
+            if (ok) {
+                if (inside_guard(v[0]) && inside_guard(v[1]) && inside_guard(v[2])) {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) to_window(v[k], hw, hh, w.X[k], w.Y[k], w.Z[k]);
+                    Setup s;
+                    if (setup_tri(w, W, H, s)) {
+                        const int64_t npix = ((int64_t)s.px1 - s.px0 + 1) * ((int64_t)s.py1 - s.py0 + 1);
+                        if (npix <= kSmallPixels) raster_own(s, (uint32_t)t, W, frag);
+                        else kind = 2;
+                    }
+                } else {
+                    kind = 3;
+                }
+            }
+        }
+        unsigned coop = __ballot_sync(kFull, kind >= 2);
+        while (coop) {
+            const int src = __ffs(coop) - 1;
+            coop &= coop - 1;
+            const int k = __shfl_sync(kFull, kind, src);
+            const uint32_t tri = (uint32_t)__shfl_sync(kFull, (unsigned long long)t, src);
+            if (k == 2) {
+                const WinTri sw = shfl_tri(w, src);
+                Setup s;
+                if (setup_tri(sw, W, H, s)) raster_warp(s, tri, W, frag, lane);
+                continue;
+            }
+            CV4 poly[8];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                poly[j].x = __shfl_sync(kFull, v[j].x, src);
+                poly[j].y = __shfl_sync(kFull, v[j].y, src);
+                poly[j].z = __shfl_sync(kFull, v[j].z, src);
+                poly[j].w = __shfl_sync(kFull, v[j].w, src);
+            }
+            const int n = clip_polygon(poly, 3);
+            bool bad = n < 3;
+            for (int j = 0; j < n; ++j) bad |= !(poly[j].w > 0.0f);
+            if (bad) continue;
+            for (int j = 1; j + 1 < n; ++j) {
+                WinTri sw;
+                to_window(poly[0], hw, hh, sw.X[0], sw.Y[0], sw.Z[0]);
+                to_window(poly[j], hw, hh, sw.X[1], sw.Y[1], sw.Z[1]);
+                to_window(poly[j + 1], hw, hh, sw.X[2], sw.Y[2], sw.Z[2]);
+                Setup s;
+                if (setup_tri(sw, W, H, s)) raster_warp(s, tri, W, frag, lane);
+            }
+        }
+    }
+}
+
+// ---- shading ---------------------------------------------------------------
+
+struct ShadeTex {
+    const float* depth;
+    const uint8_t* refl;
+    const uint8_t* refr;
+    const uint8_t* sky;
+    uint32_t sky_size;
+};
+
+__device__ __forceinline__ uint32_t clampi(int64_t i, uint32_t n) {
+    return (uint32_t)(i < 0 ? 0 : (i >= (int64_t)n ? n - 1 : i));
+}
+
+// GL_LINEAR, CLAMP_TO_EDGE over RGBA8 texels converted to c / 255.
+__device__ float4 bilinear_rgba8(const uint8_t* px, uint32_t w, uint32_t h, float s, float t) {
+    const float u = s * (float)w - 0.5f, v = t * (float)h - 0.5f;
+    const float fi = floorf(u), fj = floorf(v);
+    const float a = u - fi, b = v - fj;
+    const uint32_t i0 = clampi((int64_t)fi, w), i1 = clampi((int64_t)fi + 1, w);
+    const uint32_t j0 = clampi((int64_t)fj, h), j1 = clampi((int64_t)fj + 1, h);
+    const uchar4 q00 = *reinterpret_cast<const uchar4*>(px + 4 * ((size_t)j0 * w + i0));
+    const uchar4 q10 = *reinterpret_cast<const uchar4*>(px + 4 * ((size_t)j0 * w + i1));
+    const uchar4 q01 = *reinterpret_cast<const uchar4*>(px + 4 * ((size_t)j1 * w + i0));
+    const uchar4 q11 = *reinterpret_cast<const uchar4*>(px + 4 * ((size_t)j1 * w + i1));
+    auto f = [&](unsigned char c00, unsigned char c10, unsigned char c01, unsigned char c11) {
+        const float t00 = (float)c00 / 255.0f, t10 = (float)c10 / 255.0f;
+        const float t01 = (float)c01 / 255.0f, t11 = (float)c11 / 255.0f;
+        return (1.0f - b) * ((1.0f - a) * t00 + a * t10) + b * ((1.0f - a) * t01 + a * t11);
+    };
+    return make_float4(f(q00.x, q10.x, q01.x, q11.x), f(q00.y, q10.y, q01.y, q11.y), f(q00.z, q10.z, q01.z, q11.z),
+                       f(q00.w, q10.w, q01.w, q11.w));
+}
+
+// Cube-map face by the major axis (OpenGL 4.1 table 3.19), then bilinear.
+__device__ float4 sample_cube(const uint8_t* faces, uint32_t size, float rx, float ry, float rz) {
+    const float ax = fabsf(rx), ay = fabsf(ry), az = fabsf(rz);
+    int face;
+    float sc, tc, ma;
+    if (ax >= ay && ax >= az) {
+        face = rx >= 0.0f ? 0 : 1;
+        sc = rx >= 0.0f ? -rz : rz;
+        tc = -ry;
+        ma = ax;
+    } else if (ay >= az) {
+        face = ry >= 0.0f ? 2 : 3;
+        sc = rx;
+        tc = ry >= 0.0f ? rz : -rz;
+        ma = ay;
+    } else {
+        face = rz >= 0.0f ? 4 : 5;
+        sc = rz >= 0.0f ? rx : -rx;
+        tc = -ry;
+        ma = az;
+    }
+    const float s = (sc / ma + 1.0f) / 2.0f, t = (tc / ma + 1.0f) / 2.0f;
+    return bilinear_rgba8(faces + (size_t)face * size * size * 4, size, size, s, t);
+}
+
+__device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+__device__ __forceinline__ float mixf(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+
+__global__ void __launch_bounds__(256) k_water_shade(const unsigned long long* __restrict__ frag,
+                                                     const float4* __restrict__ clip, uint64_t n_vertices,
+                                                     const uint32_t* __restrict__ idx, uint64_t n_tri,
+                                                     const float4* __restrict__ facing,
+                                                     const float4* __restrict__ nyaw, const float4* __restrict__ view,
+                                                     const float2* __restrict__ ndc0, uint32_t W, uint32_t H,
+                                                     wt_water_shading sh, ShadeTex tex, float4* colour_out,
+                                                     float4* composite) {
+    const uint64_t n = (uint64_t)W * H;
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n; p += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long key = frag[p];
+        const uint32_t tri1 = (uint32_t)(key & 0xffffffffull);
+        const size_t t = tri1 - 1;
+        uint32_t vi[3] = {0u, 0u, 0u};
+        bool water = tri1 != 0 && t < n_tri;
+        if (water) {
+            vi[0] = idx[3 * t];
+            vi[1] = idx[3 * t + 1];
+            vi[2] = idx[3 * t + 2];
+            water = vi[0] < n_vertices && vi[1] < n_vertices && vi[2] < n_vertices;
+        }
+        if (!water) {
+            if (colour_out) colour_out[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            continue;
+        }
+        const uint32_t py = (uint32_t)(p / W), px = (uint32_t)(p - (uint64_t)py * W);
+        // perspective-correct weights: lambda_k ~ (v_{k+1} x v_{k+2}) . (ndc x, ndc y, 1)
+        const float nx = (2.0f * ((float)px + 0.5f)) / (float)W - 1.0f;
+        const float ny = (2.0f * ((float)py + 0.5f)) / (float)H - 1.0f;
+        float cv[3][3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float4 c = clip[vi[k]];
+            cv[k][0] = c.x;
+            cv[k][1] = c.y;
+            cv[k][2] = c.w;
+        }
+        float c[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float* a = cv[k == 2 ? 0 : k + 1];
+            const float* b = cv[k == 0 ? 2 : (k == 1 ? 0 : 1)];
+            const float cx = a[1] * b[2] - a[2] * b[1];
+            const float cy = a[2] * b[0] - a[0] * b[2];
+            const float cz = a[0] * b[1] - a[1] * b[0];
+            c[k] = cx * nx + cy * ny + cz;
+        }
+        const float sum = c[0] + c[1] + c[2];
+        const float l0 = c[0] / sum, l1 = c[1] / sum, l2 = c[2] / sum;
+        const float4 n0 = facing[vi[0]], n1 = facing[vi[1]], n2 = facing[vi[2]];
+        const float4 y0 = nyaw[vi[0]], y1 = nyaw[vi[1]], y2 = nyaw[vi[2]];
+        const float4 w0 = view[vi[0]], w1 = view[vi[1]], w2 = view[vi[2]];
+        const float2 d0 = ndc0[vi[0]], d1 = ndc0[vi[1]], d2 = ndc0[vi[2]];
+        const float N[3] = {l0 * n0.x + l1 * n1.x + l2 * n2.x, l0 * n0.y + l1 * n1.y + l2 * n2.y,
+                            l0 * n0.z + l1 * n1.z + l2 * n2.z};
+        const float NY[3] = {l0 * y0.x + l1 * y1.x + l2 * y2.x, l0 * y0.y + l1 * y1.y + l2 * y2.y,
+                             l0 * y0.z + l1 * y1.z + l2 * y2.z};
+        const float V[3] = {l0 * w0.x + l1 * w1.x + l2 * w2.x, l0 * w0.y + l1 * w1.y + l2 * w2.y,
+                            l0 * w0.z + l1 * w1.z + l2 * w2.z};
+        const float D0[2] = {l0 * d0.x + l1 * d1.x + l2 * d2.x, l0 * d0.y + l1 * d1.y + l2 * d2.y};
+        const float fz = __uint_as_float((uint32_t)(key >> 32));
+
+        // water-grid.frag:65-151
+        const float view_len = sqrtf(V[0] * V[0] + V[1] * V[1] + V[2] * V[2]);
+        const float view_depth = clampf(view_len / sh.z_far, 0.0f, 1.0f);
+        const float vv[3] = {V[0] / view_len, V[1] / view_len, V[2] / view_len};
+        const float u0 = ((float)px + 0.5f) / (float)W, u1 = ((float)py + 0.5f) / (float)H;
+        const float h0 = (D0[0] + 1.0f) / 2.0f, h1 = (D0[1] + 1.0f) / 2.0f;
+        float back_raw = 1.0f;
+        if (tex.depth)
+            back_raw = tex.depth[(size_t)clampi((int64_t)floorf(u1 * (float)H), H) * W +
+                                 clampi((int64_t)floorf(u0 * (float)W), W)];
+        const float back = (sh.z_near * back_raw) / (sh.z_far - back_raw * (sh.z_far - sh.z_near));
+        const float sky_behind = back > 0.999f ? 0.0f : 1.0f;
+        const float here = (sh.z_near * fz) / (sh.z_far - fz * (sh.z_far - sh.z_near));
+        const float delta = clampf(back - here, 0.0f, 1.0f);
+        const float I[3] = {-vv[0], -vv[1], -vv[2]};
+        const float kr = 2.0f * (N[0] * I[0] + N[1] * I[1] + N[2] * I[2]);
+        const float R[3] = {I[0] - kr * N[0], I[1] - kr * N[1], I[2] - kr * N[2]};
+        const float4 sky = sample_cube(tex.sky, tex.sky_size, R[0], R[1], R[2]);
+        const float sun_p = powf(
+            clampf(R[0] * sh.sun_position[0] + R[1] * sh.sun_position[1] + R[2] * sh.sun_position[2], 0.0f, 1.0f),
+            sh.sun_shininess);
+        const float sun = (sh.sun_strength * 1.0f) * sun_p;
+        const float cos_t = N[0] * vv[0] + N[1] * vv[1] + N[2] * vv[2];
+        const float fres = 0.02f + (1.0f - 0.02f) * powf(1.0f - cos_t, 5.0f);
+        const float ds = 0.1f * (1.0f - view_depth);  // both distortion strengths are 0.1
+        const float ul0 = clampf(mixf(u0, h0, ds) + ds * NY[0], 0.0f, 1.0f);
+        const float ul1 = clampf(mixf(u1, h1, ds) + ds * -NY[2], 0.0f, 1.0f);
+        const float ur0 = clampf(mixf(u0, h0, ds) + ds * -NY[0], 0.0f, 1.0f);
+        const float ur1 = clampf(mixf(u1, h1, ds) + ds * NY[2], 0.0f, 1.0f);
+        const float4 lrefl = tex.refl ? bilinear_rgba8(tex.refl, W, H, ul0, ul1) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 lrefr = tex.refr ? bilinear_rgba8(tex.refr, W, H, ur0, ur1) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float tint_f = 0.0f == sh.tint_threshold
+                                 ? 0.0f
+                                 : sky_behind * (1.0f - clampf(delta / sh.tint_threshold, 0.0f, 1.0f));
+        const float day = clampf(sh.sun_position[1], 0.0f, 1.0f);
+        const float clarity = sh.water_clarity * lrefr.w * (1.0f - delta);
+        const float deep[3] = {0.0f, 0.341f, 0.482f}, shallow[3] = {0.3f, 0.941f, 0.903f};
+        const float skyc[3] = {sky.x, sky.y, sky.z}, lrc[3] = {lrefl.x, lrefl.y, lrefl.z};
+        const float ltc[3] = {lrefr.x, lrefr.y, lrefr.z};
+        float out[4];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float tint = day * mixf(deep[k], shallow[k], tint_f);
+            const float trans = mixf(tint, ltc[k], clarity);
+            const float refl = mixf(skyc[k] + sun, lrc[k], lrefl.w);
+            out[k] = mixf(trans, refl, fres);
+        }
+        out[3] = 0.0f == sh.soft_edges_threshold
+                     ? 1.0f
+                     : 1.0f - (sky_behind * (1.0f - clampf(delta / sh.soft_edges_threshold, 0.0f, 1.0f)));
+        const float fog_a = view_depth >= sh.fog_radius_far
+                                ? sh.fog_colour[3]
+                                : view_depth <= sh.fog_radius_near
+                                      ? 0.0f
+                                      : sh.fog_colour[3] * ((view_depth - sh.fog_radius_near) /
+                                                            (sh.fog_radius_far - sh.fog_radius_near));
+#pragma unroll
+        for (int k = 0; k < 3; ++k) out[k] = mixf(out[k], sh.fog_colour[k], fog_a);
+        const float4 col = make_float4(out[0], out[1], out[2], out[3]);
+        if (colour_out) colour_out[p] = col;
+        if (composite) {
+            const float4 d = composite[p];
+            const float a = col.w;
+            composite[p] = make_float4(col.x * a + d.x * (1.0f - a), col.y * a + d.y * (1.0f - a),
+                                       col.z * a + d.z * (1.0f - a), col.w * a + d.w * (1.0f - a));
+        }
+    }
+}
+
+wt_status fail(wt_status s, const char* msg) {
+    wt::set_last_error(msg);
+    return s;
+}
+
+wt_status cuda_fail(cudaError_t e, const char* what) {
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+    wt::set_last_error(buf);
+    return WT_ERR_CUDA;
+}
+
+bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+
+int g_sms[64] = {};
+
+wt_status sms_of_device(int* sms) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= 64) return fail(WT_ERR_UNSUPPORTED, "device ordinal beyond 63");
+    if (!g_sms[dev]) {
+        e = cudaDeviceGetAttribute(&g_sms[dev], cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+    }
+    *sms = g_sms[dev];
+    return WT_OK;
+}
+
+bool viewport_ok(uint32_t w, uint32_t h) { return w >= 1 && h >= 1 && w <= 16384 && h <= 16384; }
+
+}  // namespace
+
+extern "C" wt_status wt_water_raster(const float* clip, uint64_t n_vertices, const uint32_t* indices,
+                                     uint64_t n_triangles, uint32_t width, uint32_t height, const float* scene_depth,
+                                     uint64_t* fragments, wt_stream stream) {
+    if (!viewport_ok(width, height)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: viewport outside [1, 16384]^2");
+    if (!fragments || !aligned(fragments, 8)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: fragments NULL or misaligned");
+    if (scene_depth && !aligned(scene_depth, 4)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: scene_depth misaligned");
+    if (n_triangles > 0) {
+        if (!clip || !aligned(clip, 16)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: clip NULL or not 16-byte aligned");
+        if (!indices || !aligned(indices, 4)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: indices NULL or misaligned");
+        if (n_triangles > (1ull << 32) - 2) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: more than 2^32 - 2 triangles");
+    }
+    int sms = 0;
+    wt_status st = sms_of_device(&sms);
+    if (st != WT_OK) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint64_t npx = (uint64_t)width * height;
+    const uint64_t cb = (npx + 255) / 256;
+    k_water_clear<<<(unsigned)(cb < (uint64_t)sms * 8 ? cb : (uint64_t)sms * 8), 256, 0, s>>>(
+        scene_depth, npx, reinterpret_cast<unsigned long long*>(fragments));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "wt_water_raster clear launch");
+    if (n_triangles == 0) return WT_OK;
+    const uint64_t rb = (n_triangles + 255) / 256;
+    k_water_raster<<<(unsigned)(rb < (uint64_t)sms * 8 ? rb : (uint64_t)sms * 8), 256, 0, s>>>(
+        reinterpret_cast<const float4*>(clip), n_vertices, indices, n_triangles, width, height,
+        reinterpret_cast<unsigned long long*>(fragments));
+    e = cudaGetLastError();
+    return e == cudaSuccess ? WT_OK : cuda_fail(e, "wt_water_raster launch");
+}
+
+extern "C" wt_status wt_water_shade(const uint64_t* fragments, const float* clip, uint64_t n_vertices,
+                                    const uint32_t* indices, uint64_t n_triangles, const float* facing, const float* nrm_yaw, const float* view, const float* ndc0,
+                                    uint32_t width, uint32_t height, const wt_water_shading* shading,
+                                    const wt_water_textures* textures, float* colour_out, float* composite,
+                                    wt_stream stream) {
+    if (!viewport_ok(width, height)) return fail(WT_ERR_INVALID_ARG, "wt_water_shade: viewport outside [1, 16384]^2");
+    if (!fragments || !aligned(fragments, 8)) return fail(WT_ERR_INVALID_ARG, "wt_water_shade: fragments NULL or misaligned");
+    const float* v16[4] = {clip, facing, nrm_yaw, view};
+    for (const float* q : v16)
+        if (!q || !aligned(q, 16)) return fail(WT_ERR_INVALID_ARG, "wt_water_shade: vertex array NULL or not 16-byte aligned");
+    if (!ndc0 || !aligned(ndc0, 8)) return fail(WT_ERR_INVALID_ARG, "wt_water_shade: ndc0 NULL or misaligned");
+    if (!indices || !aligned(indices, 4)) return fail(WT_ERR_INVALID_ARG, "wt_water_shade: indices NULL or misaligned");
+    if (!shading || !textures) return fail(WT_ERR_INVALID_ARG, "wt_water_shade: shading or textures NULL");
+    if (!textures->skybox || textures->skybox_size == 0 || textures->skybox_size > 16384 || !aligned(textures->skybox, 4))
+        return fail(WT_ERR_INVALID_ARG, "wt_water_shade: a sky box (6 RGBA8 faces, 4-byte aligned) is required");
+    if ((textures->local_reflections && !aligned(textures->local_reflections, 4)) ||
+        (textures->local_refractions && !aligned(textures->local_refractions, 4)) ||
+        (textures->scene_depth && !aligned(textures->scene_depth, 4)))
+        return fail(WT_ERR_INVALID_ARG, "wt_water_shade: texture misaligned");
+    const float* vals = &shading->sun_position[0];
+    for (size_t i = 0; i < sizeof(wt_water_shading) / sizeof(float); ++i)
+        if (!std::isfinite(vals[i])) return fail(WT_ERR_INVALID_ARG, "wt_water_shade: non-finite shading parameter");
+    if (!(shading->z_near > 0.0f && shading->z_far > shading->z_near))
+        return fail(WT_ERR_INVALID_ARG, "wt_water_shade: need 0 < z_near < z_far");
+    if (!colour_out && !composite) return WT_OK;
+    if ((colour_out && !aligned(colour_out, 16)) || (composite && !aligned(composite, 16)))
+        return fail(WT_ERR_INVALID_ARG, "wt_water_shade: colour outputs must be 16-byte aligned");
+    int sms = 0;
+    wt_status st = sms_of_device(&sms);
+    if (st != WT_OK) return st;
+    const uint64_t npx = (uint64_t)width * height;
+    const uint64_t b = (npx + 255) / 256;
+    const ShadeTex tx{textures->scene_depth, textures->local_reflections, textures->local_refractions,
+                      textures->skybox, textures->skybox_size};
+    k_water_shade<<<(unsigned)(b < (uint64_t)sms * 8 ? b : (uint64_t)sms * 8), 256, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const unsigned long long*>(fragments), reinterpret_cast<const float4*>(clip), n_vertices,
+        indices, n_triangles,
+        reinterpret_cast<const float4*>(facing), reinterpret_cast<const float4*>(nrm_yaw),
+        reinterpret_cast<const float4*>(view), reinterpret_cast<const float2*>(ndc0), width, height, *shading, tx,
+        reinterpret_cast<float4*>(colour_out), reinterpret_cast<float4*>(composite));
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? WT_OK : cuda_fail(e, "wt_water_shade launch");
+}
