@@ -222,11 +222,12 @@ def frame_pipeline(wt, workloads, stream, flush):
     lrefr = torch.randint(0, 256, (VH, VW, 4), dtype=torch.uint8, device="cuda", generator=gen)
     idx = wt.grid_indices(int(patch["cols"][0]), int(patch["rows"][0]))
     frags = torch.empty((VH, VW), dtype=torch.int64, device="cuda")
+    rws = wt.empty_bytes(wt.water_raster_workspace_bytes(n))
     colour = torch.empty((VH, VW, 4), dtype=torch.float32, device="cuda")
     shading = wt.water_shading(sun_position=(0.6, 0.8, 0.0))
 
     def raster():
-        wt.water_raster(outs["clip"], idx, VW, VH, fragments=frags)
+        wt.water_raster(outs["clip"], idx, VW, VH, fragments=frags, workspace=rws)
 
     def shade():
         wt.water_shade(frags, outs["clip"], idx, outs, VW, VH, shading, sky, local_reflections=lrefl,
@@ -236,7 +237,7 @@ def frame_pipeline(wt, workloads, stream, flush):
         wt.projected_grid_async(cam_dev, surf.patches, view_dev, stream=s)
         surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD, stream=s)
         wt.vertex_stage(view_dev, pos, nrm, out=outs, stream=s)
-        wt.water_raster(outs["clip"], idx, VW, VH, fragments=frags, stream=s)
+        wt.water_raster(outs["clip"], idx, VW, VH, fragments=frags, workspace=rws, stream=s)
         wt.water_shade(frags, outs["clip"], idx, outs, VW, VH, shading, sky, local_reflections=lrefl,
                        local_refractions=lrefr, colour=colour, stream=s)
 
@@ -320,8 +321,10 @@ def side_measurements(wt, workloads, surf, pos, nrm, flags, flush, stream, ms_st
         del s5, p5, n5
     out["precision_2048sq_128waves"] = prec
     out["frame_1024sq_32waves_noise"] = frame_pipeline(wt, workloads, stream, flush)
-    # the Adam fit: 500 steps of forward + adjoint on 512^2 x 16 waves
+    # the Adam fit: 500 steps of forward + adjoint on 512^2 x 16 waves (after
+    # a 50-step warm-up fit: the first use of the optimiser's kernels is slow)
     target, start = workloads.config4()
+    fit.fit_waves(target.patches, target.waves, start, steps=50, lr=1e-2)
     r = fit.fit_waves(target.patches, target.waves, start, steps=500, lr=1e-2)
     out["adam_fit_512sq_16waves_500steps"] = {"ms_per_step": r["ms_per_step"], "loss_first": r["loss_first"],
                                               "loss_last": r["loss_last"],
@@ -395,12 +398,16 @@ def run_ours(args):
     terms = w.n_terms
     value = terms * world / (ms_step * 1e-3)
 
-    # end to end through the C ABI from pinned host buffers
+    # end to end through the C ABI from pinned host buffers, outputs in the
+    # layout the reference's vertex array consumes (world positions and normals
+    # as tightly packed vec3, render-engine.cpp:1175-1191)
+    e2e_flags = wt.WT_OUT_WORLD | wt.WT_LAYOUT_VEC3
+    epos, enrm = surf.alloc_outputs(e2e_flags)
     hp = torch.from_numpy(np.ascontiguousarray(w.patches).view(np.uint8).reshape(-1)).pin_memory()
     hw = torch.from_numpy(np.ascontiguousarray(w.waves).view(np.uint8).reshape(-1)).pin_memory()
     htex = hm.texels.cpu().pin_memory()
-    hpos = torch.empty(pos.shape, dtype=pos.dtype, pin_memory=True)
-    hnrm = torch.empty(nrm.shape, dtype=nrm.dtype, pin_memory=True)
+    hpos = torch.empty(epos.shape, dtype=epos.dtype, pin_memory=True)
+    hnrm = torch.empty(enrm.shape, dtype=enrm.dtype, pin_memory=True)
     h2d = hp.numel() + hw.numel() + htex.numel() * 4
     d2h = hpos.numel() * 4 + hnrm.numel() * 4
 
@@ -408,9 +415,9 @@ def run_ours(args):
         surf.patches.copy_(hp, non_blocking=True)
         surf.waves.copy_(hw, non_blocking=True)
         hm.texels.copy_(htex, non_blocking=True)
-        surf.displace(pos, nrm, flags=flags)
-        hpos.copy_(pos, non_blocking=True)
-        hnrm.copy_(nrm, non_blocking=True)
+        surf.displace(epos, enrm, flags=e2e_flags)
+        hpos.copy_(epos, non_blocking=True)
+        hnrm.copy_(enrm, non_blocking=True)
 
     e2e_steps = max(3, min(args.steps, 10))
     for _ in range(2):
@@ -483,7 +490,8 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (SplitMix64 seed 2 + rank)",
             "config": {"workload": w.name, "patches": args.patches, "vertices": verts, "terms_per_step": terms,
                        "waves_per_patch": "8..64", "grid_side": "64..1024 log-uniform", "heightmap": "512^2 noise",
-                       "outputs": "float4 displacement + float4 normal", "phase": "FP64-reduced",
+                       "outputs": "float4 displacement + float4 normal (e2e: packed vec3 world position + "
+                                  "normal, the reference's vertex-array layout)", "phase": "FP64-reduced",
                        "l2": "256 MiB buffer zeroed between timed steps (outside the per-step events)",
                        "parallelism": f"weak x{world} (each GPU its own 256 patches)",
                        "tuning": tuning},

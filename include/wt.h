@@ -381,10 +381,15 @@ typedef struct wt_water_textures {
  * near plane or far outside the viewport are clipped in clip space first.
  * Ties in depth go to the lower triangle index (the first one drawn, as
  * GL_LESS keeps it).  Independent of launch order: bitwise reproducible.
- * Needs no workspace; fragments: device, width*height uint64. */
+ * fragments: device, width*height uint64; workspace: device, 16-byte aligned,
+ * wt_water_raster_workspace_size bytes. */
 wt_status wt_water_raster(const float* clip, uint64_t n_vertices, const uint32_t* indices, uint64_t n_triangles,
                           uint32_t width, uint32_t height, const float* scene_depth, uint64_t* fragments,
-                          wt_stream stream);
+                          void* workspace, size_t workspace_bytes, wt_stream stream);
+
+/* Workspace of wt_water_raster: 16 bytes per vertex (each vertex's snapped
+ * window coordinates, computed once for the triangles that share it). */
+wt_status wt_water_raster_workspace_size(uint64_t n_vertices, size_t* bytes);
 
 /* Shades every water pixel of a visibility buffer with the arithmetic of
  * water-grid.frag:65-151: perspective-correct varyings (facing normal, yaw-only

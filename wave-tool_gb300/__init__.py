@@ -34,7 +34,7 @@ EXPORTED = [
     "wt_gerstner_adjoint", "wt_grid_indices", "wt_noise_synth", "wt_wave_from_reference",
     "wt_measure_peaks", "wt_set_tuning", "wt_get_tuning", "wt_autotune_displace",
     "wt_projected_grid", "wt_projected_grid_async", "wt_vertex_stage", "wt_heightmap_from_unorm8",
-    "wt_water_raster", "wt_water_shade",
+    "wt_water_raster", "wt_water_raster_workspace_size", "wt_water_shade",
 ]
 
 
@@ -118,7 +118,8 @@ def lib():
         L.wt_projected_grid_async.argtypes = [vp, vp, vp, vp]
         L.wt_vertex_stage.argtypes = [vp, vp, vp, u64, u32, vp, vp, vp, vp, vp, vp]
         L.wt_heightmap_from_unorm8.argtypes = [vp, u32, u32, u32, u64, u32, vp, vp]
-        L.wt_water_raster.argtypes = [vp, u64, vp, u64, u32, u32, vp, vp, vp]
+        L.wt_water_raster.argtypes = [vp, u64, vp, u64, u32, u32, vp, vp, vp, sz, vp]
+        L.wt_water_raster_workspace_size.argtypes = [u64, C.POINTER(sz)]
         L.wt_water_shade.argtypes = [vp, vp, u64, vp, u64, vp, vp, vp, vp, u32, u32, C.POINTER(CWaterShading),
                                      C.POINTER(CWaterTextures), vp, vp, vp]
         for name in EXPORTED:
@@ -407,14 +408,24 @@ def water_shading(**kw) -> CWaterShading:
     return s
 
 
-def water_raster(clip, indices, width: int, height: int, scene_depth=None, fragments=None, stream=None):
+def water_raster_workspace_bytes(n_vertices: int) -> int:
+    out = C.c_size_t()
+    check(lib().wt_water_raster_workspace_size(n_vertices, C.byref(out)))
+    return out.value
+
+
+def water_raster(clip, indices, width: int, height: int, scene_depth=None, fragments=None, workspace=None,
+                 stream=None):
     """Visibility buffer (int64 tensor of height x width keys) of the
     triangles `indices` over float4 clip positions."""
     torch = _torch()
     if fragments is None:
         fragments = torch.empty((height, width), dtype=torch.int64, device=clip.device)
+    if workspace is None:
+        workspace = empty_bytes(water_raster_workspace_bytes(clip.shape[0]), clip.device)
     check(lib().wt_water_raster(clip.data_ptr(), clip.shape[0], indices.data_ptr(), indices.numel() // 3, width,
-                                height, _ptr(scene_depth), fragments.data_ptr(), stream_handle(stream)))
+                                height, _ptr(scene_depth), fragments.data_ptr(), workspace.data_ptr(),
+                                workspace.numel(), stream_handle(stream)))
     return fragments
 
 
@@ -458,6 +469,6 @@ __all__ = [
     "NOISE_TERM_DTYPE", "WAVE_GRAD_DTYPE", "WT_OUT_WORLD", "WT_OUT_DISPLACEMENT", "WT_LAYOUT_FLOAT4",
     "WT_LAYOUT_VEC3", "WT_PHASE_FP64", "WT_PHASE_FP32_NAIVE", "WT_WRAP_REPEAT", "WT_WRAP_MIRRORED_REPEAT",
     "EXPORTED", "math", "CAMERA_DTYPE", "VIEW_DTYPE", "camera", "displaceable_amplitude", "projected_grid",
-    "projected_grid_async", "vertex_stage", "water_shading", "water_raster", "water_shade",
+    "projected_grid_async", "vertex_stage", "water_shading", "water_raster", "water_raster_workspace_bytes", "water_shade",
     "WATER_SHADING_DEFAULTS",
 ]

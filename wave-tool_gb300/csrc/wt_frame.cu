@@ -1,11 +1,12 @@
 // wt_frame.cu — per-frame set-up of the projected grid, and the vertex-stage
 // outputs that follow the displacement.
 //
-// projected_grid() restates src/render-engine.cpp:797-1042 in FP64.  It is
-// one __host__ __device__ function: wt_projected_grid runs it on the host,
-// wt_projected_grid_async in a single-thread kernel that reads the camera
-// from device memory, so that camera -> corners -> displaced vertices is one
-// stream of kernels a CUDA graph can replay with a new camera every frame.
+// The projected grid restates src/render-engine.cpp:797-1042 in FP64 as a
+// set of __host__ __device__ steps: wt_projected_grid runs them one after
+// another on the host, wt_projected_grid_async spreads them over one warp of
+// a kernel that reads the camera from device memory, so that camera ->
+// corners -> displaced vertices is one stream of kernels a CUDA graph can
+// replay with a new camera every frame.
 //
 // k_vertex_stage computes the rest of water-grid.vert's outputs
 // (:150-158, :190-193) from the displaced positions and exact normals: a
@@ -23,7 +24,6 @@ namespace {
 #define WT_HD __host__ __device__ inline
 
 constexpr double kPi = 3.14159265358979323846;
-constexpr double kDeg = kPi / 180.0;
 
 // Constants of the reference's projected grid (src/render-engine.cpp).
 constexpr double kFrustumPad = 1.2;          // SAFETY_PADDING_SCALAR, :826
@@ -72,9 +72,19 @@ struct Basis {
     D3 pos, fwd, right, up;
 };
 
-WT_HD Basis camera_basis(D3 pos, double cy, double sy, double pitch_deg) {
-    double sp, cp;
-    sincos(fmin(fmax(pitch_deg, -kPitchLimit), kPitchLimit) * kDeg, &sp, &cp);
+// sin and cos of pi * x (exact argument reduction on the device).
+WT_HD void sincos_pi(double x, double* s, double* c) {
+#ifdef __CUDA_ARCH__
+    sincospi(x, s, c);
+#else
+    sincos(x * kPi, s, c);
+#endif
+}
+
+// cos(89 degrees), the smallest cosine of a clamped pitch
+WT_HD double cos89() { return 0.017452406437283512819; }
+
+WT_HD Basis camera_basis(D3 pos, double cy, double sy, double sp, double cp) {
     Basis b;
     b.pos = pos;
     b.fwd = unit(D3{cy * cp, sp, sy * cp});
@@ -123,108 +133,150 @@ struct Grid {
     bool visible;
 };
 
-// src/render-engine.cpp:797-1042.  The view-projection inverses the
-// reference forms with glm::inverse are used in closed form: NDC (X, Y) at
-// view depth d is pos + d * (X*tx*right + Y*ty*up + fwd), tx = tan(fov/2) *
-// aspect, ty = tan(fov/2).  The slab points only enter through their x and z
-// (they are flattened onto y = 0 before projection, :989-991) and only
-// through the bounds of their projector NDC, so they are bounded as they are
-// found; the projector does not depend on them.
-WT_HD void projected_grid(const wt_camera& c, Grid* g) {
-    const double amp = c.displaceable_amplitude;
-    const D3 eye{c.position[0], c.position[1], c.position[2]};
-    const double yaw = (c.yaw_deg - 360.0 * floor(c.yaw_deg / 360.0)) * kDeg;
-    double sy, cy;
-    sincos(yaw, &sy, &cy);
-    const Basis cam = camera_basis(eye, cy, sy, c.pitch_deg);
-    const double ty = tan(0.5 * c.fov_deg * kDeg), tx = ty * c.aspect;
-    const M4 proj = perspective(ty, c.aspect, c.z_near, c.z_far);
-    g->view_projection = mul(proj, view_matrix(cam));
-    g->view_only_yaw = view_matrix(Basis{eye, D3{cy, 0.0, sy}, D3{-sy, 0.0, cy}, D3{0.0, 1.0, 0.0}});
-    g->visible = false;
+// What the per-item steps of the projected grid need: the camera and
+// projector bases and the frustum's tangents.
+struct Frame {
+    double amp, tx, ty, itx, ity, z_near, z_far;
+    Basis cam, pj;
+};
 
+// src/render-engine.cpp:897-984 from the sines and cosines of the yaw, the
+// clamped pitch and half the field of view.  NDC (X, Y) at view depth d is
+// pos + d * (X*tx*right + Y*ty*up + fwd), tx = tan(fov/2) * aspect,
+// ty = tan(fov/2): the view-projection inverses the reference forms with
+// glm::inverse are used in this closed form.
+WT_HD void frame_setup(const wt_camera& c, double sy, double cy, double sp, double cp, double sf, double cf,
+                       Frame* f) {
+    f->amp = c.displaceable_amplitude;
+    f->z_near = c.z_near;
+    f->z_far = c.z_far;
+    const D3 eye{c.position[0], c.position[1], c.position[2]};
+    f->cam = camera_basis(eye, cy, sy, sp, cp);
+    f->ty = sf / cf;
+    f->tx = f->ty * c.aspect;
+    f->itx = 1.0 / f->tx;
+    f->ity = 1.0 / f->ty;
     // the projector: the camera raised out of the slab and pitched down at
-    // an aim point blended between the bird's-eye and horizon aims (:897-984)
+    // an aim point blended between the bird's-eye and horizon aims
     const bool underwater = eye.y < 0.0;
-    const double min_height = amp + kProjectorElevation;
+    const double min_height = f->amp + kProjectorElevation;
     D3 ppos = eye;
     if (eye.y < min_height) ppos.y = underwater ? min_height - eye.y : min_height;
-    D3 fs = cam.fwd;
+    D3 fs = f->cam.fwd;
     if (fabs(fs.y) < kHorizonEpsilon) fs.y = (fs.y >= 0.0) ? kHorizonEpsilon : -kHorizonEpsilon;
     const bool looking_down = fs.y < 0.0;
     const D3 ray = (looking_down != underwater) ? fs : D3{fs.x, -fs.y, fs.z};
     const D3 aim1 = eye + (-eye.y / ray.y) * ray;
-    D3 aim2 = eye + cam.fwd;
+    D3 aim2 = eye + f->cam.fwd;
     aim2.y = 0.0;
     const double a = fabs(fs.y);
     const D3 aim = (1.0 - a) * aim2 + a * aim1;
-    const D3 d = unit(aim - ppos);
-    // angle below the horizon of the unit aim direction; the reference's
-    // acos(d . normalize(d.x, 0, d.z)) is the same angle
-    const double pitch = -atan2(fabs(d.y), sqrt(d.x * d.x + d.z * d.z)) / kDeg;
-    const Basis pj = camera_basis(ppos, cy, sy, pitch);
+    const D3 d = aim - ppos;
+    // pitched down by the angle of d below the horizon (the reference's
+    // -acos(normalize(d) . normalize(d.x, 0, d.z))), clamped at 89 degrees:
+    // its sine and cosine come straight from d
+    const double hz = sqrt(d.x * d.x + d.z * d.z), r = sqrt(hz * hz + d.y * d.y);
+    double psp = -fabs(d.y) / r, pcp = hz / r;
+    if (!(pcp >= cos89())) sincos_pi(-kPitchLimit / 180.0, &psp, &pcp);
+    f->pj = camera_basis(ppos, cy, sy, psp, pcp);
+}
 
-    // frustum corners, NDC x and y widened (:815-838); bit 2 = right,
-    // bit 1 = top, bit 0 = far
-    D3 fc[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        const double depth = (i & 1) ? c.z_far : c.z_near;
-        const double X = ((i & 4) ? kFrustumPad : -kFrustumPad) * tx * depth;
-        const double Y = ((i & 2) ? kFrustumPad : -kFrustumPad) * ty * depth;
-        fc[i] = eye + X * cam.right + Y * cam.up + depth * cam.fwd;
+// Frustum corner i with NDC x and y widened (:815-838); bit 2 = right,
+// bit 1 = top, bit 0 = far.
+WT_HD D3 frustum_corner(const Frame& f, int i) {
+    const double depth = (i & 1) ? f.z_far : f.z_near;
+    const double X = ((i & 4) ? kFrustumPad : -kFrustumPad) * f.tx * depth;
+    const double Y = ((i & 2) ? kFrustumPad : -kFrustumPad) * f.ty * depth;
+    return f.cam.pos + X * f.cam.right + Y * f.cam.up + depth * f.cam.fwd;
+}
+
+// The 12 frustum edges (corner pairs differing in one bit).
+WT_HD int edge_end(int e, int which) {
+    const int a = e < 3 ? 0 : e < 5 ? 1 : e < 7 ? 2 : e < 8 ? 3 : e < 10 ? 4 : e < 11 ? 5 : 6;
+    const int bit[12] = {1, 2, 4, 2, 4, 1, 4, 4, 1, 2, 2, 1};
+    return which ? (a | bit[e]) : a;
+}
+
+// Where edge (e0, e1) crosses the planes y = +-amp (:857-883): 0 to 2 points.
+WT_HD int edge_points(const Frame& f, D3 e0, D3 e1, double px[2], double pz[2]) {
+    if (e0.y == e1.y) return 0;  // parallel to the planes: no single crossing
+    const double lo = fmin(e0.y, e1.y), hi = fmax(e0.y, e1.y);
+    int n = 0;
+    for (int sgn = 0; sgn < 2; ++sgn) {
+        const double h = sgn ? -f.amp : f.amp;
+        if (lo <= h && h <= hi) {
+            const double t = (h - e0.y) / (e1.y - e0.y);
+            px[n] = e0.x + t * (e1.x - e0.x);
+            pz[n] = e0.z + t * (e1.z - e0.z);
+            ++n;
+        }
     }
+    return n;
+}
 
-    // points of the frustum inside the slab |y| <= amp (the 12 edges cut by
-    // the planes y = +-amp, then the corners, :857-893), flattened and
-    // bounded in the projector's NDC (:993-1005)
+// NDC of the base-plane point (px, 0, pz) in the projector (:993-1005).
+WT_HD void projector_ndc(const Frame& f, double px, double pz, double* X, double* Y) {
+    const D3 q = D3{px, 0.0, pz} - f.pj.pos;
+    const double iw = 1.0 / dot(f.pj.fwd, q);
+    *X = dot(f.pj.right, q) * f.itx * iw;
+    *Y = dot(f.pj.up, q) * f.ity * iw;
+}
+
+// The projector's ray through NDC (X, Y) cast onto y = 0 (:1007-1036).
+WT_HD bool corner_ray(const Frame& f, double X, double Y, double* cx, double* cz) {
+    const D3 dir = (X * f.tx) * f.pj.right + (Y * f.ty) * f.pj.up + f.pj.fwd;
+    if (dir.y == 0.0) return false;
+    const double t = -f.pj.pos.y / dir.y;
+    *cx = f.pj.pos.x + t * dir.x;
+    *cz = f.pj.pos.z + t * dir.z;
+    return isfinite(*cx) && isfinite(*cz);
+}
+
+WT_HD void view_matrices(const wt_camera& c, const Frame& f, double sy, double cy, M4* vp, M4* yaw) {
+    *vp = mul(perspective(f.ty, c.aspect, c.z_near, c.z_far), view_matrix(f.cam));
+    *yaw = view_matrix(Basis{f.cam.pos, D3{cy, 0.0, sy}, D3{-sy, 0.0, cy}, D3{0.0, 1.0, 0.0}});
+}
+
+WT_HD void camera_trig(const wt_camera& c, int which, double* s, double* co) {
+    if (which == 0) sincos_pi((c.yaw_deg - 360.0 * floor(c.yaw_deg / 360.0)) / 180.0, s, co);
+    else if (which == 1) sincos_pi(fmin(fmax(c.pitch_deg, -kPitchLimit), kPitchLimit) / 180.0, s, co);
+    else sincos_pi(c.fov_deg / 360.0, s, co);
+}
+
+// src/render-engine.cpp:797-1042, one step after another (host).  The slab
+// points only enter through their x and z (they are flattened onto y = 0
+// before projection, :989-991) and only through the bounds of their
+// projector NDC, so they are bounded as they are found.
+inline void projected_grid(const wt_camera& c, Grid* g) {
+    double t[6];
+    for (int k = 0; k < 3; ++k) camera_trig(c, k, &t[2 * k], &t[2 * k + 1]);
+    Frame f;
+    frame_setup(c, t[0], t[1], t[2], t[3], t[4], t[5], &f);
+    view_matrices(c, f, t[0], t[1], &g->view_projection, &g->view_only_yaw);
+    g->visible = false;
+    D3 fc[8];
+    for (int i = 0; i < 8; ++i) fc[i] = frustum_corner(f, i);
     double x0 = 0.0, x1 = 0.0, y0 = 0.0, y1 = 0.0;
     bool any = false;
     auto add = [&](double px, double pz) {
-        const D3 q = D3{px, 0.0, pz} - ppos;
-        const double w = dot(pj.fwd, q);
-        const double X = dot(pj.right, q) / (tx * w), Y = dot(pj.up, q) / (ty * w);
+        double X, Y;
+        projector_ndc(f, px, pz, &X, &Y);
         x0 = any ? fmin(x0, X) : X;
         x1 = any ? fmax(x1, X) : X;
         y0 = any ? fmin(y0, Y) : Y;
         y1 = any ? fmax(y1, Y) : Y;
         any = true;
     };
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-        for (int bit = 1; bit < 8; bit <<= 1) {
-            if (i & bit) continue;
-            const D3 e0 = fc[i], e1 = fc[i | bit];
-            if (e0.y == e1.y) continue;  // parallel to the planes: no single crossing
-            const double lo = fmin(e0.y, e1.y), hi = fmax(e0.y, e1.y);
-#pragma unroll
-            for (int sgn = 0; sgn < 2; ++sgn) {
-                const double h = sgn ? -amp : amp;
-                if (lo <= h && h <= hi) {
-                    const double t = (h - e0.y) / (e1.y - e0.y);
-                    add(e0.x + t * (e1.x - e0.x), e0.z + t * (e1.z - e0.z));
-                }
-            }
-        }
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-        if (-amp <= fc[i].y && fc[i].y <= amp) add(fc[i].x, fc[i].z);
-    if (!any) return;
-
-    // cast the rays through the corners of that NDC range onto y = 0
-    // (:1007-1036): ray (X, Y) from the projector along X*tx*right + Y*ty*up + fwd
-    const double uv[4][2] = {{0.0, 0.0}, {1.0, 0.0}, {0.0, 1.0}, {1.0, 1.0}};
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const double X = x0 + uv[k][0] * (x1 - x0), Y = y0 + uv[k][1] * (y1 - y0);
-        const D3 dir = (X * tx) * pj.right + (Y * ty) * pj.up + pj.fwd;
-        if (dir.y == 0.0) return;
-        const double t = -ppos.y / dir.y;
-        g->corner[k][0] = ppos.x + t * dir.x;
-        g->corner[k][1] = ppos.z + t * dir.z;
-        if (!isfinite(g->corner[k][0]) || !isfinite(g->corner[k][1])) return;
+    for (int e = 0; e < 12; ++e) {
+        double px[2], pz[2];
+        const int n = edge_points(f, fc[edge_end(e, 0)], fc[edge_end(e, 1)], px, pz);
+        for (int k = 0; k < n; ++k) add(px[k], pz[k]);
     }
+    for (int i = 0; i < 8; ++i)
+        if (-f.amp <= fc[i].y && fc[i].y <= f.amp) add(fc[i].x, fc[i].z);
+    if (!any) return;
+    for (int k = 0; k < 4; ++k)
+        if (!corner_ray(f, (k & 1) ? x1 : x0, (k & 2) ? y1 : y0, &g->corner[k][0], &g->corner[k][1])) return;
     g->visible = true;
 }
 
@@ -247,15 +299,77 @@ WT_HD void store_result(const wt_camera& c, const Grid& g, wt_patch* patch, wt_v
     }
 }
 
-__global__ void k_projected_grid(const wt_camera* __restrict__ camera, wt_patch* patch, wt_view* view) {
+__device__ __forceinline__ D3 shfl_d3(D3 v, int src) {
+    return D3{__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
+              __shfl_sync(0xffffffffu, v.z, src)};
+}
+
+// The same steps spread over one warp: three lanes take the trigonometry,
+// eight the frustum corners, twelve the edges and eight the corners inside
+// the slab, the NDC bounds are reduced across lanes, four lanes cast the grid
+// corners and sixteen write the matrices.  A single thread on GB300's FP64
+// pipe spends most of its time in dependent-instruction latency.
+__global__ void __launch_bounds__(32) k_projected_grid(const wt_camera* __restrict__ camera, wt_patch* patch,
+                                                       wt_view* view) {
+    const int lane = threadIdx.x;
     const wt_camera c = *camera;
     if (!camera_ok(c)) {
-        view->status = WT_VIEW_INVALID_CAMERA;
+        if (lane == 0) view->status = WT_VIEW_INVALID_CAMERA;
         return;
     }
-    Grid g;
-    projected_grid(c, &g);
-    store_result(c, g, patch, view);
+    double ts = 0.0, tc = 1.0;
+    if (lane < 3) camera_trig(c, lane, &ts, &tc);
+    const double sy = __shfl_sync(0xffffffffu, ts, 0), cy = __shfl_sync(0xffffffffu, tc, 0);
+    const double sp = __shfl_sync(0xffffffffu, ts, 1), cp = __shfl_sync(0xffffffffu, tc, 1);
+    const double sf = __shfl_sync(0xffffffffu, ts, 2), cf = __shfl_sync(0xffffffffu, tc, 2);
+    Frame f;
+    frame_setup(c, sy, cy, sp, cp, sf, cf, &f);
+
+    const D3 mine = frustum_corner(f, lane & 7);
+    const int e = lane < 12 ? lane : 0;
+    const D3 ea = shfl_d3(mine, edge_end(e, 0)), eb = shfl_d3(mine, edge_end(e, 1));
+    const D3 corner = shfl_d3(mine, (lane >= 12 && lane < 20) ? lane - 12 : 0);
+    double px[2], pz[2];
+    int n = 0;
+    if (lane < 12) {
+        n = edge_points(f, ea, eb, px, pz);
+    } else if (lane < 20 && -f.amp <= corner.y && corner.y <= f.amp) {
+        px[0] = corner.x;
+        pz[0] = corner.z;
+        n = 1;
+    }
+    double x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+    for (int k = 0; k < n; ++k) {
+        double X, Y;
+        projector_ndc(f, px[k], pz[k], &X, &Y);
+        x0 = fmin(x0, X);
+        x1 = fmax(x1, X);
+        y0 = fmin(y0, Y);
+        y1 = fmax(y1, Y);
+    }
+    const bool any = __ballot_sync(0xffffffffu, n > 0) != 0;
+    for (int o = 16; o > 0; o >>= 1) {
+        x0 = fmin(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+        x1 = fmax(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+        y0 = fmin(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+        y1 = fmax(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+    }
+    double gx = 0.0, gz = 0.0;
+    const bool ok = lane < 4 && any && corner_ray(f, (lane & 1) ? x1 : x0, (lane & 2) ? y1 : y0, &gx, &gz);
+    const bool visible = (__ballot_sync(0xffffffffu, ok) & 0xfu) == 0xfu;
+    if (lane < 16) {
+        M4 vp, yaw;
+        view_matrices(c, f, sy, cy, &vp, &yaw);
+        view->view_projection[lane] = (float)vp.m[lane >> 2][lane & 3];
+        view->view_only_yaw[lane] = (float)yaw.m[lane >> 2][lane & 3];
+    }
+    if (lane < 3) view->camera_position[lane] = (float)c.position[lane];
+    if (lane == 0) view->status = visible ? WT_VIEW_VISIBLE : WT_VIEW_EMPTY;
+    if (visible && lane < 4) {
+        float* dst = lane == 0 ? patch->bl : lane == 1 ? patch->br : lane == 2 ? patch->tl : patch->tr;
+        dst[0] = (float)gx;
+        dst[1] = (float)gz;
+    }
 }
 
 // ---- vertex-stage outputs ---------------------------------------------------
@@ -371,7 +485,7 @@ extern "C" wt_status wt_projected_grid_async(const wt_camera* camera, wt_patch* 
     if (!camera || !aligned(camera, 8)) return fail(WT_ERR_INVALID_ARG, "wt_projected_grid_async: camera NULL or misaligned");
     if (!patch || !aligned(patch, 8)) return fail(WT_ERR_INVALID_ARG, "wt_projected_grid_async: patch NULL or misaligned");
     if (!view || !aligned(view, 4)) return fail(WT_ERR_INVALID_ARG, "wt_projected_grid_async: view NULL or misaligned");
-    k_projected_grid<<<1, 1, 0, (cudaStream_t)stream>>>(camera, patch, view);
+    k_projected_grid<<<1, 32, 0, (cudaStream_t)stream>>>(camera, patch, view);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? WT_OK : cuda_fail(e, "wt_projected_grid_async launch");
 }

@@ -11,7 +11,8 @@
 // functions at pixel centres (left/top fill rule); the window depth is
 // interpolated linearly in screen space and folded with the triangle index
 // into one 64-bit key, (depth bits << 32) | (triangle + 1), kept per pixel by
-// atomicMin: nearest fragment wins, ties go to the lower index, and the
+// a 64-bit atomic minimum (no return value, so no round trip per fragment):
+// nearest fragment wins, ties go to the lower index, and the
 // result does not depend on launch order.  Triangles with more than
 // kSmallPixels pixels in their box, and triangles that reach behind the near
 // plane or past a guard band of 64 viewports (clipped in clip space first),
@@ -33,6 +34,7 @@ namespace {
 constexpr float kSub = 256.0f;   // sub-pixel steps per pixel
 constexpr float kGuard = 64.0f;  // guard band, in NDC units
 constexpr int kSmallPixels = 16;
+constexpr int64_t kSmallExtent = 1 << 13;  // sub-pixel steps (32 pixels)
 constexpr unsigned kFull = 0xffffffffu;
 
 struct CV4 {
@@ -93,20 +95,27 @@ struct Setup {
     float z[3];
     float area_f;
     int32_t px0, px1, py0, py1;
-    int incl;  // bit k: edge k (vertex k+1 -> k+2) owns pixel centres exactly on it
+    int incl;   // bit k: edge k (vertex k+1 -> k+2) owns pixel centres exactly on it
+    bool small; // extent below kSmallExtent in x and y (exact 32-bit edge functions)
 };
 
 __device__ __forceinline__ bool setup_tri(const WinTri& w, uint32_t W, uint32_t H, Setup& s) {
-    int64_t area = (int64_t)(w.X[1] - w.X[0]) * (w.Y[2] - w.Y[0]) - (int64_t)(w.Y[1] - w.Y[0]) * (w.X[2] - w.X[0]);
+    const int32_t xmn = min(w.X[0], min(w.X[1], w.X[2])), xmx = max(w.X[0], max(w.X[1], w.X[2]));
+    const int32_t ymn = min(w.Y[0], min(w.Y[1], w.Y[2])), ymx = max(w.Y[0], max(w.Y[1], w.Y[2]));
+    const bool small = (int64_t)xmx - xmn < kSmallExtent && (int64_t)ymx - ymn < kSmallExtent;
+    int64_t area;
+    if (small)  // |products| < 2^26: exact in 32 bits
+        area = (w.X[1] - w.X[0]) * (w.Y[2] - w.Y[0]) - (w.Y[1] - w.Y[0]) * (w.X[2] - w.X[0]);
+    else
+        area = (int64_t)(w.X[1] - w.X[0]) * (w.Y[2] - w.Y[0]) - (int64_t)(w.Y[1] - w.Y[0]) * (w.X[2] - w.X[0]);
     if (area == 0) return false;
     const int a = area > 0 ? 1 : 2, b = area > 0 ? 2 : 1;  // counter-clockwise order
     s.x[0] = w.X[0]; s.y[0] = w.Y[0]; s.z[0] = w.Z[0];
     s.x[1] = w.X[a]; s.y[1] = w.Y[a]; s.z[1] = w.Z[a];
     s.x[2] = w.X[b]; s.y[2] = w.Y[b]; s.z[2] = w.Z[b];
     if (area < 0) area = -area;
-    s.area_f = (float)area;
-    const int32_t xmin = min(s.x[0], min(s.x[1], s.x[2])), xmax = max(s.x[0], max(s.x[1], s.x[2]));
-    const int32_t ymin = min(s.y[0], min(s.y[1], s.y[2])), ymax = max(s.y[0], max(s.y[1], s.y[2]));
+    s.area_f = small ? (float)(int32_t)area : (float)area;
+    const int32_t xmin = xmn, xmax = xmx, ymin = ymn, ymax = ymx;
     int64_t px0 = -((128 - (int64_t)xmin) >> 8), px1 = ((int64_t)xmax - 128) >> 8;
     int64_t py0 = -((128 - (int64_t)ymin) >> 8), py1 = ((int64_t)ymax - 128) >> 8;
     px0 = px0 < 0 ? 0 : px0;
@@ -115,6 +124,7 @@ __device__ __forceinline__ bool setup_tri(const WinTri& w, uint32_t W, uint32_t 
     py1 = py1 > (int64_t)H - 1 ? (int64_t)H - 1 : py1;
     if (px0 > px1 || py0 > py1) return false;
     s.px0 = (int32_t)px0; s.px1 = (int32_t)px1; s.py0 = (int32_t)py0; s.py1 = (int32_t)py1;
+    s.small = small;
     s.incl = 0;
     for (int k = 0; k < 3; ++k) {
         const int i = k == 2 ? 0 : k + 1, j = k == 0 ? 2 : (k == 1 ? 0 : 1);
@@ -138,8 +148,45 @@ __device__ __forceinline__ void raster_pixel(const Setup& s, int32_t px, int32_t
     if (!(d >= 0.0f && d <= 1.0f)) return;
     d = d + 0.0f;  // -0 -> +0
     const unsigned long long key = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned long long)(tri + 1u);
-    unsigned long long* slot = frag + (size_t)py * W + px;
-    if (key < *slot) atomicMin(slot, key);
+    atomicMin(frag + (size_t)py * W + px, key);
+}
+
+// Triangles less than kSmallExtent sub-pixel steps wide and high: the edge
+// functions, taken relative to vertex 0, stay below 2^28 in magnitude, so they
+// are evaluated exactly in 32-bit integers, stepping from pixel to pixel (the
+// same values the 64-bit form gives).
+__device__ __forceinline__ void raster_small(const Setup& s, uint32_t tri, uint32_t W, unsigned long long* frag) {
+    int32_t e0[3], dx[3], dy[3];
+    const int32_t cx0 = s.px0 * 256 + 128 - s.x[0], cy0 = s.py0 * 256 + 128 - s.y[0];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int i = k == 2 ? 0 : k + 1, j = k == 0 ? 2 : (k == 1 ? 0 : 1);
+        const int32_t ex = s.x[j] - s.x[i], ey = s.y[j] - s.y[i];
+        e0[k] = ex * (cy0 - (s.y[i] - s.y[0])) - ey * (cx0 - (s.x[i] - s.x[0]));
+        dx[k] = -ey * 256;
+        dy[k] = ex * 256;
+    }
+    for (int32_t py = s.py0; py <= s.py1; ++py) {
+        int32_t e[3] = {e0[0], e0[1], e0[2]};
+        for (int32_t px = s.px0; px <= s.px1; ++px) {
+            bool in = true;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) in &= e[k] > 0 || (e[k] == 0 && ((s.incl >> k) & 1));
+            if (in) {
+                float d = ((float)e[0] * s.z[0] + (float)e[1] * s.z[1] + (float)e[2] * s.z[2]) / s.area_f;
+                if (d >= 0.0f && d <= 1.0f) {
+                    d = d + 0.0f;  // -0 -> +0
+                    const unsigned long long key =
+                        ((unsigned long long)__float_as_uint(d) << 32) | (unsigned long long)(tri + 1u);
+                    atomicMin(frag + (size_t)py * W + px, key);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) e[k] += dx[k];
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) e0[k] += dy[k];
+    }
 }
 
 __device__ __forceinline__ void raster_own(const Setup& s, uint32_t tri, uint32_t W, unsigned long long* frag) {
@@ -147,13 +194,39 @@ __device__ __forceinline__ void raster_own(const Setup& s, uint32_t tri, uint32_
         for (int32_t px = s.px0; px <= s.px1; ++px) raster_pixel(s, px, py, tri, W, frag);
 }
 
+// raster_pixel for a small-extent triangle: the same edge values in 32 bits.
+__device__ __forceinline__ void raster_pixel32(const Setup& s, int32_t px, int32_t py, uint32_t tri, uint32_t W,
+                                               unsigned long long* frag) {
+    const int32_t cx = px * 256 + 128, cy = py * 256 + 128;
+    int32_t e[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int i = k == 2 ? 0 : k + 1, j = k == 0 ? 2 : (k == 1 ? 0 : 1);
+        e[k] = (s.x[j] - s.x[i]) * (cy - s.y[i]) - (s.y[j] - s.y[i]) * (cx - s.x[i]);
+        if (!(e[k] > 0 || (e[k] == 0 && ((s.incl >> k) & 1)))) return;
+    }
+    float d = ((float)e[0] * s.z[0] + (float)e[1] * s.z[1] + (float)e[2] * s.z[2]) / s.area_f;
+    if (!(d >= 0.0f && d <= 1.0f)) return;
+    d = d + 0.0f;  // -0 -> +0
+    atomicMin(frag + (size_t)py * W + px,
+              ((unsigned long long)__float_as_uint(d) << 32) | (unsigned long long)(tri + 1u));
+}
+
 __device__ __forceinline__ void raster_warp(const Setup& s, uint32_t tri, uint32_t W, unsigned long long* frag,
                                             int lane) {
-    const int64_t bw = (int64_t)s.px1 - s.px0 + 1;
-    const int64_t n = bw * ((int64_t)s.py1 - s.py0 + 1);
-    for (int64_t p = lane; p < n; p += 32) {
-        const int64_t r = p / bw;
-        raster_pixel(s, (int32_t)(s.px0 + (p - r * bw)), (int32_t)(s.py0 + r), tri, W, frag);
+    // box <= 16384^2 pixels: 32-bit indices
+    const uint32_t bw = (uint32_t)(s.px1 - s.px0 + 1);
+    const uint32_t n = bw * (uint32_t)(s.py1 - s.py0 + 1);
+    if (s.small) {
+        for (uint32_t p = (uint32_t)lane; p < n; p += 32) {
+            const uint32_t r = p / bw;
+            raster_pixel32(s, s.px0 + (int32_t)(p - r * bw), s.py0 + (int32_t)r, tri, W, frag);
+        }
+        return;
+    }
+    for (uint32_t p = (uint32_t)lane; p < n; p += 32) {
+        const uint32_t r = p / bw;
+        raster_pixel(s, s.px0 + (int32_t)(p - r * bw), s.py0 + (int32_t)r, tri, W, frag);
     }
 }
 
@@ -168,6 +241,26 @@ __device__ __forceinline__ WinTri shfl_tri(const WinTri& w, int src) {
     return o;
 }
 
+// Per-vertex window coordinates, computed once for the ~6 triangles sharing a
+// vertex: (X, Y, depth bits, 1) for vertices inside the guard band, w = 0
+// otherwise (their triangles take the clipping path).
+__global__ void __launch_bounds__(256) k_water_vertices(const float4* __restrict__ clip, uint64_t n, uint32_t W,
+                                                        uint32_t H, int4* __restrict__ win) {
+    const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float4 c4 = clip[i];
+        const CV4 c{c4.x, c4.y, c4.z, c4.w};
+        int4 o = make_int4(0, 0, 0, 0);
+        if (inside_guard(c)) {
+            float z;
+            to_window(c, hw, hh, o.x, o.y, z);
+            o.z = __float_as_int(z);
+            o.w = 1;
+        }
+        win[i] = o;
+    }
+}
+
 __global__ void __launch_bounds__(256) k_water_clear(const float* __restrict__ scene_depth, uint64_t n,
                                                      unsigned long long* __restrict__ frag) {
     for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n; p += (uint64_t)gridDim.x * blockDim.x) {
@@ -176,38 +269,37 @@ __global__ void __launch_bounds__(256) k_water_clear(const float* __restrict__ s
     }
 }
 
-__global__ void __launch_bounds__(256) k_water_raster(const float4* __restrict__ clip, uint64_t n_vertices,
-                                                      const uint32_t* __restrict__ idx, uint64_t n_tri, uint32_t W,
-                                                      uint32_t H, unsigned long long* frag) {
+__global__ void __launch_bounds__(256, 3) k_water_raster(const float4* __restrict__ clip,
+                                                         const int4* __restrict__ win, uint64_t n_vertices,
+                                                         const uint32_t* __restrict__ idx, uint64_t n_tri,
+                                                         uint32_t W, uint32_t H, unsigned long long* frag) {
     const int lane = threadIdx.x & 31;
     const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); base < n_tri; base += stride) {
         const uint64_t t = base + lane;
         int kind = 0;  // 0 nothing, 2 warp-rasterised window triangle, 3 clip first
-        CV4 v[3];
+        uint32_t vi[3] = {0u, 0u, 0u};
         WinTri w;
         if (t < n_tri) {
-            bool ok = true;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const uint32_t i = idx[3 * t + k];
-                if (i >= n_vertices) {
-                    ok = false;
-                    break;
-                }
-                const float4 c = clip[i];
-                v[k] = CV4{c.x, c.y, c.z, c.w};
-            }
-            if (ok) {
-                if (inside_guard(v[0]) && inside_guard(v[1]) && inside_guard(v[2])) {
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) to_window(v[k], hw, hh, w.X[k], w.Y[k], w.Z[k]);
+            vi[0] = idx[3 * t];
+            vi[1] = idx[3 * t + 1];
+            vi[2] = idx[3 * t + 2];
+            if (vi[0] < n_vertices && vi[1] < n_vertices && vi[2] < n_vertices) {
+                const int4 a = win[vi[0]], b = win[vi[1]], c = win[vi[2]];
+                if (a.w & b.w & c.w) {
+                    w.X[0] = a.x; w.Y[0] = a.y; w.Z[0] = __int_as_float(a.z);
+                    w.X[1] = b.x; w.Y[1] = b.y; w.Z[1] = __int_as_float(b.z);
+                    w.X[2] = c.x; w.Y[2] = c.y; w.Z[2] = __int_as_float(c.z);
                     Setup s;
                     if (setup_tri(w, W, H, s)) {
                         const int64_t npix = ((int64_t)s.px1 - s.px0 + 1) * ((int64_t)s.py1 - s.py0 + 1);
-                        if (npix <= kSmallPixels) raster_own(s, (uint32_t)t, W, frag);
-                        else kind = 2;
+                        if (npix <= kSmallPixels) {
+                            if (s.small) raster_small(s, (uint32_t)t, W, frag);
+                            else raster_own(s, (uint32_t)t, W, frag);
+                        } else {
+                            kind = 2;
+                        }
                     }
                 } else {
                     kind = 3;
@@ -229,10 +321,8 @@ __global__ void __launch_bounds__(256) k_water_raster(const float4* __restrict__
             CV4 poly[8];
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
-                poly[j].x = __shfl_sync(kFull, v[j].x, src);
-                poly[j].y = __shfl_sync(kFull, v[j].y, src);
-                poly[j].z = __shfl_sync(kFull, v[j].z, src);
-                poly[j].w = __shfl_sync(kFull, v[j].w, src);
+                const float4 c = clip[__shfl_sync(kFull, vi[j], src)];
+                poly[j] = CV4{c.x, c.y, c.z, c.w};
             }
             const int n = clip_polygon(poly, 3);
             bool bad = n < 3;
@@ -260,24 +350,30 @@ struct ShadeTex {
     uint32_t sky_size;
 };
 
-__device__ __forceinline__ uint32_t clampi(int64_t i, uint32_t n) {
-    return (uint32_t)(i < 0 ? 0 : (i >= (int64_t)n ? n - 1 : i));
+// Texel index clamped to [0, n): the coordinates come from texture
+// coordinates in [0, 1] (or NaN, which converts to 0), so 32 bits hold them.
+__device__ __forceinline__ uint32_t clampi(int32_t i, uint32_t n) {
+    return (uint32_t)(i < 0 ? 0 : (i >= (int32_t)n ? (int32_t)n - 1 : i));
 }
+
+// UNORM8 -> float (c / 255, correctly rounded), one table per block.
+__shared__ float s_unorm8[256];
 
 // GL_LINEAR, CLAMP_TO_EDGE over RGBA8 texels converted to c / 255.
 __device__ float4 bilinear_rgba8(const uint8_t* px, uint32_t w, uint32_t h, float s, float t) {
     const float u = s * (float)w - 0.5f, v = t * (float)h - 0.5f;
     const float fi = floorf(u), fj = floorf(v);
     const float a = u - fi, b = v - fj;
-    const uint32_t i0 = clampi((int64_t)fi, w), i1 = clampi((int64_t)fi + 1, w);
-    const uint32_t j0 = clampi((int64_t)fj, h), j1 = clampi((int64_t)fj + 1, h);
+    const int32_t ii = (int32_t)fi, jj = (int32_t)fj;
+    const uint32_t i0 = clampi(ii, w), i1 = clampi(ii + 1, w);
+    const uint32_t j0 = clampi(jj, h), j1 = clampi(jj + 1, h);
     const uchar4 q00 = *reinterpret_cast<const uchar4*>(px + 4 * ((size_t)j0 * w + i0));
     const uchar4 q10 = *reinterpret_cast<const uchar4*>(px + 4 * ((size_t)j0 * w + i1));
     const uchar4 q01 = *reinterpret_cast<const uchar4*>(px + 4 * ((size_t)j1 * w + i0));
     const uchar4 q11 = *reinterpret_cast<const uchar4*>(px + 4 * ((size_t)j1 * w + i1));
     auto f = [&](unsigned char c00, unsigned char c10, unsigned char c01, unsigned char c11) {
-        const float t00 = (float)c00 / 255.0f, t10 = (float)c10 / 255.0f;
-        const float t01 = (float)c01 / 255.0f, t11 = (float)c11 / 255.0f;
+        const float t00 = s_unorm8[c00], t10 = s_unorm8[c10];
+        const float t01 = s_unorm8[c01], t11 = s_unorm8[c11];
         return (1.0f - b) * ((1.0f - a) * t00 + a * t10) + b * ((1.0f - a) * t01 + a * t11);
     };
     return make_float4(f(q00.x, q10.x, q01.x, q11.x), f(q00.y, q10.y, q01.y, q11.y), f(q00.z, q10.z, q01.z, q11.z),
@@ -320,6 +416,8 @@ __global__ void __launch_bounds__(256) k_water_shade(const unsigned long long* _
                                                      const float2* __restrict__ ndc0, uint32_t W, uint32_t H,
                                                      wt_water_shading sh, ShadeTex tex, float4* colour_out,
                                                      float4* composite) {
+    for (uint32_t c = threadIdx.x; c < 256; c += blockDim.x) s_unorm8[c] = (float)c / 255.0f;
+    __syncthreads();
     const uint64_t n = (uint64_t)W * H;
     for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n; p += (uint64_t)gridDim.x * blockDim.x) {
         const unsigned long long key = frag[p];
@@ -382,8 +480,8 @@ __global__ void __launch_bounds__(256) k_water_shade(const unsigned long long* _
         const float h0 = (D0[0] + 1.0f) / 2.0f, h1 = (D0[1] + 1.0f) / 2.0f;
         float back_raw = 1.0f;
         if (tex.depth)
-            back_raw = tex.depth[(size_t)clampi((int64_t)floorf(u1 * (float)H), H) * W +
-                                 clampi((int64_t)floorf(u0 * (float)W), W)];
+            back_raw = tex.depth[(size_t)clampi((int32_t)floorf(u1 * (float)H), H) * W +
+                                 clampi((int32_t)floorf(u0 * (float)W), W)];
         const float back = (sh.z_near * back_raw) / (sh.z_far - back_raw * (sh.z_far - sh.z_near));
         const float sky_behind = back > 0.999f ? 0.0f : 1.0f;
         const float here = (sh.z_near * fz) / (sh.z_far - fz * (sh.z_far - sh.z_near));
@@ -476,9 +574,16 @@ bool viewport_ok(uint32_t w, uint32_t h) { return w >= 1 && h >= 1 && w <= 16384
 
 }  // namespace
 
+extern "C" wt_status wt_water_raster_workspace_size(uint64_t n_vertices, size_t* bytes) {
+    if (!bytes) return fail(WT_ERR_INVALID_ARG, "wt_water_raster_workspace_size: bytes is NULL");
+    *bytes = 16 * (size_t)(n_vertices > 0 ? n_vertices : 1);
+    return WT_OK;
+}
+
 extern "C" wt_status wt_water_raster(const float* clip, uint64_t n_vertices, const uint32_t* indices,
                                      uint64_t n_triangles, uint32_t width, uint32_t height, const float* scene_depth,
-                                     uint64_t* fragments, wt_stream stream) {
+                                     uint64_t* fragments, void* workspace, size_t workspace_bytes,
+                                     wt_stream stream) {
     if (!viewport_ok(width, height)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: viewport outside [1, 16384]^2");
     if (!fragments || !aligned(fragments, 8)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: fragments NULL or misaligned");
     if (scene_depth && !aligned(scene_depth, 4)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: scene_depth misaligned");
@@ -486,6 +591,8 @@ extern "C" wt_status wt_water_raster(const float* clip, uint64_t n_vertices, con
         if (!clip || !aligned(clip, 16)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: clip NULL or not 16-byte aligned");
         if (!indices || !aligned(indices, 4)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: indices NULL or misaligned");
         if (n_triangles > (1ull << 32) - 2) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: more than 2^32 - 2 triangles");
+        if (!workspace || !aligned(workspace, 16)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: workspace NULL or not 16-byte aligned");
+        if (workspace_bytes < 16 * (size_t)n_vertices) return fail(WT_ERR_NOMEM, "wt_water_raster: workspace below 16 bytes per vertex");
     }
     int sms = 0;
     wt_status st = sms_of_device(&sms);
@@ -497,11 +604,16 @@ extern "C" wt_status wt_water_raster(const float* clip, uint64_t n_vertices, con
         scene_depth, npx, reinterpret_cast<unsigned long long*>(fragments));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "wt_water_raster clear launch");
-    if (n_triangles == 0) return WT_OK;
+    if (n_triangles == 0 || n_vertices == 0) return WT_OK;
+    const uint64_t vb = (n_vertices + 255) / 256;
+    k_water_vertices<<<(unsigned)(vb < (uint64_t)sms * 8 ? vb : (uint64_t)sms * 8), 256, 0, s>>>(
+        reinterpret_cast<const float4*>(clip), n_vertices, width, height, static_cast<int4*>(workspace));
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "wt_water_raster vertex launch");
     const uint64_t rb = (n_triangles + 255) / 256;
     k_water_raster<<<(unsigned)(rb < (uint64_t)sms * 8 ? rb : (uint64_t)sms * 8), 256, 0, s>>>(
-        reinterpret_cast<const float4*>(clip), n_vertices, indices, n_triangles, width, height,
-        reinterpret_cast<unsigned long long*>(fragments));
+        reinterpret_cast<const float4*>(clip), static_cast<const int4*>(workspace), n_vertices, indices,
+        n_triangles, width, height, reinterpret_cast<unsigned long long*>(fragments));
     e = cudaGetLastError();
     return e == cudaSuccess ? WT_OK : cuda_fail(e, "wt_water_raster launch");
 }
