@@ -47,8 +47,9 @@ def parse_args():
     ap.add_argument("--patches", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
     ap.add_argument("--no-extras", action="store_true", help="skip the unbatched / single-patch side runs")
-    ap.add_argument("--mode", choices=["forward", "adjoint"], default="forward",
-                    help="'adjoint' times only wt_gerstner_adjoint on 64 uneven patches (for profiling)")
+    ap.add_argument("--mode", choices=["forward", "adjoint", "frame"], default="forward",
+                    help="'adjoint' times only wt_gerstner_adjoint on 64 uneven patches, 'frame' only the "
+                         "camera-to-pixels water frame (for profiling)")
     ap.add_argument("--tuning", default="auto",
                     help="'auto' (autotune before timing) or WARPS,CHUNK[,VPL,EPI] to fix the launch shape")
     return ap.parse_args()
@@ -193,14 +194,14 @@ def _event_ms(fn, reps, stream, flush=None):
     return sum(a.elapsed_time(b) for a, b in evs) / reps
 
 
-def frame_pipeline(wt, workloads, stream, flush):
+def build_frame(wt, workloads):
     """One rendered frame of the water grid as the reference's render loop
     does it (render-engine.cpp:797-1135, water-grid.vert, water-grid.frag), on
     a 1024^2 grid with the 32 waves and noise heightmap of the 1024^2 workload:
-    camera -> projected-grid corners (one-thread FP64 kernel) -> displacement
-    + normals -> clip / NDC-at-height-0 / view vector / facing normal /
-    yaw-only normal -> rasterisation at 1920 x 1080 -> water shading, replayed
-    as one CUDA graph.  Also each stage alone, the vertex stage against HBM."""
+    camera -> projected-grid corners (FP64, one warp) -> displacement +
+    normals -> clip / NDC-at-height-0 / view vector / facing normal /
+    yaw-only normal -> rasterisation at 1920 x 1080 -> water shading.
+    Returns the stage callables and sizes."""
     import torch
     w = workloads.config2()
     amp = wt.displaceable_amplitude(w.waves, w.heightmap.disp_scale)
@@ -241,6 +242,18 @@ def frame_pipeline(wt, workloads, stream, flush):
         wt.water_shade(frags, outs["clip"], idx, outs, VW, VH, shading, sky, local_reflections=lrefl,
                        local_refractions=lrefr, colour=colour, stream=s)
 
+    return dict(frame=frame, raster=raster, shade=shade, n=n, waves=len(w.waves), VW=VW, VH=VH, frags=frags,
+                projected_grid=lambda: wt.projected_grid_async(cam_dev, surf.patches, view_dev),
+                displace=lambda: surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD),
+                vertex_stage=lambda: wt.vertex_stage(view_dev, pos, nrm, out=outs))
+
+
+def frame_pipeline(wt, workloads, stream, flush):
+    """The frame of build_frame replayed as one CUDA graph, and each stage
+    alone (the vertex stage against HBM)."""
+    import torch
+    F = build_frame(wt, workloads)
+    frame, raster, shade, n, VW, VH, frags = (F[k] for k in ("frame", "raster", "shade", "n", "VW", "VH", "frags"))
     for _ in range(3):
         frame()
     torch.cuda.synchronize()
@@ -253,9 +266,9 @@ def frame_pipeline(wt, workloads, stream, flush):
         g.replay()
     torch.cuda.synchronize()
     fms = _event_ms(g.replay, 20, stream, flush)
-    gms = _event_ms(lambda: wt.projected_grid_async(cam_dev, surf.patches, view_dev), 20, stream, flush)
-    dms = _event_ms(lambda: surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD), 20, stream, flush)
-    vms = _event_ms(lambda: wt.vertex_stage(view_dev, pos, nrm, out=outs), 20, stream, flush)
+    gms = _event_ms(F["projected_grid"], 20, stream, flush)
+    dms = _event_ms(F["displace"], 20, stream, flush)
+    vms = _event_ms(F["vertex_stage"], 20, stream, flush)
     rms = _event_ms(raster, 20, stream, flush)
     sms = _event_ms(shade, 20, stream, flush)
     covered = float(((frags & 0xffffffff) != 0).float().mean())
@@ -265,7 +278,7 @@ def frame_pipeline(wt, workloads, stream, flush):
         peak_src = "MEASURED_PEAKS.json hbm_gbs (copy, measured)"
     except (OSError, KeyError, ValueError):
         hbm_peak, peak_src = 6800.0, "fallback 6.8 TB/s"
-    return {"vertices": n, "terms": n * len(w.waves), "viewport": [VW, VH], "water_pixels_frac": covered,
+    return {"vertices": n, "terms": n * F["waves"], "viewport": [VW, VH], "water_pixels_frac": covered,
             "frame_graph_ms": fms, "raster_ms": rms, "shade_ms": sms,
             "frames_per_s": 1e3 / fms, "projected_grid_kernel_ms": gms, "displace_ms": dms,
             "vertex_stage_ms": vms, "vertex_stage_bytes": stage_bytes,
@@ -536,10 +549,28 @@ def run_adjoint_only(args):
                       "terms_per_s": w.n_terms / (ms * 1e-3)}), flush=True)
 
 
+def run_frame_only(args):
+    """The water frame (camera -> pixels at 1920 x 1080 over a 1024^2 grid,
+    eager launches): warmup, then `steps` timed frames; prints one JSON line
+    (not the headline)."""
+    import torch
+    wt = __graft_entry__.load_package()
+    from wave_tool_gb300 import workloads
+    F = build_frame(wt, workloads)
+    for _ in range(args.warmup):
+        F["frame"]()
+    ms = _event_ms(F["frame"], args.steps, torch.cuda.current_stream())
+    print(json.dumps({"mode": "frame", "vertices": F["n"], "viewport": [F["VW"], F["VH"]], "ms_per_frame": ms,
+                      "frames_per_s": 1e3 / ms}), flush=True)
+
+
 def main():
     args = parse_args()
     if args.mode == "adjoint":
         run_adjoint_only(args)
+        return
+    if args.mode == "frame":
+        run_frame_only(args)
         return
     if args.impl == "reference":
         run_reference(args)
