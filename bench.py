@@ -36,6 +36,7 @@ import __graft_entry__  # noqa: E402
 METRIC = "Gerstner terms/s (verts x waves) at <=1e-5 rel err vs FP64; batched persistent launch"
 UNIT = "terms/s"
 PROFILE_TRAFFIC = ROOT / "profiles" / "forward_config3_ncu.md"
+E2E_GROUPS = 4  # streams the end-to-end step is split over
 
 
 def parse_args():
@@ -413,24 +414,45 @@ def run_ours(args):
 
     # end to end through the C ABI from pinned host buffers, outputs in the
     # layout the reference's vertex array consumes (world positions and normals
-    # as tightly packed vec3, render-engine.cpp:1175-1191)
+    # as tightly packed vec3, render-engine.cpp:1175-1191).  The patches are
+    # split into E2E_GROUPS contiguous groups of about equal terms, each a
+    # wt_gerstner_displace call on its own stream with its own workspace: the
+    # copy back of one group overlaps the kernel of the next.
     e2e_flags = wt.WT_OUT_WORLD | wt.WT_LAYOUT_VEC3
     epos, enrm = surf.alloc_outputs(e2e_flags)
-    hp = torch.from_numpy(np.ascontiguousarray(w.patches).view(np.uint8).reshape(-1)).pin_memory()
-    hw = torch.from_numpy(np.ascontiguousarray(w.waves).view(np.uint8).reshape(-1)).pin_memory()
-    htex = hm.texels.cpu().pin_memory()
     hpos = torch.empty(epos.shape, dtype=epos.dtype, pin_memory=True)
     hnrm = torch.empty(enrm.shape, dtype=enrm.dtype, pin_memory=True)
-    h2d = hp.numel() + hw.numel() + htex.numel() * 4
+    htex = hm.texels.cpu().pin_memory()
+    hw = torch.from_numpy(np.ascontiguousarray(w.waves).view(np.uint8).reshape(-1)).pin_memory()
+    cum = np.cumsum(w.patches["cols"].astype(np.int64) * w.patches["rows"] * w.patches["wave_count"])
+    cuts = [0] + [int(np.searchsorted(cum, cum[-1] * (g + 1) / E2E_GROUPS)) + 1 for g in range(E2E_GROUPS - 1)] + \
+        [len(w.patches)]
+    groups = []
+    for g in range(E2E_GROUPS):
+        sub = w.patches[cuts[g]:cuts[g + 1]]
+        if len(sub) == 0:
+            continue
+        o0 = int(sub["out_offset"][0])
+        o1 = int(sub["out_offset"][-1]) + int(sub["cols"][-1]) * int(sub["rows"][-1])
+        gs = wt.Surface(sub, w.waves, hm)
+        hp_g = torch.from_numpy(np.ascontiguousarray(sub).view(np.uint8).reshape(-1)).pin_memory()
+        groups.append((gs, hp_g, o0, o1, torch.cuda.Stream()))
+    h2d = htex.numel() * 4 + sum(g[1].numel() + hw.numel() for g in groups)
     d2h = hpos.numel() * 4 + hnrm.numel() * 4
 
     def e2e_step():
-        surf.patches.copy_(hp, non_blocking=True)
-        surf.waves.copy_(hw, non_blocking=True)
         hm.texels.copy_(htex, non_blocking=True)
-        surf.displace(epos, enrm, flags=e2e_flags)
-        hpos.copy_(epos, non_blocking=True)
-        hnrm.copy_(enrm, non_blocking=True)
+        main = torch.cuda.current_stream()
+        for gs, hp_g, o0, o1, st in groups:
+            st.wait_stream(main)
+            with torch.cuda.stream(st):
+                gs.patches.copy_(hp_g, non_blocking=True)
+                gs.waves.copy_(hw, non_blocking=True)
+                gs.displace(epos, enrm, flags=e2e_flags, stream=st)
+                hpos[o0:o1].copy_(epos[o0:o1], non_blocking=True)
+                hnrm[o0:o1].copy_(enrm[o0:o1], non_blocking=True)
+        for g in groups:
+            main.wait_stream(g[4])
 
     e2e_steps = max(3, min(args.steps, 10))
     for _ in range(2):
