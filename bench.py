@@ -505,6 +505,25 @@ def run_ours(args):
         torch.cuda.synchronize()
         ms2 = statistics.median(x.elapsed_time(y) for x, y in evs)
         extras["single_patch_1024sq_32waves_noise"] = {"ms_per_step": ms2, "value": w2.n_terms / (ms2 * 1e-3)}
+        # the reference-sized case: one 128^2 patch, 4 waves (launch-latency bound:
+        # reported, not held to a roofline); eager call and graph replay
+        w1 = workloads.config1()
+        s1 = wt.Surface(w1.patches, w1.waves)
+        p1, n1 = s1.alloc_outputs(flags)
+        for _ in range(5):
+            s1.displace(p1, n1, flags=flags)
+        ms1 = _event_ms(lambda: s1.displace(p1, n1, flags=flags), 20, stream, flush)
+        gs1 = torch.cuda.Stream()
+        gs1.wait_stream(stream)
+        g1 = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g1, stream=gs1):
+            s1.displace(p1, n1, flags=flags, stream=gs1)
+        g1.replay()
+        torch.cuda.synchronize()
+        gms1 = _event_ms(g1.replay, 20, stream, flush)
+        extras["plain_128sq_4waves"] = {"ms_per_step": ms1, "graph_ms_per_step": gms1,
+                                        "value": w1.n_terms / (ms1 * 1e-3),
+                                        "hbm_gbs": 32.0 * w1.n_vertices / (ms1 * 1e-3) / 1e9}
 
     cpu = None
     if rank == 0:
