@@ -461,8 +461,9 @@ wt_status wt_set_tuning(const wt_tuning* tuning);
 wt_status wt_get_tuning(wt_tuning* tuning);
 
 /* Times every candidate launch shape on the given (device-resident) workload
- * with `reps` launches each (CUDA events on `stream`, synchronising it) and
- * caches the fastest for the workload's shape bucket (the bit lengths of
+ * (CUDA events on `stream`, synchronising it; after 4 * reps warm-up
+ * launches, each candidate's best of three batches of `reps` launches, over
+ * two passes) and caches the fastest for the workload's shape bucket (the bit lengths of
  * n_patches and n_waves): later wt_gerstner_displace calls in that bucket use
  * it.  Returns it in *best (may be NULL).  Arguments as wt_gerstner_displace;
  * the outputs are overwritten. */

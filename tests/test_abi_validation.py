@@ -1,0 +1,78 @@
+"""Host-side argument validation of the frame-stage entry points (no GPU
+needed: every call here is rejected before any CUDA call)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import pytest
+
+FAKE = 0x10000  # an aligned, never dereferenced address
+ODD = 0x10004   # 4-byte aligned, not 8 / 16
+
+
+@pytest.fixture(scope="module")
+def L(wt):
+    wt.build()
+    return wt.lib()
+
+
+def test_vertex_stage_rejects_bad_arguments(wt, L):
+    E = wt.abi.WT_ERR_INVALID_ARG
+    assert L.wt_vertex_stage(None, FAKE, FAKE, 10, 0, FAKE, None, None, None, None, None) == E  # no view
+    assert L.wt_vertex_stage(FAKE, None, FAKE, 10, 0, FAKE, None, None, None, None, None) == E  # no positions
+    assert L.wt_vertex_stage(FAKE, ODD, FAKE, 10, 0, FAKE, None, None, None, None, None) == E   # float4 misaligned
+    assert L.wt_vertex_stage(FAKE, FAKE, None, 10, 0, None, None, None, FAKE, None, None) == E  # facing needs nrm
+    assert L.wt_vertex_stage(FAKE, FAKE, FAKE, 10, 0, ODD, None, None, None, None, None) == E   # clip misaligned
+    assert L.wt_vertex_stage(FAKE, FAKE, FAKE, 10, 8, FAKE, None, None, None, None, None) == E  # unknown flag
+    assert b"wt_vertex_stage" in L.wt_last_error()
+
+
+def test_water_raster_rejects_bad_arguments(wt, L):
+    E, N = wt.abi.WT_ERR_INVALID_ARG, wt.abi.WT_ERR_NOMEM
+    ok = (FAKE, 4, FAKE, 2, 64, 32, None, FAKE, FAKE, 64, None)
+
+    def call(**kw):
+        a = list(ok)
+        names = ["clip", "nv", "idx", "nt", "w", "h", "depth", "frags", "ws", "wsb", "stream"]
+        for k, v in kw.items():
+            a[names.index(k)] = v
+        return L.wt_water_raster(*a)
+
+    assert call(w=0) == E and call(h=16385) == E
+    assert call(frags=None) == E and call(frags=ODD) == E
+    assert call(clip=ODD) == E and call(idx=None) == E
+    assert call(ws=None) == E and call(wsb=63) == N
+    sz = C.c_size_t()
+    assert L.wt_water_raster_workspace_size(1000, C.byref(sz)) == 0 and sz.value == 16000
+
+
+def test_water_shade_rejects_bad_arguments(wt, L):
+    E = wt.abi.WT_ERR_INVALID_ARG
+    sh = wt.water_shading()
+    tex = wt.CWaterTextures(None, None, None, FAKE, 8, 0)
+
+    def call(shading=sh, textures=tex, w=64, h=32, frags=FAKE, ndc0=FAKE, colour=FAKE):
+        return L.wt_water_shade(frags, FAKE, 4, FAKE, 2, FAKE, FAKE, FAKE, ndc0, w, h,
+                                C.byref(shading) if shading is not None else None,
+                                C.byref(textures) if textures is not None else None, colour, None, None)
+
+    assert call(w=0) == E
+    assert call(frags=None) == E and call(ndc0=ODD + 2) == E
+    assert call(shading=None) == E and call(textures=None) == E
+    assert call(textures=wt.CWaterTextures(None, None, None, None, 8, 0)) == E   # a sky box is required
+    assert call(shading=wt.water_shading(z_near=0.0)) == E
+    assert call(shading=wt.water_shading(z_far=0.05)) == E
+    assert call(shading=wt.water_shading(sun_strength=float("nan"))) == E
+    assert call(colour=ODD) == E
+
+
+def test_projected_grid_async_and_unorm8_reject_bad_arguments(wt, L):
+    E = wt.abi.WT_ERR_INVALID_ARG
+    assert L.wt_projected_grid_async(None, FAKE, FAKE, None) == E
+    assert L.wt_projected_grid_async(FAKE, None, FAKE, None) == E
+    assert L.wt_projected_grid_async(FAKE, FAKE, None, None) == E
+    assert L.wt_heightmap_from_unorm8(FAKE, 16, 16, 5, 80, 1, FAKE, None) == E   # channels
+    assert L.wt_heightmap_from_unorm8(FAKE, 16, 16, 4, 60, 1, FAKE, None) == E   # stride < width * channels
+    assert L.wt_heightmap_from_unorm8(FAKE, 16, 16, 4, 64, 2, FAKE, None) == E   # flip flag
+    assert L.wt_heightmap_from_unorm8(None, 16, 16, 4, 64, 1, FAKE, None) == E
+    assert L.wt_heightmap_from_unorm8(FAKE, 0, 16, 4, 64, 1, FAKE, None) == E
