@@ -65,6 +65,13 @@ __host__ __device__ __forceinline__ void row_tiling(uint32_t cols, uint32_t smax
     *tpr_out = bestT;
 }
 
+// Forward tiling: tiles of 32*smax columns along a row, the row's last tile
+// only as many 32-column blocks as the row still needs (so a row is padded to
+// a multiple of 32 columns, not of 32*smax).
+__host__ __device__ __forceinline__ uint32_t fwd_tiles_per_row(uint32_t cols, uint32_t smax) {
+    return (cols + 32 * smax - 1) / (32 * smax);
+}
+
 // ---- shared epilogue -------------------------------------------------------
 
 // Texel coordinate -> the two texel indices of the GL_LINEAR footprint and
