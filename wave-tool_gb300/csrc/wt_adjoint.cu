@@ -406,12 +406,7 @@ __global__ void __launch_bounds__(256) k_adj_waves(const wt_patch* __restrict__ 
     }
 }
 
-int device_sms() {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return sms;
-}
+int device_sms() { return sm_count(); }
 
 template <typename K, typename... Args>
 cudaError_t launch_pdl(K kernel, dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {

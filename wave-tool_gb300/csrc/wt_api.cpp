@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <atomic>
 #include <mutex>
 #include <string>
 
@@ -149,6 +150,17 @@ wt_status run_displace(const wt_patch* patches, uint32_t n_patches, const wt_wav
 
 namespace wt {
 void set_last_error(const char* msg) { g_last_error = msg; }
+
+int sm_count() {
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v > 0) return v;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) return 0;
+    cache[dev].store(v, std::memory_order_relaxed);
+    return v;
+}
 FwdConfig forward_config(uint32_t n_patches, uint32_t n_waves) { return cfg_for(n_patches, n_waves); }
 }  // namespace wt
 

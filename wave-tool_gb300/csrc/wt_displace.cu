@@ -20,6 +20,8 @@
 //                            surface Jacobian.  Epilogue: heightmap bilerp +
 //                            gradient, exact normal, streaming float4 stores.
 #include <cuda_runtime.h>
+
+#include <atomic>
 #include <cstdint>
 
 #include "wt_device.cuh"
@@ -413,24 +415,27 @@ template <int THREADS, int MINB, int SMAX, int EPI>
 cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const HmDev& hm, float* pos,
                          float* nrm, uint32_t flags, void* ws, const WsLayout& L, cudaStream_t s) {
     constexpr int kMaxDev = 64;
-    static int sms[kMaxDev] = {}, occ[kMaxDev] = {};
+    static std::atomic<int> occ_cache[kMaxDev];  // resident blocks per SM, per device
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+    const int sm = sm_count();
+    if (sm <= 0) return cudaErrorInvalidDevice;
     constexpr size_t smem = sizeof(float4) * (THREADS / 32) * (32 * kStage + EPI * SMAX * 2 * 32);
-    if (sms[dev] == 0) {
-        int o = 0, m = 0;
+    int occ = occ_cache[dev].load(std::memory_order_relaxed);
+    if (occ == 0) {
+        int o = 0;
         cudaError_t e = cudaFuncSetAttribute(k_forward<THREADS, MINB, SMAX, EPI>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        cudaDeviceGetAttribute(&m, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_forward<THREADS, MINB, SMAX, EPI>, THREADS, smem);
-        occ[dev] = o < 1 ? 1 : o;
-        sms[dev] = m;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_forward<THREADS, MINB, SMAX, EPI>, THREADS, smem);
+        if (e != cudaSuccess) return e;
+        occ = o < 1 ? 1 : o;
+        occ_cache[dev].store(occ, std::memory_order_relaxed);
     }
-    const int bps = cfg.blocks_per_sm > 0 ? (cfg.blocks_per_sm < occ[dev] ? cfg.blocks_per_sm : occ[dev]) : occ[dev];
+    const int bps = cfg.blocks_per_sm > 0 ? (cfg.blocks_per_sm < occ ? cfg.blocks_per_sm : occ) : occ;
     cudaLaunchConfig_t lc = {};
-    lc.gridDim = dim3((unsigned)(sms[dev] * bps));
+    lc.gridDim = dim3((unsigned)(sm * bps));
     lc.blockDim = dim3(THREADS);
     lc.dynamicSmemBytes = smem;
     lc.stream = s;
@@ -457,12 +462,8 @@ cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wa
                                    fwd_tiling ? 1u : 0u, w, L);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    static int sms = -1;
-    if (sms < 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
+    const int sms = sm_count();
+    if (sms <= 0) return cudaErrorInvalidDevice;
     cudaLaunchConfig_t lc = {};
     lc.gridDim = dim3((unsigned)sms);
     lc.blockDim = dim3(256);
@@ -502,12 +503,8 @@ cudaError_t launch_forward(const FwdConfig& cfg, const wt_patch* patches, uint32
 cudaError_t launch_forward_naive(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
                                  const HmDev& hm, float* pos, float* nrm, uint32_t flags, void* ws,
                                  const WsLayout& L, uint64_t, cudaStream_t s) {
-    static int sms = -1;
-    if (sms < 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
+    const int sms = sm_count();
+    if (sms <= 0) return cudaErrorInvalidDevice;
     k_forward_naive<<<sms * 4, 256, 0, s>>>(patches, n_patches, waves, hm, pos, nrm, flags,
                                             static_cast<const char*>(ws), L);
     return cudaGetLastError();

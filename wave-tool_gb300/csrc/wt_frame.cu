@@ -13,6 +13,7 @@
 // streaming, HBM-bound kernel (reads 2 x 16 B, writes up to 72 B per vertex).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -463,7 +464,7 @@ wt_status cuda_fail(cudaError_t e, const char* what) {
 
 bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
 
-int g_stage_blocks[64] = {};
+std::atomic<int> g_stage_blocks[64];  // blocks per launch of the vertex stage, per device
 
 }  // namespace
 
@@ -511,17 +512,19 @@ extern "C" wt_status wt_vertex_stage(const wt_view* view, const float* pos, cons
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
     if (dev < 0 || dev >= 64) return fail(WT_ERR_UNSUPPORTED, "device ordinal beyond 63");
-    if (!g_stage_blocks[dev]) {
-        int sms = 0, occ = 0;
-        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+    int cap = g_stage_blocks[dev].load(std::memory_order_relaxed);
+    if (cap == 0) {
+        int occ = 0;
+        const int sms = wt::sm_count();
+        if (sms <= 0) return fail(WT_ERR_CUDA, "cannot read the device's SM count");
         e = vec3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_vertex_stage<true>, kStageThreads, 0)
                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_vertex_stage<false>, kStageThreads, 0);
         if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
-        g_stage_blocks[dev] = sms * (occ > 0 ? occ : 1);
+        cap = sms * (occ > 0 ? occ : 1);
+        g_stage_blocks[dev].store(cap, std::memory_order_relaxed);
     }
     const uint64_t need = (n_vertices + kStageThreads - 1) / kStageThreads;
-    const unsigned blocks = (unsigned)(need < (uint64_t)g_stage_blocks[dev] ? need : (uint64_t)g_stage_blocks[dev]);
+    const unsigned blocks = (unsigned)(need < (uint64_t)cap ? need : (uint64_t)cap);
     const StageOut o{clip_out, ndc0_out, view_out, facing_out, nrm_yaw_out};
     cudaStream_t s = (cudaStream_t)stream;
     if (vec3)

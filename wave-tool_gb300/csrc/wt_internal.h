@@ -143,6 +143,8 @@ cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt
 // ---- host helpers (wt_api.cpp) ---------------------------------------------
 void set_last_error(const char* msg);  // message returned by wt_last_error() on this thread
 FwdConfig forward_config(uint32_t n_patches, uint32_t n_waves);  // tuning in effect for this shape
+// SM count of the current device (cached per device; 0 if it cannot be read)
+int sm_count();
 
 // ---- misc kernels (wt_misc.cu) --------------------------------------------
 cudaError_t launch_indices(uint32_t cols, uint32_t rows, uint32_t base, uint32_t* out, cudaStream_t s);

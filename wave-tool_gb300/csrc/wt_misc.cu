@@ -144,12 +144,7 @@ __global__ void __launch_bounds__(256) k_peak_sin(float* out, int iters) {
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
-int device_sms() {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return sms;
-}
+int device_sms() { return sm_count(); }
 
 }  // namespace
 

@@ -555,18 +555,9 @@ wt_status cuda_fail(cudaError_t e, const char* what) {
 
 bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
 
-int g_sms[64] = {};
-
 wt_status sms_of_device(int* sms) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-    if (dev < 0 || dev >= 64) return fail(WT_ERR_UNSUPPORTED, "device ordinal beyond 63");
-    if (!g_sms[dev]) {
-        e = cudaDeviceGetAttribute(&g_sms[dev], cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
-    }
-    *sms = g_sms[dev];
+    *sms = wt::sm_count();
+    if (*sms <= 0) return fail(WT_ERR_CUDA, "cannot read the device's SM count");
     return WT_OK;
 }
 
