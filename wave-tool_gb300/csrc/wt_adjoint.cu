@@ -27,6 +27,8 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
+#include <atomic>
+
 #include "wt_device.cuh"
 #include "wt_internal.h"
 
@@ -205,10 +207,11 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
         const uint32_t nwaves = patches[p].wave_count;
         const uint64_t out0 = patches[p].out_offset;
         const PatchAux a = aux[p];
-        uint32_t S, tpr;
-        row_tiling(cols, 8, &S, &tpr);
+        // the forward's tiling: 256-column tiles, each row's last tile narrower
+        const uint32_t tpr = tiles_per_row(cols, 8);
         const uint32_t row = lt / tpr;
-        const uint32_t c0 = (lt - row * tpr) * 32u * S;
+        const uint32_t c0 = (lt - row * tpr) * 256u;
+        const uint32_t S = min(8u, (cols - c0 + 31u) / 32u);
         if (nwaves > 0) {
             // ---- phase 1: forward sums and vertex adjoints, vertex per lane
             float acc[8][8];
@@ -427,9 +430,7 @@ cudaError_t launch_pdl(K kernel, dim3 grid, dim3 block, size_t smem, cudaStream_
 
 uint64_t adjoint_records(const wt_patch& p) {
     if (p.cols < 2 || p.rows < 2) return 0;
-    uint32_t S, tpr;
-    dev::row_tiling(p.cols, 8, &S, &tpr);
-    return (uint64_t)p.rows * tpr * p.wave_count;
+    return (uint64_t)p.rows * dev::tiles_per_row(p.cols, 8) * p.wave_count;
 }
 
 cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
@@ -440,13 +441,13 @@ cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt
     cudaError_t e = launch_pdl(k_adj_scan, dim3(1), dim3(1024), 0, s, patches, n_patches, w, L);
     if (e != cudaSuccess) return e;
     const size_t smem = sizeof(float4) * kAdjWarps * (32 * kStage + kGbufVerts * kGbufF4);
-    static bool attr_set[64] = {};
+    static std::atomic<bool> attr_set[64];
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    if (dev >= 0 && dev < 64 && !attr_set[dev].load(std::memory_order_relaxed)) {
         e = cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        attr_set[dev] = true;
+        attr_set[dev].store(true, std::memory_order_relaxed);
     }
     int occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint, 32 * kAdjWarps, smem);

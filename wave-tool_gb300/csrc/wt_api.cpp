@@ -136,7 +136,7 @@ wt_status run_displace(const wt_patch* patches, uint32_t n_patches, const wt_wav
     st = check_outputs(pos, nrm, flags);
     if (st != WT_OK) return st;
     if (n_patches == 0) return WT_OK;
-    cudaError_t e = wt::launch_prep(patches, n_patches, waves, n_waves, P.hm, cap, 32u * cfg.s, true, ws, P.L, s);
+    cudaError_t e = wt::launch_prep(patches, n_patches, waves, n_waves, P.hm, cap, 32u * cfg.s, ws, P.L, s);
     if (e != cudaSuccess) return cuda_fail(e, "prep launch");
     if (flags & WT_PHASE_FP32_NAIVE)
         e = wt::launch_forward_naive(patches, n_patches, waves, P.hm, pos, nrm, flags, ws, P.L, cap, s);
@@ -263,7 +263,7 @@ wt_status wt_gerstner_adjoint(const wt_patch* host_patches, const wt_patch* patc
         cudaError_t e = cudaMemsetAsync(grad_out, 0, sizeof(wt_wave_grad) * n_waves, s);
         return e == cudaSuccess ? WT_OK : cuda_fail(e, "clearing grad_out");
     }
-    cudaError_t e = wt::launch_prep(patches, n_patches, waves, n_waves, P.hm, out_capacity, 256u, false, workspace, L.f, s);
+    cudaError_t e = wt::launch_prep(patches, n_patches, waves, n_waves, P.hm, out_capacity, 256u, workspace, L.f, s);
     if (e != cudaSuccess) return cuda_fail(e, "prep launch");
     uint32_t maxw = 0;
     for (uint32_t i = 0; i < n_patches; ++i) maxw = host_patches[i].wave_count > maxw ? host_patches[i].wave_count : maxw;

@@ -49,26 +49,10 @@ static __device__ uint32_t block_exclusive_scan(uint32_t* a, uint32_t n) {
     return carry;
 }
 
-// Tiling of one patch row: tiles of 32*S columns, S in 1..8, choosing the S
-// whose tiles cover the row with the least padding, with a preference for
-// larger S (each wave's start-up costs about as much as two vertices).
-__host__ __device__ __forceinline__ void row_tiling(uint32_t cols, uint32_t smax, uint32_t* S_out,
-                                                    uint32_t* tpr_out) {
-    uint32_t bestS = smax, bestT = (cols + 32 * smax - 1) / (32 * smax);
-    float best = 32.0f * smax * bestT * (1.0f + 2.0f / (float)smax);
-    for (uint32_t S = smax - 1; S >= 1; --S) {
-        const uint32_t t = (cols + 32 * S - 1) / (32 * S);
-        const float cost = 32.0f * S * t * (1.0f + 2.0f / (float)S);
-        if (cost < best) { best = cost; bestS = S; bestT = t; }
-    }
-    *S_out = bestS;
-    *tpr_out = bestT;
-}
-
-// Forward tiling: tiles of 32*smax columns along a row, the row's last tile
-// only as many 32-column blocks as the row still needs (so a row is padded to
-// a multiple of 32 columns, not of 32*smax).
-__host__ __device__ __forceinline__ uint32_t fwd_tiles_per_row(uint32_t cols, uint32_t smax) {
+// Tiling of a patch row (forward and adjoint): tiles of 32*smax columns, the
+// row's last tile only as many 32-column blocks as the row still needs (so a
+// row is padded to a multiple of 32 columns, not of 32*smax).
+__host__ __device__ __forceinline__ uint32_t tiles_per_row(uint32_t cols, uint32_t smax) {
     return (cols + 32 * smax - 1) / (32 * smax);
 }
 

@@ -61,8 +61,7 @@ __device__ __forceinline__ bool patch_ok(const wt_patch& P, uint32_t n_waves, ui
 __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__ patches, uint32_t n,
                                                     const wt_wave* __restrict__ waves, uint32_t n_waves,
                                                     uint64_t out_capacity, uint64_t coef_capacity,
-                                                    uint32_t tile_cols, uint32_t fwd_tiling, char* ws,
-                                                    WsLayout L) {
+                                                    uint32_t tile_cols, char* ws, WsLayout L) {
     WsHeader* hdr = reinterpret_cast<WsHeader*>(ws);
     uint32_t* sorted = reinterpret_cast<uint32_t*>(ws + L.sorted);
     uint32_t* tile_pre = reinterpret_cast<uint32_t*>(ws + L.tile_pre);
@@ -86,10 +85,7 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
         const bool ok = patch_ok(P, n_waves, out_capacity);
         if (!ok) flag_error(hdr, WT_ERR_INVALID_ARG, p);
         pair_off[p] = ok ? P.wave_count : 0u;
-        uint32_t S, tpr;
-        if (fwd_tiling) tpr = fwd_tiles_per_row(P.cols, tile_cols / 32);
-        else row_tiling(P.cols, tile_cols / 32, &S, &tpr);
-        tiles[p] = ok ? P.rows * tpr : 0u;
+        tiles[p] = ok ? P.rows * tiles_per_row(P.cols, tile_cols / 32) : 0u;
         const uint32_t key = P.wave_count < kSortBins ? P.wave_count : kSortBins - 1;
         atomicAdd(&bins[kSortBins - 1 - key], 1u);  // descending wave count
     }
@@ -300,7 +296,7 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
         const uint32_t nwaves = patches[p].wave_count;
         const uint64_t out0 = patches[p].out_offset;
         const PatchAux a = aux[p];
-        const uint32_t tpr = fwd_tiles_per_row(cols, SMAX);
+        const uint32_t tpr = tiles_per_row(cols, SMAX);
         const uint32_t row = lt / tpr;
         const uint32_t c0 = (lt - row * tpr) * 32u * SMAX;
         const uint32_t S = min((uint32_t)SMAX, (cols - c0 + 31u) / 32u);  // the row's last tile is narrower
@@ -452,14 +448,13 @@ cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const Hm
 }  // namespace
 
 cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
-                        const HmDev& hm, uint64_t out_capacity, uint32_t tile_cols, bool fwd_tiling, void* ws,
+                        const HmDev& hm, uint64_t out_capacity, uint32_t tile_cols, void* ws,
                         const WsLayout& L, cudaStream_t s) {
     char* w = static_cast<char*>(ws);
     // coefficient capacity = what the caller's workspace holds past the fixed part
     // (the header records the real total; the scan refuses to overflow it)
     uint64_t coef_cap = (L.end - L.coef) / sizeof(PairCoef);
-    k_prep_scan<<<1, 1024, 0, s>>>(patches, n_patches, waves, n_waves, out_capacity, coef_cap, tile_cols,
-                                   fwd_tiling ? 1u : 0u, w, L);
+    k_prep_scan<<<1, 1024, 0, s>>>(patches, n_patches, waves, n_waves, out_capacity, coef_cap, tile_cols, w, L);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const int sms = sm_count();

@@ -119,11 +119,10 @@ struct HmDev {
 };
 
 // ---- launchers (wt_displace.cu) -------------------------------------------
-// tile_cols: widest tile; fwd_tiling: the forward's fixed-width tiles with a
-// narrower last tile per row (else the adjoint's one tile width per patch)
+// tile_cols: tile width (each row's last tile narrower, see tiles_per_row)
 cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
                         uint32_t n_waves, const HmDev& hm, uint64_t out_capacity,
-                        uint32_t tile_cols, bool fwd_tiling, void* ws, const WsLayout& L, cudaStream_t s);
+                        uint32_t tile_cols, void* ws, const WsLayout& L, cudaStream_t s);
 cudaError_t launch_forward(const FwdConfig& cfg, const wt_patch* patches, uint32_t n_patches,
                            const HmDev& hm, float* pos, float* nrm, uint32_t flags, void* ws,
                            const WsLayout& L, cudaStream_t s);

@@ -99,7 +99,7 @@ extern "C" wt_status wt_gerstner_displace_noalloc(const wt_patch* patches, uint3
         return fail(WT_ERR_UNSUPPORTED, "no-alloc scratch smaller than its stated limits");
     const wt::FwdConfig cfg = wt::forward_config(n_patches, n_waves);
     cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t e = wt::launch_prep(patches, n_patches, waves, n_waves, h, out_capacity, 32u * cfg.s, true, ws, L, s);
+    cudaError_t e = wt::launch_prep(patches, n_patches, waves, n_waves, h, out_capacity, 32u * cfg.s, ws, L, s);
     if (e != cudaSuccess) return cuda_fail(e, "prep launch");
     if (flags & WT_PHASE_FP32_NAIVE)
         e = wt::launch_forward_naive(patches, n_patches, waves, h, pos_out, nrm_out, flags, ws, L, out_capacity, s);
