@@ -3,8 +3,8 @@ reference gradient (oracle/gerstner_f64.c:wto_adjoint_f64, itself checked
 against FP64 central differences in test_oracle.py).
 
 Tolerance: for each gradient field, max over waves |g_gpu - g_64| <=
-1e-4 * max over waves |g_64| (the benchmark spec's 1e-4 relative bound, taken relative
-to the field's scale so that near-zero entries do not divide by zero)."""
+1e-4 * max over waves |g_64| (the path's 1e-4 relative bound on gradients, taken
+relative to the field's scale so that near-zero entries do not divide by zero)."""
 from __future__ import annotations
 
 import numpy as np

@@ -12,7 +12,9 @@ import pytest
 
 from helpers import golden_cases, golden_uniforms, rel_err
 
-REF_ASSET = Path("/root/reference/assets/textures/noise/waves/waves3/00.png")
+from oracle.build import reference_dir  # noqa: E402
+
+REF_ASSET = reference_dir() / "assets" / "textures" / "noise" / "waves" / "waves3" / "00.png"
 
 
 def decode_grey_png(path: Path) -> np.ndarray:
