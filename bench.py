@@ -51,6 +51,8 @@ def parse_args():
     ap.add_argument("--mode", choices=["forward", "adjoint", "frame"], default="forward",
                     help="'adjoint' times only wt_gerstner_adjoint on 64 uneven patches, 'frame' only the "
                          "camera-to-pixels water frame (for profiling)")
+    ap.add_argument("--saved-sums", action="store_true",
+                    help="with --mode adjoint: time wt_gerstner_adjoint_saved on a saving forward's sums")
     ap.add_argument("--tuning", default="auto",
                     help="'auto' (autotune before timing) or WARPS,CHUNK[,VPL,EPI] to fix the launch shape")
     return ap.parse_args()
@@ -319,7 +321,18 @@ def side_measurements(wt, workloads, surf, pos, nrm, flags, flush, stream, ms_st
             sa.adjoint(gp, gn)
         fms = _event_ms(lambda: sa.displace(pa, na, flags=flags), 10, stream, flush)
         ams = _event_ms(lambda: sa.adjoint(gp, gn), 10, stream, flush)
-        out[name] = {"terms": w.n_terms, "forward_ms": fms, "adjoint_ms": ams, "adjoint_over_forward": ams / fms}
+        # the saving forward (also writes 32 B of wave sums per vertex) and the
+        # adjoint that reads them instead of recomputing the wave sum
+        sums = torch.empty((sa.n_vertices, 8), dtype=torch.float32, device="cuda")
+        for _ in range(3):
+            sa.displace(pa, na, flags=flags, sums=sums)
+            sa.adjoint(gp, gn, sums=sums)
+        sfms = _event_ms(lambda: sa.displace(pa, na, flags=flags, sums=sums), 10, stream, flush)
+        sams = _event_ms(lambda: sa.adjoint(gp, gn, sums=sums), 10, stream, flush)
+        out[name] = {"terms": w.n_terms, "forward_ms": fms, "adjoint_ms": ams, "adjoint_over_forward": ams / fms,
+                     "saving_forward_ms": sfms, "saved_adjoint_ms": sams,
+                     "saved_adjoint_over_forward": sams / fms}
+        del sums
     # precision configuration: 2048^2 vertices x 128 waves at three times
     prec = {}
     for t in (1.0e2, 1.0e4, 1.0e6):
@@ -587,10 +600,15 @@ def run_adjoint_only(args):
     gen = torch.Generator(device="cuda").manual_seed(1)
     gp = torch.randn(pos.shape, device="cuda", generator=gen)
     gn = torch.randn(nrm.shape, device="cuda", generator=gen)
+    sums = None
+    if args.saved_sums:
+        sums = torch.empty((surf.n_vertices, 8), dtype=torch.float32, device="cuda")
+        surf.displace(pos, nrm, flags=0, sums=sums)
     for _ in range(args.warmup):
-        surf.adjoint(gp, gn)
-    ms = _event_ms(lambda: surf.adjoint(gp, gn), args.steps, torch.cuda.current_stream())
-    print(json.dumps({"mode": "adjoint", "workload": w.name, "terms": w.n_terms, "ms_per_step": ms,
+        surf.adjoint(gp, gn, sums=sums)
+    ms = _event_ms(lambda: surf.adjoint(gp, gn, sums=sums), args.steps, torch.cuda.current_stream())
+    print(json.dumps({"mode": "adjoint", "saved_sums": sums is not None, "workload": w.name, "terms": w.n_terms,
+                      "ms_per_step": ms,
                       "terms_per_s": w.n_terms / (ms * 1e-3)}), flush=True)
 
 

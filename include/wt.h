@@ -236,6 +236,29 @@ wt_status wt_gerstner_adjoint(const wt_patch* host_patches, const wt_patch* patc
                               uint32_t flags, wt_wave_grad* grad_out,
                               void* workspace, size_t workspace_bytes, wt_stream stream);
 
+/* wt_gerstner_displace that also writes each output vertex's eight wave sums
+ * (the displacement and surface-Jacobian sums the normal is built from) to
+ * sums_out: device, 16-byte aligned, 8 floats per output vertex (32 *
+ * out_capacity bytes), vertex v at sums_out[8v .. 8v+7].  With them,
+ * wt_gerstner_adjoint_saved skips recomputing the forward, the way an
+ * autograd function saves its activations.  No reference counterpart. */
+wt_status wt_gerstner_displace_saving(const wt_patch* patches, uint32_t n_patches,
+                                      const wt_wave* waves, uint32_t n_waves,
+                                      const wt_heightmap* hm,
+                                      float* pos_out, float* nrm_out, uint64_t out_capacity,
+                                      uint32_t flags, float* sums_out, void* workspace,
+                                      size_t workspace_bytes, wt_stream stream);
+
+/* wt_gerstner_adjoint from the sums a wt_gerstner_displace_saving call wrote
+ * for the same patches and waves (same arguments otherwise, same gradients up
+ * to FP32 rounding: the saved sums come from the forward's own tiling). */
+wt_status wt_gerstner_adjoint_saved(const wt_patch* host_patches, const wt_patch* patches, uint32_t n_patches,
+                                    const wt_wave* waves, uint32_t n_waves,
+                                    const wt_heightmap* hm,
+                                    const float* d_pos, const float* d_nrm, uint64_t out_capacity,
+                                    uint32_t flags, const float* sums, wt_wave_grad* grad_out,
+                                    void* workspace, size_t workspace_bytes, wt_stream stream);
+
 /* The projected-grid triangle list: for each cell (row, col) the triangles
  * (r,c),(r+1,c+1),(r+1,c) and (r,c),(r,c+1),(r+1,c+1), vertex (r,c) =
  * base_vertex + r*cols + c.  6*(cols-1)*(rows-1) uint32 into idx_out (device).

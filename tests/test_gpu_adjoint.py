@@ -34,11 +34,34 @@ def _check(grad_gpu, grad64, tol=GRAD_TOL, used=None):
         assert err <= tol * max(scale, 1e-30), f"{name}: max err {err:.3e} vs scale {scale:.3e}"
 
 
-def run_adjoint(wt, w, gp, gn, flags=0, texels=None):
+EDGE_MARGIN = 2e-3  # texels
+
+
+def run_adjoint(wt, w, gp, gn, flags=0, texels=None, saved=False, oracle=None):
+    """saved: the forward's sums from wt_gerstner_displace_saving instead of
+    the adjoint's own recompute.
+
+    oracle (with a heightmap): the upstream gradients gp, gn (CPU tensors) are
+    zeroed IN PLACE at the vertices whose FP64 sample point lies within
+    EDGE_MARGIN texels of a texel-cell boundary.  The bilinear layer's slope
+    and cross derivative jump there, so an FP32 sample point a rounding away
+    from the FP64 one can fall in the neighbouring cell; those few vertices
+    would measure the cell they landed in, not the gradient arithmetic."""
     import torch
     hm = wt.heightmap_from(w.heightmap, texels)
     surf = wt.Surface(w.patches, w.waves, hm)
-    grad = surf.adjoint(gp.cuda(), None if gn is None else gn.cuda(), flags=flags)
+    if oracle is not None and hm is not None:
+        tex = hm.texels.cpu().numpy()
+        edge = oracle.displace_f64(w.patches, w.waves, tex, w.heightmap)[3]
+        near = torch.from_numpy(edge < EDGE_MARGIN)
+        gp[near[:gp.shape[0]]] = 0
+        if gn is not None:
+            gn[near[:gn.shape[0]]] = 0
+    sums = None
+    if saved:
+        sums = torch.empty((max(surf.n_vertices, 1), 8), dtype=torch.float32, device="cuda")
+        surf.displace(flags=flags & wt.WT_LAYOUT_VEC3, sums=sums)
+    grad = surf.adjoint(gp.cuda(), None if gn is None else gn.cuda(), flags=flags, sums=sums)
     torch.cuda.synchronize()
     st, bad = wt.workspace_status(surf.adj_workspace)
     assert st == 0, (st, bad)
@@ -71,9 +94,9 @@ def test_adjoint_with_noise_heightmap(wt, oracle, gpu):
     from wave_tool_gb300 import workloads
     w = workloads.config3(n_patches=4, seed=7)
     gp, gn = _upstream(w.n_vertices, 3, 1.0, 1.0)
-    g, tex = run_adjoint(wt, w, gp, gn)
+    g, tex = run_adjoint(wt, w, gp, gn, oracle=oracle)
     g64 = oracle.adjoint_f64(w.patches, w.waves, gp.numpy(), gn.numpy(), tex, w.heightmap)
-    _check(g, g64, tol=3e-4)
+    _check(g, g64)
 
 
 def test_adjoint_deterministic_and_layouts(wt, gpu):
@@ -120,3 +143,42 @@ def test_adjoint_validation(wt, gpu):
     st, first = wt.workspace_status(s2.adj_workspace)
     assert st == wt.abi.WT_ERR_INVALID_ARG and first == 1
     assert np.isfinite(grad.cpu().numpy()).all()
+
+
+@pytest.mark.parametrize("saved", [False, True])
+@pytest.mark.parametrize("seed", range(3))
+def test_adjoint_ragged_with_heightmap(wt, oracle, gpu, seed, saved):
+    """Ragged patches up to 300 x 300, with and without the heightmap layer
+    (both wrap modes): wt_gerstner_adjoint, and wt_gerstner_adjoint_saved (the
+    forward's sums instead of a recompute), against the FP64 gradient."""
+    from wave_tool_gb300 import workloads
+    w = workloads.small_random(seed + 10, n_patches=3, side_range=(2, 300), n_waves_range=(1, 40),
+                               heightmap=bool(seed % 2), wrap=seed % 2)
+    gp, gn = _upstream(w.n_vertices, seed)
+    g, tex = run_adjoint(wt, w, gp, gn, saved=saved, oracle=oracle)
+    g64 = oracle.adjoint_f64(w.patches, w.waves, gp.numpy(), gn.numpy(), tex, w.heightmap)
+    _check(g, g64)
+
+
+def test_saving_forward_outputs_and_batched_saved_adjoint(wt, oracle, gpu):
+    """The saving forward writes the same positions and normals as the plain
+    one; on uneven batched patches the saved-sums adjoint agrees with the
+    recomputing one to FP32 rounding of the sums."""
+    import torch
+    from wave_tool_gb300 import workloads
+    w = workloads.config3(n_patches=10, seed=31)
+    hm = wt.heightmap_from(w.heightmap)
+    surf = wt.Surface(w.patches, w.waves, hm)
+    p0, n0 = surf.displace(flags=0)
+    sums = torch.empty((surf.n_vertices, 8), dtype=torch.float32, device="cuda")
+    p1, n1 = surf.displace(flags=0, sums=sums)
+    torch.cuda.synchronize()
+    assert torch.equal(p0, p1) and torch.equal(n0, n1)
+    assert torch.isfinite(sums).all()
+    gp, gn = _upstream(surf.n_vertices, 5)
+    gp, gn = gp.cuda(), gn.cuda()
+    a = surf.adjoint(gp, gn).cpu().numpy().astype(np.float64)
+    b = surf.adjoint(gp, gn, sums=sums).cpu().numpy().astype(np.float64)
+    _check(b, a, tol=2e-5)
+    with pytest.raises(wt.WtError):
+        surf.displace(flags=wt.WT_PHASE_FP32_NAIVE, sums=sums)

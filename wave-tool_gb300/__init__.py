@@ -35,6 +35,7 @@ EXPORTED = [
     "wt_measure_peaks", "wt_set_tuning", "wt_get_tuning", "wt_autotune_displace",
     "wt_projected_grid", "wt_projected_grid_async", "wt_vertex_stage", "wt_heightmap_from_unorm8",
     "wt_water_raster", "wt_water_raster_workspace_size", "wt_water_shade",
+    "wt_gerstner_displace_saving", "wt_gerstner_adjoint_saved",
 ]
 
 
@@ -106,6 +107,10 @@ def lib():
                                                      u32, vp, sz, vp]
         L.wt_gerstner_adjoint.argtypes = [vp, vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, u64, u32, vp,
                                           vp, sz, vp]
+        L.wt_gerstner_displace_saving.argtypes = [vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, u64, u32, vp,
+                                                  vp, sz, vp]
+        L.wt_gerstner_adjoint_saved.argtypes = [vp, vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, u64, u32, vp,
+                                                vp, vp, sz, vp]
         L.wt_grid_indices.argtypes = [u32, u32, u32, vp, vp]
         L.wt_noise_synth.argtypes = [vp, u32, u32, u32, vp, vp, sz, vp]
         L.wt_wave_from_reference.argtypes = [C.c_float] * 6 + [u32, C.POINTER(CWave)]
@@ -232,13 +237,22 @@ class Surface:
         nrm = torch.empty_like(pos) if normals else None
         return pos, nrm
 
-    def displace(self, pos=None, nrm=None, flags: int = 0, normals: bool = True, stream=None, unbatched=False):
+    def displace(self, pos=None, nrm=None, flags: int = 0, normals: bool = True, stream=None, unbatched=False,
+                 sums=None):
+        """Positions and normals; with `sums` (an (n_vertices, 8) float32
+        tensor) also the per-vertex wave sums an adjoint can reuse."""
         if pos is None:
             pos, nrm = self.alloc_outputs(flags, normals)
         hm = self.heightmap.cstruct() if self.heightmap is not None else None
         hmp = C.byref(hm) if hm is not None else None
         cap = pos.shape[0]
-        if unbatched:
+        if sums is not None:
+            assert sums.shape[0] >= cap and sums.shape[-1] == 8 and sums.is_contiguous()
+            check(lib().wt_gerstner_displace_saving(
+                self.patches.data_ptr(), self.n_patches, self.waves.data_ptr(), self.n_waves, hmp,
+                pos.data_ptr(), _ptr(nrm), cap, flags, sums.data_ptr(), self.workspace.data_ptr(),
+                self.workspace.numel(), stream_handle(stream)))
+        elif unbatched:
             check(lib().wt_gerstner_displace_unbatched(
                 self.host_patches.ctypes.data, self.patches.data_ptr(), self.n_patches, self.waves.data_ptr(),
                 self.n_waves, hmp, pos.data_ptr(), _ptr(nrm), cap, flags, self.workspace.data_ptr(),
@@ -253,18 +267,26 @@ class Surface:
     def status(self, stream=None):
         return workspace_status(self.workspace, stream)
 
-    def adjoint(self, d_pos, d_nrm=None, flags: int = 0, grad=None, stream=None):
+    def adjoint(self, d_pos, d_nrm=None, flags: int = 0, grad=None, stream=None, sums=None):
         """dL/dwave (n_waves x 8 float32 tensor, the wt_wave_grad fields) for
-        upstream gradients d_pos / d_nrm laid out like the outputs."""
+        upstream gradients d_pos / d_nrm laid out like the outputs; with the
+        `sums` a saving displace wrote, the forward is not recomputed."""
         torch = _torch()
         if getattr(self, "adj_workspace", None) is None:
             self.adj_workspace = empty_bytes(adjoint_workspace_bytes(self.host_patches), self.patches.device)
         if grad is None:
             grad = torch.empty((self.n_waves, 8), dtype=torch.float32, device=self.patches.device)
         hm = self.heightmap.cstruct() if self.heightmap is not None else None
+        hmp = C.byref(hm) if hm is not None else None
+        if sums is not None:
+            check(lib().wt_gerstner_adjoint_saved(
+                self.host_patches.ctypes.data, self.patches.data_ptr(), self.n_patches, self.waves.data_ptr(),
+                self.n_waves, hmp, d_pos.data_ptr(), _ptr(d_nrm), d_pos.shape[0], flags, sums.data_ptr(),
+                grad.data_ptr(), self.adj_workspace.data_ptr(), self.adj_workspace.numel(), stream_handle(stream)))
+            return grad
         check(lib().wt_gerstner_adjoint(
             self.host_patches.ctypes.data, self.patches.data_ptr(), self.n_patches, self.waves.data_ptr(),
-            self.n_waves, C.byref(hm) if hm is not None else None, d_pos.data_ptr(), _ptr(d_nrm), d_pos.shape[0],
+            self.n_waves, hmp, d_pos.data_ptr(), _ptr(d_nrm), d_pos.shape[0],
             flags, grad.data_ptr(), self.adj_workspace.data_ptr(), self.adj_workspace.numel(),
             stream_handle(stream)))
         return grad

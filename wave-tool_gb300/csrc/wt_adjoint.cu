@@ -162,9 +162,13 @@ __device__ __forceinline__ void wave_moments(const float4* __restrict__ gbuf, ui
     }
 }
 
+// SAVED: phase 1 reads the forward's saved sums instead of recomputing them
+// (a compile-time switch, so that the recomputing kernel carries no test).
+template <bool SAVED>
 __global__ void __launch_bounds__(32 * kAdjWarps, 4)
 k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restrict__ gpos,
-          const float* __restrict__ gnrm, uint32_t flags, char* __restrict__ ws, AdjLayout L) {
+          const float* __restrict__ gnrm, uint32_t flags, char* __restrict__ ws, AdjLayout L,
+          const float4* __restrict__ sums) {
 #if __CUDA_ARCH__ >= 900
     cudaGridDependencySynchronize();
 #endif
@@ -213,33 +217,46 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
         const uint32_t c0 = (lt - row * tpr) * 256u;
         const uint32_t S = min(8u, (cols - c0 + 31u) / 32u);
         if (nwaves > 0) {
-            // ---- phase 1: forward sums and vertex adjoints, vertex per lane
-            float acc[8][8];
+            const uint64_t rowbase = out0 + (uint64_t)row * cols;
+            if (SAVED) {
+                // ---- phase 1 from the forward's saved sums: park them
+                for (uint32_t j = 0; j < S; ++j) {
+                    const uint32_t col = c0 + lane + 32 * j;
+                    float4* d = gbuf + kGbufF4 * (lane + 32 * j);
+                    if (col < cols) {
+                        d[0] = __ldcs(sums + 2 * (rowbase + col));
+                        d[1] = __ldcs(sums + 2 * (rowbase + col) + 1);
+                    }
+                }
+            } else {
+                // ---- phase 1: forward sums recomputed, vertex per lane
+                float acc[8][8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j)
+                for (int j = 0; j < 8; ++j)
 #pragma unroll
-                for (int mm = 0; mm < 8; ++mm) acc[j][mm] = 0.0f;
-            for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
-                const uint32_t nw = min(32u, nwaves - w0);
-                __syncwarp();
-                if (lane < nw) stage_wave(coef[a.pair_offset + w0 + lane], c0, row, wst + kStage * lane);
-                __syncwarp();
-                wave_loop_dispatch<8>(S, acc, wst, nw, lane);
+                    for (int mm = 0; mm < 8; ++mm) acc[j][mm] = 0.0f;
+                for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
+                    const uint32_t nw = min(32u, nwaves - w0);
+                    __syncwarp();
+                    if (lane < nw) stage_wave(coef[a.pair_offset + w0 + lane], c0, row, wst + kStage * lane);
+                    __syncwarp();
+                    wave_loop_dispatch<8>(S, acc, wst, nw, lane);
+                }
+                // park the eight sums of each vertex
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    if ((uint32_t)j < S) {
+                        float4* d = gbuf + kGbufF4 * (lane + 32 * j);
+                        d[0] = make_float4(acc[j][0], acc[j][1], acc[j][2], acc[j][3]);
+                        d[1] = make_float4(acc[j][4], acc[j][5], acc[j][6], acc[j][7]);
+                    }
+                }
             }
+            // then turn them into the vertex adjoints in a rolled loop (one
+            // copy of that code)
             const float v = (float)row * a.inv_rm1;
             const float gx = (a.e1x + v * a.e3x) * a.inv_cm1, gz = (a.e1z + v * a.e3z) * a.inv_cm1;
             const float xb0 = fmaf((float)c0, gx, v * a.e2x), zb0 = fmaf((float)c0, gz, v * a.e2z);
-            const uint64_t rowbase = out0 + (uint64_t)row * cols;
-            // park the eight sums of each vertex, then turn them into the
-            // vertex adjoints in a rolled loop (one copy of that code)
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                if ((uint32_t)j < S) {
-                    float4* d = gbuf + kGbufF4 * (lane + 32 * j);
-                    d[0] = make_float4(acc[j][0], acc[j][1], acc[j][2], acc[j][3]);
-                    d[1] = make_float4(acc[j][4], acc[j][5], acc[j][6], acc[j][7]);
-                }
-            }
             for (uint32_t j = 0; j < S; ++j) {
                 const uint32_t vi = lane + 32 * j;
                 const uint32_t col = c0 + vi;
@@ -426,6 +443,30 @@ cudaError_t launch_pdl(K kernel, dim3 grid, dim3 block, size_t smem, cudaStream_
     return cudaLaunchKernelEx(&lc, kernel, args...);
 }
 
+// The persistent main kernel: one grid of SMs x resident blocks (the
+// occupancy is read once per device and instantiation).
+template <bool SAVED>
+cudaError_t launch_adj_main(int sms, cudaStream_t s, const wt_patch* patches, const HmDev& hm, const float* gpos,
+                            const float* gnrm, uint32_t flags, char* w, const AdjLayout& L, const float* sums) {
+    constexpr size_t smem = sizeof(float4) * kAdjWarps * (32 * kStage + kGbufVerts * kGbufF4);
+    static std::atomic<int> occ_cache[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    int occ = occ_cache[dev].load(std::memory_order_relaxed);
+    if (occ == 0) {
+        cudaError_t e = cudaFuncSetAttribute(k_adjoint<SAVED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        int o = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_adjoint<SAVED>, 32 * kAdjWarps, smem);
+        if (e != cudaSuccess) return e;
+        occ = o < 1 ? 1 : o;
+        occ_cache[dev].store(occ, std::memory_order_relaxed);
+    }
+    return launch_pdl(k_adjoint<SAVED>, dim3(sms * occ), dim3(32 * kAdjWarps), smem, s, patches, hm, gpos, gnrm,
+                      flags, w, L, reinterpret_cast<const float4*>(sums));
+}
+
 }  // namespace
 
 uint64_t adjoint_records(const wt_patch& p) {
@@ -435,24 +476,14 @@ uint64_t adjoint_records(const wt_patch& p) {
 
 cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
                            uint32_t max_waves_per_patch, const HmDev& hm, const float* gpos, const float* gnrm,
-                           uint32_t flags, wt_wave_grad* grad, void* ws, const AdjLayout& L, cudaStream_t s) {
+                           uint32_t flags, wt_wave_grad* grad, void* ws, const AdjLayout& L, const float* sums,
+                           cudaStream_t s) {
     char* w = static_cast<char*>(ws);
     const int sms = device_sms();
     cudaError_t e = launch_pdl(k_adj_scan, dim3(1), dim3(1024), 0, s, patches, n_patches, w, L);
     if (e != cudaSuccess) return e;
-    const size_t smem = sizeof(float4) * kAdjWarps * (32 * kStage + kGbufVerts * kGbufF4);
-    static std::atomic<bool> attr_set[64];
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev >= 0 && dev < 64 && !attr_set[dev].load(std::memory_order_relaxed)) {
-        e = cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr_set[dev].store(true, std::memory_order_relaxed);
-    }
-    int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint, 32 * kAdjWarps, smem);
-    if (occ < 1) occ = 1;
-    e = launch_pdl(k_adjoint, dim3(sms * occ), dim3(32 * kAdjWarps), smem, s, patches, hm, gpos, gnrm, flags, w, L);
+    e = sums ? launch_adj_main<true>(sms, s, patches, hm, gpos, gnrm, flags, w, L, sums)
+             : launch_adj_main<false>(sms, s, patches, hm, gpos, gnrm, flags, w, L, nullptr);
     if (e != cudaSuccess) return e;
     const dim3 cg((max_waves_per_patch * kAdjRecord + 31) / 32, n_patches < 65535u ? n_patches : 65535u);
     e = launch_pdl(k_adj_cols, cg, dim3(32 * kColLanes), 0, s, n_patches, static_cast<const char*>(ws), L);

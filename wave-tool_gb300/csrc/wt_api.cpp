@@ -129,7 +129,7 @@ wt::FwdConfig cfg_for(uint32_t n_patches, uint32_t n_waves) {
 
 wt_status run_displace(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
                        const wt_heightmap* hm, float* pos, float* nrm, uint64_t cap, uint32_t flags, void* ws,
-                       size_t ws_bytes, cudaStream_t s, const wt::FwdConfig& cfg) {
+                       size_t ws_bytes, cudaStream_t s, const wt::FwdConfig& cfg, float* sums = nullptr) {
     Prepared P;
     wt_status st = check_common(patches, n_patches, waves, n_waves, hm, cap, flags, ws, ws_bytes, &P);
     if (st != WT_OK) return st;
@@ -141,7 +141,7 @@ wt_status run_displace(const wt_patch* patches, uint32_t n_patches, const wt_wav
     if (flags & WT_PHASE_FP32_NAIVE)
         e = wt::launch_forward_naive(patches, n_patches, waves, P.hm, pos, nrm, flags, ws, P.L, cap, s);
     else
-        e = wt::launch_forward(cfg, patches, n_patches, P.hm, pos, nrm, flags, ws, P.L, s);
+        e = wt::launch_forward(cfg, patches, n_patches, P.hm, pos, nrm, flags, ws, P.L, sums, s);
     if (e != cudaSuccess) return cuda_fail(e, "forward launch");
     return WT_OK;
 }
@@ -222,6 +222,17 @@ wt_status wt_gerstner_displace(const wt_patch* patches, uint32_t n_patches, cons
                         workspace, workspace_bytes, (cudaStream_t)stream, cfg_for(n_patches, n_waves));
 }
 
+wt_status wt_gerstner_displace_saving(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
+                                      uint32_t n_waves, const wt_heightmap* hm, float* pos_out, float* nrm_out,
+                                      uint64_t out_capacity, uint32_t flags, float* sums_out, void* workspace,
+                                      size_t workspace_bytes, wt_stream stream) {
+    if (!sums_out || !aligned(sums_out, 16)) return fail(WT_ERR_INVALID_ARG, "sums_out NULL or not 16-byte aligned");
+    if (flags & WT_PHASE_FP32_NAIVE)
+        return fail(WT_ERR_UNSUPPORTED, "saving forward: the FP32-naive phase has no adjoint to save for");
+    return run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags, workspace,
+                        workspace_bytes, (cudaStream_t)stream, cfg_for(n_patches, n_waves), sums_out);
+}
+
 wt_status wt_gerstner_displace_unbatched(const wt_patch* host_patches, const wt_patch* patches,
                                          uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
                                          const wt_heightmap* hm, float* pos_out, float* nrm_out,
@@ -237,10 +248,10 @@ wt_status wt_gerstner_displace_unbatched(const wt_patch* host_patches, const wt_
     return WT_OK;
 }
 
-wt_status wt_gerstner_adjoint(const wt_patch* host_patches, const wt_patch* patches, uint32_t n_patches,
-                              const wt_wave* waves, uint32_t n_waves, const wt_heightmap* hm, const float* d_pos,
-                              const float* d_nrm, uint64_t out_capacity, uint32_t flags, wt_wave_grad* grad_out,
-                              void* workspace, size_t workspace_bytes, wt_stream stream) {
+static wt_status run_adjoint(const wt_patch* host_patches, const wt_patch* patches, uint32_t n_patches,
+                             const wt_wave* waves, uint32_t n_waves, const wt_heightmap* hm, const float* d_pos,
+                             const float* d_nrm, uint64_t out_capacity, uint32_t flags, const float* sums,
+                             wt_wave_grad* grad_out, void* workspace, size_t workspace_bytes, wt_stream stream) {
     if (n_patches > 0 && !host_patches) return fail(WT_ERR_INVALID_ARG, "host_patches is NULL");
     Prepared P;
     wt_status st = check_common(patches, n_patches, waves, n_waves, hm, out_capacity, flags, workspace,
@@ -268,9 +279,27 @@ wt_status wt_gerstner_adjoint(const wt_patch* host_patches, const wt_patch* patc
     uint32_t maxw = 0;
     for (uint32_t i = 0; i < n_patches; ++i) maxw = host_patches[i].wave_count > maxw ? host_patches[i].wave_count : maxw;
     e = wt::launch_adjoint(patches, n_patches, waves, n_waves, maxw > 0 ? maxw : 1, P.hm, d_pos, d_nrm, flags, grad_out,
-                           workspace, L, s);
+                           workspace, L, sums, s);
     if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
     return WT_OK;
+}
+
+wt_status wt_gerstner_adjoint(const wt_patch* host_patches, const wt_patch* patches, uint32_t n_patches,
+                              const wt_wave* waves, uint32_t n_waves, const wt_heightmap* hm, const float* d_pos,
+                              const float* d_nrm, uint64_t out_capacity, uint32_t flags, wt_wave_grad* grad_out,
+                              void* workspace, size_t workspace_bytes, wt_stream stream) {
+    return run_adjoint(host_patches, patches, n_patches, waves, n_waves, hm, d_pos, d_nrm, out_capacity, flags,
+                       nullptr, grad_out, workspace, workspace_bytes, stream);
+}
+
+wt_status wt_gerstner_adjoint_saved(const wt_patch* host_patches, const wt_patch* patches, uint32_t n_patches,
+                                    const wt_wave* waves, uint32_t n_waves, const wt_heightmap* hm,
+                                    const float* d_pos, const float* d_nrm, uint64_t out_capacity, uint32_t flags,
+                                    const float* sums, wt_wave_grad* grad_out, void* workspace,
+                                    size_t workspace_bytes, wt_stream stream) {
+    if (!sums || !aligned(sums, 16)) return fail(WT_ERR_INVALID_ARG, "sums NULL or not 16-byte aligned");
+    return run_adjoint(host_patches, patches, n_patches, waves, n_waves, hm, d_pos, d_nrm, out_capacity, flags,
+                       sums, grad_out, workspace, workspace_bytes, stream);
 }
 
 wt_status wt_grid_indices(uint32_t cols, uint32_t rows, uint32_t base_vertex, uint32_t* idx_out, wt_stream stream) {

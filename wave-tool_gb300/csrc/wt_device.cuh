@@ -132,11 +132,16 @@ struct VertexSums {
     float dx, dy, dz, jx, jz, sxx, sxz, szz;
 };
 
-// Heightmap, bounce, normal, stores for one vertex.
+// Heightmap, bounce, normal, stores for one vertex; with `sums`, also the
+// vertex's eight wave sums (two float4 at 2*vidx) for a later adjoint.
 __device__ __forceinline__ void finish_vertex(const VertexSums& s, float xl, float zl, const PatchAux& a,
                                               const HmDev& hm, bool pow2, uint64_t vidx,
                                               float* __restrict__ pos, float* __restrict__ nrm,
-                                              uint32_t flags) {
+                                              uint32_t flags, float4* __restrict__ sums) {
+    if (sums) {
+        __stcs(sums + 2 * vidx, make_float4(s.dx, s.dy, s.dz, s.jx));
+        __stcs(sums + 2 * vidx + 1, make_float4(s.jz, s.sxx, s.sxz, s.szz));
+    }
     float px0 = 1.0f - s.sxx, px1 = s.jx, px2 = -s.sxz;
     float pz0 = -s.sxz, pz1 = s.jz, pz2 = 1.0f - s.szz;
     float dy = s.dy;

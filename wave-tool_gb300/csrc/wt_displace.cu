@@ -248,13 +248,17 @@ __global__ void __launch_bounds__(256) k_prep_coef(const wt_patch* __restrict__ 
 // EPI = 0: epilogue unrolled over the lane's vertices straight from the
 // accumulator registers; EPI = 1: the sums are parked in shared memory and a
 // single rolled copy of the epilogue runs (smaller code, larger smem carve-out).
-template <int THREADS, int MINB, int SMAX, int EPI>
+// SAVE: also store each vertex's eight wave sums to `sums` (a compile-time
+// switch: a run-time null test in the epilogue cost 4 % of the kernel).
+template <int THREADS, int MINB, int SMAX, int EPI, bool SAVE>
 __global__ void __launch_bounds__(THREADS, MINB)
 k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ pos,
-          float* __restrict__ nrm, uint32_t flags, char* __restrict__ ws, WsLayout L, uint32_t chunk) {
+          float* __restrict__ nrm, uint32_t flags, char* __restrict__ ws, WsLayout L, uint32_t chunk,
+          float4* __restrict__ sums_arg) {
 #if __CUDA_ARCH__ >= 900
     cudaGridDependencySynchronize();
 #endif
+    float4* const sums = SAVE ? sums_arg : nullptr;
     // per warp: wave staging (32 x kStage float4), then the parked sums of
     // the tile's vertices ([j][half][lane] float4, conflict-free)
     extern __shared__ float4 fwd_smem[];
@@ -341,7 +345,7 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
                     const float xl = fmaf(32.0f * (float)j, gx, xb);
                     const float zl = fmaf(32.0f * (float)j, gz, zb);
                     VertexSums s{s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
-                    finish_vertex(s, xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags);
+                    finish_vertex(s, xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums);
                 }
             }
         } else {
@@ -353,7 +357,7 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
                     const float zl = fmaf(32.0f * j, gz, zb);
                     VertexSums s{acc[j][0], acc[j][1], acc[j][2], acc[j][3],
                                  acc[j][4], acc[j][5], acc[j][6], acc[j][7]};
-                    finish_vertex(s, xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags);
+                    finish_vertex(s, xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums);
                 }
             }
         }
@@ -402,14 +406,14 @@ __global__ void __launch_bounds__(256) k_forward_naive(const wt_patch* __restric
                 s.sxz += Q * A * k * w.dir_x * w.dir_z * sn;
                 s.szz += Q * A * k * w.dir_z * w.dir_z * sn;
             }
-            finish_vertex(s, xl, zl, a, hm, pow2, P.out_offset + v, pos, nrm, flags);
+            finish_vertex(s, xl, zl, a, hm, pow2, P.out_offset + v, pos, nrm, flags, nullptr);
         }
     }
 }
 
-template <int THREADS, int MINB, int SMAX, int EPI>
+template <int THREADS, int MINB, int SMAX, int EPI, bool SAVE>
 cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const HmDev& hm, float* pos,
-                         float* nrm, uint32_t flags, void* ws, const WsLayout& L, cudaStream_t s) {
+                         float* nrm, uint32_t flags, void* ws, const WsLayout& L, float* sums, cudaStream_t s) {
     constexpr int kMaxDev = 64;
     static std::atomic<int> occ_cache[kMaxDev];  // resident blocks per SM, per device
     int dev = 0;
@@ -421,10 +425,11 @@ cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const Hm
     int occ = occ_cache[dev].load(std::memory_order_relaxed);
     if (occ == 0) {
         int o = 0;
-        cudaError_t e = cudaFuncSetAttribute(k_forward<THREADS, MINB, SMAX, EPI>,
+        cudaError_t e = cudaFuncSetAttribute(k_forward<THREADS, MINB, SMAX, EPI, SAVE>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_forward<THREADS, MINB, SMAX, EPI>, THREADS, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_forward<THREADS, MINB, SMAX, EPI, SAVE>, THREADS,
+                                                          smem);
         if (e != cudaSuccess) return e;
         occ = o < 1 ? 1 : o;
         occ_cache[dev].store(occ, std::memory_order_relaxed);
@@ -441,8 +446,8 @@ cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const Hm
     lc.attrs = attr;
     lc.numAttrs = 1;
     const uint32_t chunk = cfg.chunk >= 1 && cfg.chunk <= 32 ? (uint32_t)cfg.chunk : 32u;
-    return cudaLaunchKernelEx(&lc, k_forward<THREADS, MINB, SMAX, EPI>, patches, hm, pos, nrm, flags,
-                              static_cast<char*>(ws), L, chunk);
+    return cudaLaunchKernelEx(&lc, k_forward<THREADS, MINB, SMAX, EPI, SAVE>, patches, hm, pos, nrm, flags,
+                              static_cast<char*>(ws), L, chunk, reinterpret_cast<float4*>(sums));
 }
 
 }  // namespace
@@ -479,18 +484,29 @@ bool forward_config_supported(const FwdConfig& c) {
 }
 
 cudaError_t launch_forward(const FwdConfig& cfg, const wt_patch* patches, uint32_t, const HmDev& hm,
-                           float* pos, float* nrm, uint32_t flags, void* ws, const WsLayout& L,
+                           float* pos, float* nrm, uint32_t flags, void* ws, const WsLayout& L, float* sums,
                            cudaStream_t s) {
-    // warps per block; the minimum-blocks hint sets the register budget
+    // warps per block; the minimum-blocks hint sets the register budget.
+    // The saving kernels exist with the register epilogue only: a tuning with
+    // the shared-memory epilogue saves through the register one, same shape.
+    if (sums) {
+        if (cfg.s == 4 && cfg.warps == 8)
+            return launch_fwd_t<256, 3, 4, 0, true>(cfg, patches, hm, pos, nrm, flags, ws, L, sums, s);
+        if (cfg.s == 8 && cfg.warps == 8)
+            return launch_fwd_t<256, 2, 8, 0, true>(cfg, patches, hm, pos, nrm, flags, ws, L, sums, s);
+        if (cfg.s == 8 && cfg.warps == 16)
+            return launch_fwd_t<512, 1, 8, 0, true>(cfg, patches, hm, pos, nrm, flags, ws, L, sums, s);
+        return cudaErrorInvalidValue;
+    }
     if (cfg.s == 4 && cfg.warps == 8 && cfg.epi == 0)
-        return launch_fwd_t<256, 3, 4, 0>(cfg, patches, hm, pos, nrm, flags, ws, L, s);   // 85 regs
+        return launch_fwd_t<256, 3, 4, 0, false>(cfg, patches, hm, pos, nrm, flags, ws, L, nullptr, s);  // 80 regs
     if (cfg.s == 8 && cfg.epi == 0) {
-        if (cfg.warps == 8) return launch_fwd_t<256, 2, 8, 0>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
-        if (cfg.warps == 16) return launch_fwd_t<512, 1, 8, 0>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
+        if (cfg.warps == 8) return launch_fwd_t<256, 2, 8, 0, false>(cfg, patches, hm, pos, nrm, flags, ws, L, nullptr, s);
+        if (cfg.warps == 16) return launch_fwd_t<512, 1, 8, 0, false>(cfg, patches, hm, pos, nrm, flags, ws, L, nullptr, s);
     }
     if (cfg.s == 8 && cfg.epi == 1) {
-        if (cfg.warps == 8) return launch_fwd_t<256, 2, 8, 1>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
-        if (cfg.warps == 16) return launch_fwd_t<512, 1, 8, 1>(cfg, patches, hm, pos, nrm, flags, ws, L, s);
+        if (cfg.warps == 8) return launch_fwd_t<256, 2, 8, 1, false>(cfg, patches, hm, pos, nrm, flags, ws, L, nullptr, s);
+        if (cfg.warps == 16) return launch_fwd_t<512, 1, 8, 1, false>(cfg, patches, hm, pos, nrm, flags, ws, L, nullptr, s);
     }
     return cudaErrorInvalidValue;
 }

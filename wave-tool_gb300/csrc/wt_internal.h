@@ -123,9 +123,10 @@ struct HmDev {
 cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
                         uint32_t n_waves, const HmDev& hm, uint64_t out_capacity,
                         uint32_t tile_cols, void* ws, const WsLayout& L, cudaStream_t s);
+// sums: NULL, or 8 floats per output vertex (its wave sums, for the adjoint)
 cudaError_t launch_forward(const FwdConfig& cfg, const wt_patch* patches, uint32_t n_patches,
                            const HmDev& hm, float* pos, float* nrm, uint32_t flags, void* ws,
-                           const WsLayout& L, cudaStream_t s);
+                           const WsLayout& L, float* sums, cudaStream_t s);
 cudaError_t launch_forward_naive(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
                                  const HmDev& hm, float* pos, float* nrm, uint32_t flags,
                                  void* ws, const WsLayout& L, uint64_t total_vertices,
@@ -135,9 +136,11 @@ bool forward_config_supported(const FwdConfig& cfg);
 // ---- adjoint (wt_adjoint.cu) ----------------------------------------------
 // Records (tiles x waves) of one patch, as the adjoint lays them out.
 uint64_t adjoint_records(const wt_patch& p);
+// sums: NULL (phase 1 recomputes the forward sums) or the forward's saved sums
 cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
                            uint32_t max_waves_per_patch, const HmDev& hm, const float* gpos, const float* gnrm,
-                           uint32_t flags, wt_wave_grad* grad, void* ws, const AdjLayout& L, cudaStream_t s);
+                           uint32_t flags, wt_wave_grad* grad, void* ws, const AdjLayout& L, const float* sums,
+                           cudaStream_t s);
 
 // ---- host helpers (wt_api.cpp) ---------------------------------------------
 void set_last_error(const char* msg);  // message returned by wt_last_error() on this thread

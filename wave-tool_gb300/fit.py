@@ -1,8 +1,9 @@
 """Fitting wave parameters to a target surface with the forward/adjoint pair.
 
 `GerstnerFunction` is a torch.autograd.Function whose forward is
-wt_gerstner_displace and whose backward is wt_gerstner_adjoint (both through
-the C ABI); torch only carries the tensors and the optimiser.  `fit_waves`
+wt_gerstner_displace_saving (the outputs plus each vertex's wave sums, kept as
+the saved activation) and whose backward is wt_gerstner_adjoint_saved (both
+through the C ABI); torch only carries the tensors and the optimiser.  `fit_waves`
 runs Adam on (log A, log lambda, direction angle, log Q, phase) against an
 L2 height + normal loss — the adjoint-fit configuration (512 x 512 grid,
 16 hidden waves, 10 % / 10 degree / 0.5 rad perturbed start, 500 steps).
@@ -42,8 +43,10 @@ class GerstnerFunction:
                 @staticmethod
                 def forward(ctx, w, surf, fl):
                     surf.waves.copy_(w.detach().contiguous().view(torch.uint8).reshape(-1))
-                    pos, nrm = surf.displace(flags=fl)
+                    sums = torch.empty((surf.n_vertices, 8), dtype=torch.float32, device=w.device)
+                    pos, nrm = surf.displace(flags=fl, sums=sums)
                     ctx.surf, ctx.flags = surf, fl
+                    ctx.save_for_backward(sums)
                     return pos, nrm
 
                 @staticmethod
@@ -51,8 +54,9 @@ class GerstnerFunction:
                     surf = ctx.surf
                     gpos = gpos.contiguous() if gpos is not None else torch.zeros(
                         (surf.n_vertices, 4), device=surf.patches.device)
+                    (sums,) = ctx.saved_tensors
                     g = surf.adjoint(gpos, None if gnrm is None else gnrm.contiguous(),
-                                     flags=ctx.flags & WT_LAYOUT_VEC3)
+                                     flags=ctx.flags & WT_LAYOUT_VEC3, sums=sums)
                     out = torch.zeros((surf.n_waves, 8), dtype=torch.float32, device=g.device)
                     for dst, src in enumerate(_GRAD_TO_WAVE):
                         out[:, dst] = g[:, src]
