@@ -125,10 +125,11 @@ def traffic_from_profile():
     return float(m.group(1)) if m else None
 
 
-def cpu_sample(w, target_s: float, threads: int):
+def cpu_sample(w, target_s: float, threads: int, analytic: bool = False):
     """Runs the oracle's FP32 restatement of the reference shader (5 surface
-    evaluations per vertex, central-difference normals) over the first rows
-    of every patch, rows chosen so the run lasts about target_s."""
+    evaluations per vertex, central-difference normals; with `analytic`, one
+    evaluation per vertex with Jacobian normals) over the first rows of every
+    patch, rows chosen so the run lasts about target_s."""
     from oracle import oracle as O
     import types
     hmp = None
@@ -138,11 +139,11 @@ def cpu_sample(w, target_s: float, threads: int):
         hmp = types.SimpleNamespace(sample_scale=w.heightmap.sample_scale, disp_scale=w.heightmap.disp_scale,
                                     wrap=w.heightmap.wrap)
     t0 = time.perf_counter()
-    O.cpu_baseline(w.patches, w.waves, tex, hmp, row_limit=1, threads=threads)
+    O.cpu_baseline(w.patches, w.waves, tex, hmp, row_limit=1, threads=threads, analytic=analytic)
     probe = time.perf_counter() - t0
     rows = max(1, min(int(target_s / max(probe, 1e-3)), int(w.patches["rows"].max())))
     t0 = time.perf_counter()
-    nv, _, _ = O.cpu_baseline(w.patches, w.waves, tex, hmp, row_limit=rows, threads=threads)
+    nv, _, _ = O.cpu_baseline(w.patches, w.waves, tex, hmp, row_limit=rows, threads=threads, analytic=analytic)
     dt = time.perf_counter() - t0
     terms = int(sum(min(rows, int(p["rows"])) * int(p["cols"]) * int(p["wave_count"]) for p in w.patches))
     return terms / dt, dt, rows, terms
@@ -237,10 +238,13 @@ def build_frame(wt, workloads):
         wt.water_shade(frags, outs["clip"], idx, outs, VW, VH, shading, sky, local_reflections=lrefl,
                        local_refractions=lrefr, colour=colour)
 
-    def frame(s=None):
+    def frame(s=None, fused=True):
         wt.projected_grid_async(cam_dev, surf.patches, view_dev, stream=s)
-        surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD, stream=s)
-        wt.vertex_stage(view_dev, pos, nrm, out=outs, stream=s)
+        if fused:   # the vertex stage in the displacement's epilogue
+            surf.displace_stage(view_dev, out=outs, stream=s)
+        else:
+            surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD, stream=s)
+            wt.vertex_stage(view_dev, pos, nrm, out=outs, stream=s)
         wt.water_raster(outs["clip"], idx, VW, VH, fragments=frags, workspace=rws, stream=s)
         wt.water_shade(frags, outs["clip"], idx, outs, VW, VH, shading, sky, local_reflections=lrefl,
                        local_refractions=lrefr, colour=colour, stream=s)
@@ -248,30 +252,38 @@ def build_frame(wt, workloads):
     return dict(frame=frame, raster=raster, shade=shade, n=n, waves=len(w.waves), VW=VW, VH=VH, frags=frags,
                 projected_grid=lambda: wt.projected_grid_async(cam_dev, surf.patches, view_dev),
                 displace=lambda: surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD),
-                vertex_stage=lambda: wt.vertex_stage(view_dev, pos, nrm, out=outs))
+                vertex_stage=lambda: wt.vertex_stage(view_dev, pos, nrm, out=outs),
+                displace_stage=lambda: surf.displace_stage(view_dev, out=outs))
 
 
 def frame_pipeline(wt, workloads, stream, flush):
-    """The frame of build_frame replayed as one CUDA graph, and each stage
-    alone (the vertex stage against HBM)."""
+    """The frame of build_frame replayed as one CUDA graph (the vertex stage
+    fused into the displacement, and as its own kernel), and each stage alone
+    (the stand-alone vertex stage against HBM)."""
     import torch
     F = build_frame(wt, workloads)
     frame, raster, shade, n, VW, VH, frags = (F[k] for k in ("frame", "raster", "shade", "n", "VW", "VH", "frags"))
-    for _ in range(3):
-        frame()
-    torch.cuda.synchronize()
-    side = torch.cuda.Stream()
-    side.wait_stream(stream)
-    g = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g, stream=side):
-        frame(side)
-    for _ in range(3):
-        g.replay()
-    torch.cuda.synchronize()
-    fms = _event_ms(g.replay, 20, stream, flush)
+    graph_ms = {}
+    for fused in (True, False):
+        for _ in range(3):
+            frame(fused=fused)
+        torch.cuda.synchronize()
+        side = torch.cuda.Stream()
+        side.wait_stream(stream)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            frame(side, fused=fused)
+        for _ in range(3):
+            g.replay()
+        torch.cuda.synchronize()
+        graph_ms[fused] = _event_ms(g.replay, 20, stream, flush)
+        del g
+    fms = graph_ms[True]
+    frame()  # leave the fused frame's pixels in frags
     gms = _event_ms(F["projected_grid"], 20, stream, flush)
     dms = _event_ms(F["displace"], 20, stream, flush)
     vms = _event_ms(F["vertex_stage"], 20, stream, flush)
+    fsms = _event_ms(F["displace_stage"], 20, stream, flush)
     rms = _event_ms(raster, 20, stream, flush)
     sms = _event_ms(shade, 20, stream, flush)
     covered = float(((frags & 0xffffffff) != 0).float().mean())
@@ -282,7 +294,8 @@ def frame_pipeline(wt, workloads, stream, flush):
     except (OSError, KeyError, ValueError):
         hbm_peak, peak_src = 6800.0, "fallback 6.8 TB/s"
     return {"vertices": n, "terms": n * F["waves"], "viewport": [VW, VH], "water_pixels_frac": covered,
-            "frame_graph_ms": fms, "raster_ms": rms, "shade_ms": sms,
+            "frame_graph_ms": fms, "frame_graph_unfused_ms": graph_ms[False], "raster_ms": rms, "shade_ms": sms,
+            "displace_with_fused_stage_ms": fsms,
             "frames_per_s": 1e3 / fms, "projected_grid_kernel_ms": gms, "displace_ms": dms,
             "vertex_stage_ms": vms, "vertex_stage_bytes": stage_bytes,
             "vertex_stage_gbs": stage_bytes / (vms * 1e-3) / 1e9,
@@ -544,6 +557,15 @@ def run_ours(args):
         cpu = {"value": r, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                "sample": f"first {rows} rows of each of the {args.patches} patches ({cterms} terms, {dt:.1f} s); "
                          "FP32 restatement of water-grid.vert, 5 evaluations/vertex"}
+        # beside it: the same restatement on one thread, and the analytic form
+        # (one evaluation per vertex, Jacobian normals) on every core
+        short = max(1.0, args.cpu_seconds / 4)
+        r1, _, rows1, _ = cpu_sample(w, short, 1)
+        ra, _, rowsa, _ = cpu_sample(w, short, os.cpu_count() or 1, analytic=True)
+        cpu["single_thread_value"] = r1
+        cpu["analytic_value"] = ra
+        cpu["analytic_note"] = (f"one evaluation per vertex, Jacobian normals, {os.cpu_count() or 1} threads, "
+                                f"first {rowsa} rows per patch; single thread: first {rows1} rows per patch")
 
     if rank == 0:
         clocks = clk.summary()

@@ -360,6 +360,33 @@ wt_status wt_vertex_stage(const wt_view* view, const float* pos, const float* nr
                           uint32_t flags, float* clip_out, float* ndc0_out, float* view_out,
                           float* facing_out, float* nrm_yaw_out, wt_stream stream);
 
+/* Vertex-stage output buffers (device, any may be NULL), as wt_vertex_stage
+ * writes them: clip float4, ndc0 float2, view / facing / nrm_yaw float4. */
+typedef struct wt_stage_outputs {
+    float* clip;
+    float* ndc0;
+    float* view;
+    float* facing;
+    float* nrm_yaw;
+} wt_stage_outputs;
+
+/* wt_gerstner_displace with wt_vertex_stage fused into its epilogue: each
+ * vertex's clip position, NDC at height 0, view vector, camera-facing normal
+ * and yaw-only normal (water-grid.vert:150-158, :190-193) are computed from
+ * the world position and normal in registers and written straight to
+ * `outputs` (float4 / float2 layouts), bit-identical to wt_vertex_stage on
+ * the positions and normals wt_gerstner_displace writes.  pos_out and nrm_out
+ * may each be NULL (that output is then not written); flags: 0 or
+ * WT_LAYOUT_VEC3 (the layout of pos_out / nrm_out only); WT_OUT_DISPLACEMENT and WT_PHASE_FP32_NAIVE are
+ * refused.  view: device wt_view (e.g. from wt_projected_grid_async on the
+ * same stream). */
+wt_status wt_gerstner_displace_stage(const wt_patch* patches, uint32_t n_patches,
+                                     const wt_wave* waves, uint32_t n_waves,
+                                     const wt_heightmap* hm, const wt_view* view,
+                                     float* pos_out, float* nrm_out, uint64_t out_capacity,
+                                     uint32_t flags, const wt_stage_outputs* outputs,
+                                     void* workspace, size_t workspace_bytes, wt_stream stream);
+
 /* ---- water shading (the fragment stage) ---------------------------------- */
 
 /* Uniforms of the water fragment shader (assets/shaders/water-grid.frag:34-53),
@@ -469,13 +496,14 @@ wt_status wt_wave_from_reference(float amplitude_A, float frequency_w,
  * launches issued after it is set.  No reference counterpart (the reference
  * has one fixed draw call). */
 typedef struct wt_tuning {
-    uint32_t warps_per_block; /* 4, 6, 8 or 16 (0 = default 8) */
+    uint32_t warps_per_block; /* 8 or 16 (0 = 16) */
     uint32_t blocks_per_sm;   /* 0 = as many as fit */
     uint32_t wave_chunk;      /* waves staged per warp at a time: 8, 16 or 32 (0 = 32) */
     uint32_t max_vertices_per_lane; /* widest tile = 32 * this; 4 or 8 (0 = 8).  4 halves
                                        the accumulator registers for more resident warps */
     uint32_t epilogue_in_shared;    /* 1: per-vertex epilogue as one rolled loop over sums
-                                       parked in shared memory; 0: unrolled from registers */
+                                       parked in shared memory; 0: unrolled from registers.
+                                       The saving and vertex-stage forwards always use 0. */
 } wt_tuning;
 
 /* The default shape (used where the autotuner has not run); setting it also

@@ -61,6 +61,31 @@ def test_struct_layouts_match_c(wt, tmp_path):
             assert dt.fields[f][1] == int(v), (s, f)
 
 
+def test_ctypes_layouts_match_c(wt, tmp_path):
+    """offsetof/sizeof of the structs the host layer passes by pointer through
+    ctypes equal the ctypes mirrors."""
+    checks = {"wt_heightmap": wt.CHeightmap, "wt_tuning": wt.CTuning, "wt_water_shading": wt.CWaterShading,
+              "wt_water_textures": wt.CWaterTextures, "wt_stage_outputs": wt.CStageOutputs}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void) {"]
+    for s, S in checks.items():
+        lines.append(f'printf("{s} sizeof %zu\\n", sizeof({s}));')
+        for f, _ in S._fields_:
+            lines.append(f'printf("{s} {f} %zu\\n", offsetof({s}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout_ctypes.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout_ctypes"
+    subprocess.run(["gcc", "-o", str(exe), str(src)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    for line in filter(None, out):
+        s, f, v = line.split()
+        S = checks[s]
+        if f == "sizeof":
+            assert C.sizeof(S) == int(v), s
+        else:
+            assert getattr(S, f).offset == int(v), (s, f)
+
+
 def test_wave_from_reference_applies_q_normalisation(wt, built):
     """render-engine.cpp:1073: Q_i = Q / (w * A * count) in FP32, 0 if w*A = 0."""
     w = wt.wave_from_reference(0.06, 1.0, 2.0, 1.0, 1.0, 0.0, 4)[0]

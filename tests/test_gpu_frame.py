@@ -141,6 +141,50 @@ def test_vertex_stage_against_f64(wt, oracle, gpu, pitch):
     assert np.array_equal(nrm.cpu().numpy(), got["facing"])
 
 
+@pytest.mark.parametrize("tuning", [None, dict(warps_per_block=8, max_vertices_per_lane=4, epilogue_in_shared=0),
+                                    dict(warps_per_block=16, max_vertices_per_lane=8, epilogue_in_shared=1)])
+def test_fused_vertex_stage_bit_identical(wt, gpu, tuning):
+    """wt_gerstner_displace_stage (the vertex stage in the forward's epilogue)
+    writes the same bits as wt_gerstner_displace followed by wt_vertex_stage,
+    with and without the positions and normals, under each launch shape (the
+    shared-memory epilogue shape runs its register twin)."""
+    import torch
+    cam = wt.camera(position=(3.0, 6.0, 20.0), yaw_deg=-80.0, pitch_deg=-20.0, aspect=1.6,
+                    displaceable_amplitude=2.0)
+    surf, view = frame_surface(wt, cam, side=301, n_waves=24)
+    vd = dev_view(wt, view)
+    old = wt.get_tuning()
+    try:
+        if tuning is not None:
+            wt.set_tuning(**tuning)
+        pos, nrm = surf.displace(flags=wt.WT_OUT_WORLD)
+        ref = wt.vertex_stage(vd, pos, nrm)
+        fpos, fnrm = torch.full_like(pos, 7.0), torch.full_like(nrm, 7.0)
+        fused = surf.displace_stage(vd, pos=fpos, nrm=fnrm)
+        bare = surf.displace_stage(vd)
+        pos3, nrm3 = surf.alloc_outputs(wt.WT_LAYOUT_VEC3)
+        only_n = torch.full_like(nrm3, 7.0)
+        surf.displace_stage(vd, pos=None, nrm=only_n, flags=wt.WT_LAYOUT_VEC3, stage=("clip",))
+        torch.cuda.synchronize()
+    finally:
+        wt.set_tuning(**old)
+    assert surf.status()[0] == 0
+    assert torch.equal(fpos, pos) and torch.equal(fnrm, nrm)
+    for k in ("clip", "ndc0", "view", "facing", "nrm_yaw"):
+        assert torch.equal(fused[k], ref[k]), k
+        assert torch.equal(bare[k], ref[k]), k
+    assert torch.equal(only_n, nrm[:, :3])
+
+
+def test_fused_vertex_stage_validation(wt, gpu):
+    surf, view = frame_surface(wt, wt.camera(position=(0.0, 4.0, 30.0), displaceable_amplitude=1.0), side=33)
+    vd = dev_view(wt, view)
+    with pytest.raises(wt.WtError):
+        surf.displace_stage(vd, flags=wt.WT_OUT_DISPLACEMENT)
+    with pytest.raises(wt.WtError):
+        surf.displace_stage(vd, flags=wt.WT_PHASE_FP32_NAIVE)
+
+
 def test_vertex_stage_reproduces_reference_shader(wt, gpu):
     """Fed the reference shader's own positions and (flipped) normals, the
     kernel reproduces its clip position, NDC at height 0, view vector and
@@ -228,10 +272,12 @@ def test_camera_to_vertices_frame_graph(wt, gpu):
             assert float((replayed[k] - eout[k]).abs().max()) <= 1e-4 * max(1.0, float(eout[k].abs().max())), k
 
 
-def test_camera_to_pixels_frame_graph(wt, gpu):
+@pytest.mark.parametrize("fused", [False, True])
+def test_camera_to_pixels_frame_graph(wt, gpu, fused):
     """The whole water pass (projected grid -> displacement -> vertex stage ->
     rasterisation -> shading) captured once; replayed with new cameras it gives
-    the same pixels as the same calls made eagerly."""
+    the same pixels as the same calls made eagerly.  fused: the vertex stage
+    in the displacement's epilogue (wt_gerstner_displace_stage)."""
     import torch
     VW, VH = 160, 100
     cams = [wt.camera(position=(0.0, 4.0, 70.0), pitch_deg=-15.0, aspect=VW / VH, displaceable_amplitude=1.5),
@@ -254,8 +300,11 @@ def test_camera_to_pixels_frame_graph(wt, gpu):
 
     def frame(stream=None):
         wt.projected_grid_async(cam_dev, surf.patches, view_dev, stream=stream)
-        surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD, stream=stream)
-        wt.vertex_stage(view_dev, pos, nrm, out=outs, stream=stream)
+        if fused:
+            surf.displace_stage(view_dev, out=outs, stream=stream)
+        else:
+            surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD, stream=stream)
+            wt.vertex_stage(view_dev, pos, nrm, out=outs, stream=stream)
         wt.water_raster(outs["clip"], idx, VW, VH, fragments=frags, workspace=rws, stream=stream)
         wt.water_shade(frags, outs["clip"], idx, outs, VW, VH, shading, sky, local_reflections=refl,
                        colour=colour, stream=stream)

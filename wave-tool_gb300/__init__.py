@@ -35,7 +35,7 @@ EXPORTED = [
     "wt_measure_peaks", "wt_set_tuning", "wt_get_tuning", "wt_autotune_displace",
     "wt_projected_grid", "wt_projected_grid_async", "wt_vertex_stage", "wt_heightmap_from_unorm8",
     "wt_water_raster", "wt_water_raster_workspace_size", "wt_water_shade",
-    "wt_gerstner_displace_saving", "wt_gerstner_adjoint_saved",
+    "wt_gerstner_displace_saving", "wt_gerstner_adjoint_saved", "wt_gerstner_displace_stage",
 ]
 
 
@@ -66,6 +66,10 @@ class CWaterShading(C.Structure):
 class CWaterTextures(C.Structure):
     _fields_ = [("scene_depth", C.c_void_p), ("local_reflections", C.c_void_p), ("local_refractions", C.c_void_p),
                 ("skybox", C.c_void_p), ("skybox_size", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+class CStageOutputs(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("clip", "ndc0", "view", "facing", "nrm_yaw")]
 
 
 # the reference's water shading defaults (render-engine.h:221-235, Z_NEAR / Z_FAR)
@@ -111,6 +115,8 @@ def lib():
                                                   vp, sz, vp]
         L.wt_gerstner_adjoint_saved.argtypes = [vp, vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, u64, u32, vp,
                                                 vp, vp, sz, vp]
+        L.wt_gerstner_displace_stage.argtypes = [vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, vp, u64, u32,
+                                                 C.POINTER(CStageOutputs), vp, sz, vp]
         L.wt_grid_indices.argtypes = [u32, u32, u32, vp, vp]
         L.wt_noise_synth.argtypes = [vp, u32, u32, u32, vp, vp, sz, vp]
         L.wt_wave_from_reference.argtypes = [C.c_float] * 6 + [u32, C.POINTER(CWave)]
@@ -263,6 +269,26 @@ class Surface:
                 pos.data_ptr(), _ptr(nrm), cap, flags, self.workspace.data_ptr(), self.workspace.numel(),
                 stream_handle(stream)))
         return pos, nrm
+
+    def displace_stage(self, view_dev, out=None, pos=None, nrm=None, flags: int = 0, stream=None,
+                       stage=("clip", "ndc0", "view", "facing", "nrm_yaw")) -> dict:
+        """wt_gerstner_displace_stage: the displacement with the vertex stage
+        fused into its epilogue.  Returns the dict of (new or given) stage
+        outputs (float4, ndc0 float2); pos / nrm are written only if given."""
+        torch = _torch()
+        n = self.n_vertices
+        out = dict(out or {})
+        for k in stage:
+            if k not in out:
+                out[k] = torch.empty((n, 2 if k == "ndc0" else 4), dtype=torch.float32, device=self.patches.device)
+        so = CStageOutputs(*[_ptr(out.get(k)) for k in ("clip", "ndc0", "view", "facing", "nrm_yaw")])
+        hm = self.heightmap.cstruct() if self.heightmap is not None else None
+        hmp = C.byref(hm) if hm is not None else None
+        check(lib().wt_gerstner_displace_stage(
+            self.patches.data_ptr(), self.n_patches, self.waves.data_ptr(), self.n_waves, hmp, view_dev.data_ptr(),
+            _ptr(pos), _ptr(nrm), n, flags, C.byref(so), self.workspace.data_ptr(), self.workspace.numel(),
+            stream_handle(stream)))
+        return out
 
     def status(self, stream=None):
         return workspace_status(self.workspace, stream)

@@ -129,19 +129,24 @@ wt::FwdConfig cfg_for(uint32_t n_patches, uint32_t n_waves) {
 
 wt_status run_displace(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
                        const wt_heightmap* hm, float* pos, float* nrm, uint64_t cap, uint32_t flags, void* ws,
-                       size_t ws_bytes, cudaStream_t s, const wt::FwdConfig& cfg, float* sums = nullptr) {
+                       size_t ws_bytes, cudaStream_t s, const wt::FwdConfig& cfg,
+                       const wt::FwdExtra& extra = wt::FwdExtra{}) {
     Prepared P;
     wt_status st = check_common(patches, n_patches, waves, n_waves, hm, cap, flags, ws, ws_bytes, &P);
     if (st != WT_OK) return st;
-    st = check_outputs(pos, nrm, flags);
-    if (st != WT_OK) return st;
+    if (!(extra.view && !pos)) {  // the fused vertex stage may leave out the positions
+        st = check_outputs(pos, nrm, flags);
+        if (st != WT_OK) return st;
+    } else if (nrm && !aligned(nrm, (flags & WT_LAYOUT_VEC3) ? 4 : 16)) {
+        return fail(WT_ERR_INVALID_ARG, "nrm_out misaligned for its layout");
+    }
     if (n_patches == 0) return WT_OK;
     cudaError_t e = wt::launch_prep(patches, n_patches, waves, n_waves, P.hm, cap, 32u * cfg.s, ws, P.L, s);
     if (e != cudaSuccess) return cuda_fail(e, "prep launch");
     if (flags & WT_PHASE_FP32_NAIVE)
         e = wt::launch_forward_naive(patches, n_patches, waves, P.hm, pos, nrm, flags, ws, P.L, cap, s);
     else
-        e = wt::launch_forward(cfg, patches, n_patches, P.hm, pos, nrm, flags, ws, P.L, sums, s);
+        e = wt::launch_forward(cfg, patches, n_patches, P.hm, pos, nrm, flags, ws, P.L, extra, s);
     if (e != cudaSuccess) return cuda_fail(e, "forward launch");
     return WT_OK;
 }
@@ -229,8 +234,31 @@ wt_status wt_gerstner_displace_saving(const wt_patch* patches, uint32_t n_patche
     if (!sums_out || !aligned(sums_out, 16)) return fail(WT_ERR_INVALID_ARG, "sums_out NULL or not 16-byte aligned");
     if (flags & WT_PHASE_FP32_NAIVE)
         return fail(WT_ERR_UNSUPPORTED, "saving forward: the FP32-naive phase has no adjoint to save for");
+    wt::FwdExtra x{};
+    x.sums = sums_out;
     return run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags, workspace,
-                        workspace_bytes, (cudaStream_t)stream, cfg_for(n_patches, n_waves), sums_out);
+                        workspace_bytes, (cudaStream_t)stream, cfg_for(n_patches, n_waves), x);
+}
+
+wt_status wt_gerstner_displace_stage(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
+                                     uint32_t n_waves, const wt_heightmap* hm, const wt_view* view,
+                                     float* pos_out, float* nrm_out, uint64_t out_capacity, uint32_t flags,
+                                     const wt_stage_outputs* outputs, void* workspace, size_t workspace_bytes,
+                                     wt_stream stream) {
+    if (!view || !aligned(view, 4)) return fail(WT_ERR_INVALID_ARG, "view NULL or not 4-byte aligned");
+    if (!outputs) return fail(WT_ERR_INVALID_ARG, "outputs is NULL");
+    if (flags & (WT_OUT_DISPLACEMENT | WT_PHASE_FP32_NAIVE))
+        return fail(WT_ERR_INVALID_ARG, "displace_stage: the vertex stage needs world positions and the FP64 phase");
+    if (outputs->clip && !aligned(outputs->clip, 16)) return fail(WT_ERR_INVALID_ARG, "clip not 16-byte aligned");
+    if (outputs->ndc0 && !aligned(outputs->ndc0, 8)) return fail(WT_ERR_INVALID_ARG, "ndc0 not 8-byte aligned");
+    const float* f4[3] = {outputs->view, outputs->facing, outputs->nrm_yaw};
+    for (const float* q : f4)
+        if (q && !aligned(q, 16)) return fail(WT_ERR_INVALID_ARG, "view / facing / nrm_yaw not 16-byte aligned");
+    wt::FwdExtra x{};
+    x.view = view;
+    x.stage = wt::StageOut{outputs->clip, outputs->ndc0, outputs->view, outputs->facing, outputs->nrm_yaw};
+    return run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags, workspace,
+                        workspace_bytes, (cudaStream_t)stream, cfg_for(n_patches, n_waves), x);
 }
 
 wt_status wt_gerstner_displace_unbatched(const wt_patch* host_patches, const wt_patch* patches,

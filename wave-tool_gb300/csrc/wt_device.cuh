@@ -6,6 +6,7 @@
 #include <cstdint>
 
 #include "wt_internal.h"
+#include "wt_stage.cuh"
 
 namespace wt {
 namespace dev {
@@ -132,13 +133,22 @@ struct VertexSums {
     float dx, dy, dz, jx, jz, sxx, sxz, szz;
 };
 
-// Heightmap, bounce, normal, stores for one vertex; with `sums`, also the
-// vertex's eight wave sums (two float4 at 2*vidx) for a later adjoint.
+// What the forward's epilogue writes besides position and normal.
+enum FwdMode : int {
+    kModePlain = 0,  // positions and normals
+    kModeSave = 1,   // also the vertex's eight wave sums (two float4 at 2*vidx) for a later adjoint
+    kModeStage = 2,  // also the vertex-stage outputs (pos and nrm optional; world positions)
+};
+
+// Heightmap, bounce, normal, stores for one vertex.  su: the 36 floats of
+// wt_view in shared memory (kModeStage only).
+template <int MODE>
 __device__ __forceinline__ void finish_vertex(const VertexSums& s, float xl, float zl, const PatchAux& a,
                                               const HmDev& hm, bool pow2, uint64_t vidx,
                                               float* __restrict__ pos, float* __restrict__ nrm,
-                                              uint32_t flags, float4* __restrict__ sums) {
-    if (sums) {
+                                              uint32_t flags, float4* __restrict__ sums,
+                                              const float* __restrict__ su, const StageOut& so) {
+    if (MODE == kModeSave) {
         __stcs(sums + 2 * vidx, make_float4(s.dx, s.dy, s.dz, s.jx));
         __stcs(sums + 2 * vidx + 1, make_float4(s.jz, s.sxx, s.sxz, s.szz));
     }
@@ -160,17 +170,28 @@ __device__ __forceinline__ void finish_vertex(const VertexSums& s, float xl, flo
     float ox, oz, ow;
     if (flags & WT_OUT_DISPLACEMENT) { ox = s.dx; oz = s.dz; ow = 0.0f; }
     else { ox = a.blx + (xl + s.dx); oz = a.blz + (zl + s.dz); ow = 1.0f; }
-    if (flags & WT_LAYOUT_VEC3) {
-        float* P = pos + 3 * vidx;
-        __stcs(P, ox); __stcs(P + 1, dy); __stcs(P + 2, oz);
-        if (nrm) {
+    if (MODE != kModeStage || pos) {
+        if (flags & WT_LAYOUT_VEC3) {
+            float* P = pos + 3 * vidx;
+            __stcs(P, ox); __stcs(P + 1, dy); __stcs(P + 2, oz);
+            if (nrm) {
+                float* N = nrm + 3 * vidx;
+                __stcs(N, n0 * inv); __stcs(N + 1, n1 * inv); __stcs(N + 2, n2 * inv);
+            }
+        } else {
+            __stcs(reinterpret_cast<float4*>(pos) + vidx, make_float4(ox, dy, oz, ow));
+            if (nrm) __stcs(reinterpret_cast<float4*>(nrm) + vidx, make_float4(n0 * inv, n1 * inv, n2 * inv, 0.0f));
+        }
+    } else if (nrm) {
+        if (flags & WT_LAYOUT_VEC3) {
             float* N = nrm + 3 * vidx;
             __stcs(N, n0 * inv); __stcs(N + 1, n1 * inv); __stcs(N + 2, n2 * inv);
+        } else {
+            __stcs(reinterpret_cast<float4*>(nrm) + vidx, make_float4(n0 * inv, n1 * inv, n2 * inv, 0.0f));
         }
-    } else {
-        __stcs(reinterpret_cast<float4*>(pos) + vidx, make_float4(ox, dy, oz, ow));
-        if (nrm) __stcs(reinterpret_cast<float4*>(nrm) + vidx, make_float4(n0 * inv, n1 * inv, n2 * inv, 0.0f));
     }
+    if (MODE == kModeStage)
+        stage_vertex<false>(su, make_float3(ox, dy, oz), make_float3(n0 * inv, n1 * inv, n2 * inv), vidx, so);
 }
 
 __device__ __forceinline__ uint32_t hi32_round(unsigned long long x) {

@@ -248,21 +248,29 @@ __global__ void __launch_bounds__(256) k_prep_coef(const wt_patch* __restrict__ 
 // EPI = 0: epilogue unrolled over the lane's vertices straight from the
 // accumulator registers; EPI = 1: the sums are parked in shared memory and a
 // single rolled copy of the epilogue runs (smaller code, larger smem carve-out).
-// SAVE: also store each vertex's eight wave sums to `sums` (a compile-time
-// switch: a run-time null test in the epilogue cost 4 % of the kernel).
-template <int THREADS, int MINB, int SMAX, int EPI, bool SAVE>
+// MODE (FwdMode): kModeSave also stores each vertex's eight wave sums to `sums`,
+// kModeStage the vertex-stage outputs of `view` (a compile-time switch: a
+// run-time null test of the sums pointer in the epilogue cost 4 % of the
+// kernel).
+template <int THREADS, int MINB, int SMAX, int EPI, int MODE>
 __global__ void __launch_bounds__(THREADS, MINB)
 k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ pos,
           float* __restrict__ nrm, uint32_t flags, char* __restrict__ ws, WsLayout L, uint32_t chunk,
-          float4* __restrict__ sums_arg) {
+          float4* __restrict__ sums_arg, const wt_view* __restrict__ view, StageOut so) {
 #if __CUDA_ARCH__ >= 900
     cudaGridDependencySynchronize();
 #endif
-    float4* const sums = SAVE ? sums_arg : nullptr;
+    float4* const sums = MODE == kModeSave ? sums_arg : nullptr;
     // per warp: wave staging (32 x kStage float4), then the parked sums of
-    // the tile's vertices ([j][half][lane] float4, conflict-free)
+    // the tile's vertices ([j][half][lane] float4, conflict-free); after the
+    // warps' parts, the 36 floats of the view (kModeStage)
     extern __shared__ float4 fwd_smem[];
     float4* const wbase = fwd_smem + (threadIdx.x >> 5) * (32 * kStage + EPI * SMAX * 2 * 32);
+    float* const su = reinterpret_cast<float*>(fwd_smem + (THREADS / 32) * (32 * kStage + EPI * SMAX * 2 * 32));
+    if (MODE == kModeStage) {
+        if (threadIdx.x < 36) su[threadIdx.x] = reinterpret_cast<const float*>(view)[threadIdx.x];
+        __syncthreads();
+    }
     WsHeader* hdr = reinterpret_cast<WsHeader*>(ws);
     const uint32_t* sorted = reinterpret_cast<const uint32_t*>(ws + L.sorted);
     const uint32_t* tile_pre = reinterpret_cast<const uint32_t*>(ws + L.tile_pre);
@@ -345,7 +353,7 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
                     const float xl = fmaf(32.0f * (float)j, gx, xb);
                     const float zl = fmaf(32.0f * (float)j, gz, zb);
                     VertexSums s{s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
-                    finish_vertex(s, xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums);
+                    finish_vertex<MODE>(s, xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums, su, so);
                 }
             }
         } else {
@@ -357,7 +365,7 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
                     const float zl = fmaf(32.0f * j, gz, zb);
                     VertexSums s{acc[j][0], acc[j][1], acc[j][2], acc[j][3],
                                  acc[j][4], acc[j][5], acc[j][6], acc[j][7]};
-                    finish_vertex(s, xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums);
+                    finish_vertex<MODE>(s, xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums, su, so);
                 }
             }
         }
@@ -406,14 +414,15 @@ __global__ void __launch_bounds__(256) k_forward_naive(const wt_patch* __restric
                 s.sxz += Q * A * k * w.dir_x * w.dir_z * sn;
                 s.szz += Q * A * k * w.dir_z * w.dir_z * sn;
             }
-            finish_vertex(s, xl, zl, a, hm, pow2, P.out_offset + v, pos, nrm, flags, nullptr);
+            finish_vertex<kModePlain>(s, xl, zl, a, hm, pow2, P.out_offset + v, pos, nrm, flags, nullptr, nullptr,
+                                  StageOut{});
         }
     }
 }
 
-template <int THREADS, int MINB, int SMAX, int EPI, bool SAVE>
+template <int THREADS, int MINB, int SMAX, int EPI, int MODE>
 cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const HmDev& hm, float* pos,
-                         float* nrm, uint32_t flags, void* ws, const WsLayout& L, float* sums, cudaStream_t s) {
+                         float* nrm, uint32_t flags, void* ws, const WsLayout& L, const FwdExtra& x, cudaStream_t s) {
     constexpr int kMaxDev = 64;
     static std::atomic<int> occ_cache[kMaxDev];  // resident blocks per SM, per device
     int dev = 0;
@@ -421,14 +430,15 @@ cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const Hm
     if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
     const int sm = sm_count();
     if (sm <= 0) return cudaErrorInvalidDevice;
-    constexpr size_t smem = sizeof(float4) * (THREADS / 32) * (32 * kStage + EPI * SMAX * 2 * 32);
+    constexpr size_t smem =
+        sizeof(float4) * ((THREADS / 32) * (32 * kStage + EPI * SMAX * 2 * 32) + (MODE == kModeStage ? 9 : 0));
     int occ = occ_cache[dev].load(std::memory_order_relaxed);
     if (occ == 0) {
         int o = 0;
-        cudaError_t e = cudaFuncSetAttribute(k_forward<THREADS, MINB, SMAX, EPI, SAVE>,
+        cudaError_t e = cudaFuncSetAttribute(k_forward<THREADS, MINB, SMAX, EPI, MODE>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_forward<THREADS, MINB, SMAX, EPI, SAVE>, THREADS,
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_forward<THREADS, MINB, SMAX, EPI, MODE>, THREADS,
                                                           smem);
         if (e != cudaSuccess) return e;
         occ = o < 1 ? 1 : o;
@@ -446,8 +456,8 @@ cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const Hm
     lc.attrs = attr;
     lc.numAttrs = 1;
     const uint32_t chunk = cfg.chunk >= 1 && cfg.chunk <= 32 ? (uint32_t)cfg.chunk : 32u;
-    return cudaLaunchKernelEx(&lc, k_forward<THREADS, MINB, SMAX, EPI, SAVE>, patches, hm, pos, nrm, flags,
-                              static_cast<char*>(ws), L, chunk, reinterpret_cast<float4*>(sums));
+    return cudaLaunchKernelEx(&lc, k_forward<THREADS, MINB, SMAX, EPI, MODE>, patches, hm, pos, nrm, flags,
+                              static_cast<char*>(ws), L, chunk, reinterpret_cast<float4*>(x.sums), x.view, x.stage);
 }
 
 }  // namespace
@@ -483,30 +493,38 @@ bool forward_config_supported(const FwdConfig& c) {
     return false;
 }
 
+// The epilogue variants beyond the plain one exist with the register
+// epilogue only: a tuning with the shared-memory epilogue runs them through
+// the register one, same shape.
+template <int MODE>
+cudaError_t launch_forward_mode(const FwdConfig& cfg, const wt_patch* patches, const HmDev& hm, float* pos,
+                                float* nrm, uint32_t flags, void* ws, const WsLayout& L, const FwdExtra& x,
+                                cudaStream_t s) {
+    if (cfg.s == 4 && cfg.warps == 8)
+        return launch_fwd_t<256, 3, 4, 0, MODE>(cfg, patches, hm, pos, nrm, flags, ws, L, x, s);
+    if (cfg.s == 8 && cfg.warps == 8)
+        return launch_fwd_t<256, 2, 8, 0, MODE>(cfg, patches, hm, pos, nrm, flags, ws, L, x, s);
+    if (cfg.s == 8 && cfg.warps == 16)
+        return launch_fwd_t<512, 1, 8, 0, MODE>(cfg, patches, hm, pos, nrm, flags, ws, L, x, s);
+    return cudaErrorInvalidValue;
+}
+
 cudaError_t launch_forward(const FwdConfig& cfg, const wt_patch* patches, uint32_t, const HmDev& hm,
-                           float* pos, float* nrm, uint32_t flags, void* ws, const WsLayout& L, float* sums,
+                           float* pos, float* nrm, uint32_t flags, void* ws, const WsLayout& L, const FwdExtra& x,
                            cudaStream_t s) {
-    // warps per block; the minimum-blocks hint sets the register budget.
-    // The saving kernels exist with the register epilogue only: a tuning with
-    // the shared-memory epilogue saves through the register one, same shape.
-    if (sums) {
-        if (cfg.s == 4 && cfg.warps == 8)
-            return launch_fwd_t<256, 3, 4, 0, true>(cfg, patches, hm, pos, nrm, flags, ws, L, sums, s);
-        if (cfg.s == 8 && cfg.warps == 8)
-            return launch_fwd_t<256, 2, 8, 0, true>(cfg, patches, hm, pos, nrm, flags, ws, L, sums, s);
-        if (cfg.s == 8 && cfg.warps == 16)
-            return launch_fwd_t<512, 1, 8, 0, true>(cfg, patches, hm, pos, nrm, flags, ws, L, sums, s);
-        return cudaErrorInvalidValue;
-    }
+    if (x.sums && x.view) return cudaErrorInvalidValue;
+    if (x.sums) return launch_forward_mode<kModeSave>(cfg, patches, hm, pos, nrm, flags, ws, L, x, s);
+    if (x.view) return launch_forward_mode<kModeStage>(cfg, patches, hm, pos, nrm, flags, ws, L, x, s);
+    // warps per block; the minimum-blocks hint sets the register budget
     if (cfg.s == 4 && cfg.warps == 8 && cfg.epi == 0)
-        return launch_fwd_t<256, 3, 4, 0, false>(cfg, patches, hm, pos, nrm, flags, ws, L, nullptr, s);  // 80 regs
+        return launch_fwd_t<256, 3, 4, 0, kModePlain>(cfg, patches, hm, pos, nrm, flags, ws, L, x, s);  // 80 regs
     if (cfg.s == 8 && cfg.epi == 0) {
-        if (cfg.warps == 8) return launch_fwd_t<256, 2, 8, 0, false>(cfg, patches, hm, pos, nrm, flags, ws, L, nullptr, s);
-        if (cfg.warps == 16) return launch_fwd_t<512, 1, 8, 0, false>(cfg, patches, hm, pos, nrm, flags, ws, L, nullptr, s);
+        if (cfg.warps == 8) return launch_fwd_t<256, 2, 8, 0, kModePlain>(cfg, patches, hm, pos, nrm, flags, ws, L, x, s);
+        if (cfg.warps == 16) return launch_fwd_t<512, 1, 8, 0, kModePlain>(cfg, patches, hm, pos, nrm, flags, ws, L, x, s);
     }
     if (cfg.s == 8 && cfg.epi == 1) {
-        if (cfg.warps == 8) return launch_fwd_t<256, 2, 8, 1, false>(cfg, patches, hm, pos, nrm, flags, ws, L, nullptr, s);
-        if (cfg.warps == 16) return launch_fwd_t<512, 1, 8, 1, false>(cfg, patches, hm, pos, nrm, flags, ws, L, nullptr, s);
+        if (cfg.warps == 8) return launch_fwd_t<256, 2, 8, 1, kModePlain>(cfg, patches, hm, pos, nrm, flags, ws, L, x, s);
+        if (cfg.warps == 16) return launch_fwd_t<512, 1, 8, 1, kModePlain>(cfg, patches, hm, pos, nrm, flags, ws, L, x, s);
     }
     return cudaErrorInvalidValue;
 }

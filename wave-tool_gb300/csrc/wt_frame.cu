@@ -19,8 +19,11 @@
 #include <cstring>
 
 #include "wt_internal.h"
+#include "wt_stage.cuh"
 
 namespace {
+
+using wt::StageOut;
 
 #define WT_HD __host__ __device__ inline
 
@@ -377,32 +380,6 @@ __global__ void __launch_bounds__(32) k_projected_grid(const wt_camera* __restri
 
 constexpr int kStageThreads = 256;
 
-struct StageOut {
-    float* clip;    // float4
-    float* ndc0;    // float2
-    float* view;    // layout
-    float* facing;  // layout
-    float* nyaw;    // layout
-};
-
-template <bool VEC3>
-__device__ __forceinline__ float3 load3(const float* p, uint64_t i) {
-    if (VEC3) return make_float3(p[3 * i], p[3 * i + 1], p[3 * i + 2]);
-    const float4 v = reinterpret_cast<const float4*>(p)[i];
-    return make_float3(v.x, v.y, v.z);
-}
-
-template <bool VEC3>
-__device__ __forceinline__ void store3(float* p, uint64_t i, float3 v) {
-    if (VEC3) {
-        p[3 * i] = v.x;
-        p[3 * i + 1] = v.y;
-        p[3 * i + 2] = v.z;
-    } else {
-        reinterpret_cast<float4*>(p)[i] = make_float4(v.x, v.y, v.z, 0.0f);
-    }
-}
-
 // One vertex per thread per iteration of a grid-stride loop.  The 36 floats
 // of wt_view are staged once per block in shared memory.
 template <bool VEC3>
@@ -411,42 +388,12 @@ __global__ void __launch_bounds__(kStageThreads) k_vertex_stage(const wt_view* _
     __shared__ float u[36];
     if (threadIdx.x < 36) u[threadIdx.x] = reinterpret_cast<const float*>(view)[threadIdx.x];
     __syncthreads();
-    const float* M = u;       // view_projection, column-major
-    const float* Y = u + 16;  // view_only_yaw
-    const float cx = u[32], cy = u[33], cz = u[34];
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const bool need_n = o.facing || o.nyaw;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float3 p = load3<VEC3>(pos, i);
-        if (o.clip) {
-            float4 c;
-            c.x = fmaf(M[0], p.x, fmaf(M[4], p.y, fmaf(M[8], p.z, M[12])));
-            c.y = fmaf(M[1], p.x, fmaf(M[5], p.y, fmaf(M[9], p.z, M[13])));
-            c.z = fmaf(M[2], p.x, fmaf(M[6], p.y, fmaf(M[10], p.z, M[14])));
-            c.w = fmaf(M[3], p.x, fmaf(M[7], p.y, fmaf(M[11], p.z, M[15])));
-            reinterpret_cast<float4*>(o.clip)[i] = c;
-        }
-        if (o.ndc0) {
-            const float x = fmaf(M[0], p.x, fmaf(M[8], p.z, M[12]));
-            const float y = fmaf(M[1], p.x, fmaf(M[9], p.z, M[13]));
-            const float w = fmaf(M[3], p.x, fmaf(M[11], p.z, M[15]));
-            reinterpret_cast<float2*>(o.ndc0)[i] = make_float2(x / w, y / w);
-        }
-        const float3 v = make_float3(cx - p.x, cy - p.y, cz - p.z);
-        if (o.view) store3<VEC3>(o.view, i, v);
-        if (o.facing || o.nyaw) {
-            float3 nv = load3<VEC3>(nrm, i);
-            // the sign of dot(n, normalize(v)) is the sign of dot(n, v)
-            if (fmaf(nv.x, v.x, fmaf(nv.y, v.y, nv.z * v.z)) < 0.0f) nv = make_float3(-nv.x, -nv.y, -nv.z);
-            if (o.facing) store3<VEC3>(o.facing, i, nv);
-            if (o.nyaw) {
-                float3 q;
-                q.x = fmaf(Y[0], nv.x, fmaf(Y[4], nv.y, Y[8] * nv.z));
-                q.y = fmaf(Y[1], nv.x, fmaf(Y[5], nv.y, Y[9] * nv.z));
-                q.z = fmaf(Y[2], nv.x, fmaf(Y[6], nv.y, Y[10] * nv.z));
-                const float s = 1.0f / sqrtf(fmaf(q.x, q.x, fmaf(q.y, q.y, q.z * q.z)));
-                store3<VEC3>(o.nyaw, i, make_float3(q.x * s, q.y * s, q.z * s));
-            }
-        }
+        const float3 p = wt::dev::load3<VEC3>(pos, i);
+        const float3 nv = need_n ? wt::dev::load3<VEC3>(nrm, i) : make_float3(0.0f, 0.0f, 0.0f);
+        wt::dev::stage_vertex<VEC3>(u, p, nv, i, o);
     }
 }
 

@@ -110,6 +110,26 @@ struct FwdConfig {
     int epi;            // 0: epilogue from registers, 1: through shared memory
 };
 
+// Outputs of the vertex stage (any may be NULL): clip float4, ndc0 float2,
+// view / facing / nyaw in the call's vertex layout.
+struct StageOut {
+    float* clip;
+    float* ndc0;
+    float* view;
+    float* facing;
+    float* nyaw;
+};
+
+// Optional extra outputs of the forward (at most one of the two is set):
+// sums: 8 floats per output vertex (its wave sums, for the adjoint);
+// view: device wt_view, with `stage` the vertex-stage outputs written by the
+// forward's own epilogue (float4 layouts, world positions).
+struct FwdExtra {
+    float* sums;
+    const wt_view* view;
+    StageOut stage;
+};
+
 struct HmDev {
     const float* texels;
     uint32_t width, height;
@@ -123,10 +143,10 @@ struct HmDev {
 cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
                         uint32_t n_waves, const HmDev& hm, uint64_t out_capacity,
                         uint32_t tile_cols, void* ws, const WsLayout& L, cudaStream_t s);
-// sums: NULL, or 8 floats per output vertex (its wave sums, for the adjoint)
+// pos may be NULL only with x.view set
 cudaError_t launch_forward(const FwdConfig& cfg, const wt_patch* patches, uint32_t n_patches,
                            const HmDev& hm, float* pos, float* nrm, uint32_t flags, void* ws,
-                           const WsLayout& L, float* sums, cudaStream_t s);
+                           const WsLayout& L, const FwdExtra& x, cudaStream_t s);
 cudaError_t launch_forward_naive(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
                                  const HmDev& hm, float* pos, float* nrm, uint32_t flags,
                                  void* ws, const WsLayout& L, uint64_t total_vertices,

@@ -104,7 +104,7 @@ extern "C" wt_status wt_gerstner_displace_noalloc(const wt_patch* patches, uint3
     if (flags & WT_PHASE_FP32_NAIVE)
         e = wt::launch_forward_naive(patches, n_patches, waves, h, pos_out, nrm_out, flags, ws, L, out_capacity, s);
     else
-        e = wt::launch_forward(cfg, patches, n_patches, h, pos_out, nrm_out, flags, ws, L, nullptr, s);
+        e = wt::launch_forward(cfg, patches, n_patches, h, pos_out, nrm_out, flags, ws, L, wt::FwdExtra{}, s);
     if (e != cudaSuccess) return cuda_fail(e, "forward launch");
     return WT_OK;
 }
