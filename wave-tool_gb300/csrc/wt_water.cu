@@ -102,28 +102,35 @@ struct Setup {
 __device__ __forceinline__ bool setup_tri(const WinTri& w, uint32_t W, uint32_t H, Setup& s) {
     const int32_t xmn = min(w.X[0], min(w.X[1], w.X[2])), xmx = max(w.X[0], max(w.X[1], w.X[2]));
     const int32_t ymn = min(w.Y[0], min(w.Y[1], w.Y[2])), ymx = max(w.Y[0], max(w.Y[1], w.Y[2]));
-    const bool small = (int64_t)xmx - xmn < kSmallExtent && (int64_t)ymx - ymn < kSmallExtent;
-    int64_t area;
-    if (small)  // |products| < 2^26: exact in 32 bits
-        area = (w.X[1] - w.X[0]) * (w.Y[2] - w.Y[0]) - (w.Y[1] - w.Y[0]) * (w.X[2] - w.X[0]);
-    else
-        area = (int64_t)(w.X[1] - w.X[0]) * (w.Y[2] - w.Y[0]) - (int64_t)(w.Y[1] - w.Y[0]) * (w.X[2] - w.X[0]);
-    if (area == 0) return false;
-    const int a = area > 0 ? 1 : 2, b = area > 0 ? 2 : 1;  // counter-clockwise order
+    // pixel centres (p * 256 + 128) inside the box, clamped to the viewport;
+    // most far-field triangles of a projected grid hold none and stop here.
+    // Window coordinates stay below 2^28 in magnitude (guard band of 64
+    // viewports, viewport <= 16384, 1/256 pixel), so 32 bits hold these.
+    int32_t px0 = -((128 - xmn) >> 8), px1 = (xmx - 128) >> 8;
+    int32_t py0 = -((128 - ymn) >> 8), py1 = (ymx - 128) >> 8;
+    px0 = max(px0, 0);
+    py0 = max(py0, 0);
+    px1 = min(px1, (int32_t)W - 1);
+    py1 = min(py1, (int32_t)H - 1);
+    if (px0 > px1 || py0 > py1) return false;
+    const bool small = xmx - xmn < (int32_t)kSmallExtent && ymx - ymn < (int32_t)kSmallExtent;
+    bool ccw;
+    if (small) {  // |products| < 2^26: exact in 32 bits
+        int32_t area = (w.X[1] - w.X[0]) * (w.Y[2] - w.Y[0]) - (w.Y[1] - w.Y[0]) * (w.X[2] - w.X[0]);
+        if (area == 0) return false;
+        ccw = area > 0;
+        s.area_f = (float)(ccw ? area : -area);
+    } else {
+        int64_t area = (int64_t)(w.X[1] - w.X[0]) * (w.Y[2] - w.Y[0]) - (int64_t)(w.Y[1] - w.Y[0]) * (w.X[2] - w.X[0]);
+        if (area == 0) return false;
+        ccw = area > 0;
+        s.area_f = (float)(ccw ? area : -area);
+    }
+    const int a = ccw ? 1 : 2, b = ccw ? 2 : 1;  // counter-clockwise order
     s.x[0] = w.X[0]; s.y[0] = w.Y[0]; s.z[0] = w.Z[0];
     s.x[1] = w.X[a]; s.y[1] = w.Y[a]; s.z[1] = w.Z[a];
     s.x[2] = w.X[b]; s.y[2] = w.Y[b]; s.z[2] = w.Z[b];
-    if (area < 0) area = -area;
-    s.area_f = small ? (float)(int32_t)area : (float)area;
-    const int32_t xmin = xmn, xmax = xmx, ymin = ymn, ymax = ymx;
-    int64_t px0 = -((128 - (int64_t)xmin) >> 8), px1 = ((int64_t)xmax - 128) >> 8;
-    int64_t py0 = -((128 - (int64_t)ymin) >> 8), py1 = ((int64_t)ymax - 128) >> 8;
-    px0 = px0 < 0 ? 0 : px0;
-    py0 = py0 < 0 ? 0 : py0;
-    px1 = px1 > (int64_t)W - 1 ? (int64_t)W - 1 : px1;
-    py1 = py1 > (int64_t)H - 1 ? (int64_t)H - 1 : py1;
-    if (px0 > px1 || py0 > py1) return false;
-    s.px0 = (int32_t)px0; s.px1 = (int32_t)px1; s.py0 = (int32_t)py0; s.py1 = (int32_t)py1;
+    s.px0 = px0; s.px1 = px1; s.py0 = py0; s.py1 = py1;
     s.small = small;
     s.incl = 0;
     for (int k = 0; k < 3; ++k) {
@@ -218,9 +225,15 @@ __device__ __forceinline__ void raster_warp(const Setup& s, uint32_t tri, uint32
     const uint32_t bw = (uint32_t)(s.px1 - s.px0 + 1);
     const uint32_t n = bw * (uint32_t)(s.py1 - s.py0 + 1);
     if (s.small) {
+        // pixel p = r * bw + c walked in steps of 32 = qs * bw + rs (one
+        // division per triangle, none per pixel)
+        const uint32_t qs = 32u / bw, rs = 32u - qs * bw;
+        uint32_t r = (uint32_t)lane / bw, c = (uint32_t)lane - r * bw;
         for (uint32_t p = (uint32_t)lane; p < n; p += 32) {
-            const uint32_t r = p / bw;
-            raster_pixel32(s, s.px0 + (int32_t)(p - r * bw), s.py0 + (int32_t)r, tri, W, frag);
+            raster_pixel32(s, s.px0 + (int32_t)c, s.py0 + (int32_t)r, tri, W, frag);
+            c += rs;
+            r += qs;
+            if (c >= bw) { c -= bw; ++r; }
         }
         return;
     }
@@ -293,7 +306,8 @@ __global__ void __launch_bounds__(256, 3) k_water_raster(const float4* __restric
                     w.X[2] = c.x; w.Y[2] = c.y; w.Z[2] = __int_as_float(c.z);
                     Setup s;
                     if (setup_tri(w, W, H, s)) {
-                        const int64_t npix = ((int64_t)s.px1 - s.px0 + 1) * ((int64_t)s.py1 - s.py0 + 1);
+                        // box <= 16384^2 pixels: 32 bits hold its size
+                        const int32_t npix = (s.px1 - s.px0 + 1) * (s.py1 - s.py0 + 1);
                         if (npix <= kSmallPixels) {
                             if (s.small) raster_small(s, (uint32_t)t, W, frag);
                             else raster_own(s, (uint32_t)t, W, frag);
