@@ -214,6 +214,7 @@ def build_frame(wt, workloads):
     surf = wt.Surface(patch, w.waves, wt.heightmap_from(w.heightmap))
     cam_dev, view_dev = wt.to_device(cam), wt.to_device(view)
     pos, nrm = surf.alloc_outputs(wt.WT_OUT_WORLD)
+    tuning = surf.autotune(pos, nrm, flags=wt.WT_OUT_WORLD, reps=5)  # once, as a renderer would at start-up
     n = pos.shape[0]
     outs = {k: torch.empty((n, 2 if k == "ndc0" else 4), device="cuda")
             for k in ("clip", "ndc0", "view", "facing", "nrm_yaw")}
@@ -250,6 +251,7 @@ def build_frame(wt, workloads):
                        local_refractions=lrefr, colour=colour, stream=s)
 
     return dict(frame=frame, raster=raster, shade=shade, n=n, waves=len(w.waves), VW=VW, VH=VH, frags=frags,
+                tuning=tuning,
                 projected_grid=lambda: wt.projected_grid_async(cam_dev, surf.patches, view_dev),
                 displace=lambda: surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD),
                 vertex_stage=lambda: wt.vertex_stage(view_dev, pos, nrm, out=outs),
@@ -294,6 +296,7 @@ def frame_pipeline(wt, workloads, stream, flush):
     except (OSError, KeyError, ValueError):
         hbm_peak, peak_src = 6800.0, "fallback 6.8 TB/s"
     return {"vertices": n, "terms": n * F["waves"], "viewport": [VW, VH], "water_pixels_frac": covered,
+            "displace_tuning": F["tuning"],
             "frame_graph_ms": fms, "frame_graph_unfused_ms": graph_ms[False], "raster_ms": rms, "shade_ms": sms,
             "displace_with_fused_stage_ms": fsms,
             "frames_per_s": 1e3 / fms, "projected_grid_kernel_ms": gms, "displace_ms": dms,
