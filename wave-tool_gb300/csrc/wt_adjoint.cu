@@ -38,11 +38,20 @@ namespace {
 using namespace wt::dev;
 
 constexpr int kAdjWarps = 4;                 // warps per block
+// Tiles per queue item ("chunk"): a warp takes this many consecutive tiles of
+// one patch and adds their per-wave sums into one record, so the records (and
+// the column sums that read them back) shrink by this factor, against a
+// coarser queue.  Measured on 64 uneven patches: 2 tiles per chunk make the
+// recomputing adjoint 1.6 % faster than 1, while the saved-sums adjoint (less
+// work per tile) is 1.5 % slower at 2; 4 and 8 are slower for both.  The
+// workspace holds records for chunks of 1.
+constexpr uint32_t kAdjChunkRecompute = 2;
+constexpr uint32_t kAdjChunkSaved = 1;
 constexpr int kGbufVerts = 256;              // vertices per tile (32 lanes x S <= 8)
 constexpr int kGbufF4 = 2;                   // float4 per parked vertex
 
 __global__ void __launch_bounds__(1024) k_adj_scan(const wt_patch* __restrict__ patches, uint32_t n, char* ws,
-                                                   AdjLayout L) {
+                                                   AdjLayout L, uint32_t chunk) {
 #if __CUDA_ARCH__ >= 900
     cudaGridDependencySynchronize();
 #endif
@@ -52,20 +61,28 @@ __global__ void __launch_bounds__(1024) k_adj_scan(const wt_patch* __restrict__ 
     const uint32_t* pair_off = reinterpret_cast<const uint32_t*>(ws + L.f.pair_off);
     uint32_t* rank = reinterpret_cast<uint32_t*>(ws + L.rank);
     uint32_t* part_off = reinterpret_cast<uint32_t*>(ws + L.part_off);
+    uint32_t* chunk_pre = reinterpret_cast<uint32_t*>(ws + L.chunk_pre);
     for (uint32_t q = threadIdx.x; q < n; q += blockDim.x) {
         const uint32_t p = sorted[q];
         rank[p] = q;
-        const uint64_t rec = (uint64_t)(tile_pre[q + 1] - tile_pre[q]) * (pair_off[p + 1] - pair_off[p]);
+        const uint32_t chunks = (tile_pre[q + 1] - tile_pre[q] + chunk - 1) / chunk;
+        chunk_pre[q] = chunks;
+        const uint64_t rec = (uint64_t)chunks * (pair_off[p + 1] - pair_off[p]);
         part_off[q] = rec > 0xffffffffull ? 0xffffffffu : (uint32_t)rec;
     }
     __syncthreads();
     const uint32_t total = block_exclusive_scan(part_off, n);
+    __syncthreads();  // every thread has read the first scan's total
+    const uint32_t chunks = block_exclusive_scan(chunk_pre, n);
     if (threadIdx.x == 0) {
         part_off[n] = total;
-        if ((uint64_t)total > L.cap_records || total == 0xffffffffu) {
+        chunk_pre[n] = chunks;
+        hdr->total_chunks = chunks;
+        if ((uint64_t)total > L.cap_records || total == 0xffffffffu || hdr->total_tiles == 0) {
             // the device patches need more records than the host copy said
-            atomicCAS(&hdr->status, 0u, (uint32_t)WT_ERR_NOMEM);
-            hdr->total_tiles = 0;
+            // (or the prep refused them)
+            if (hdr->total_tiles != 0) atomicCAS(&hdr->status, 0u, (uint32_t)WT_ERR_NOMEM);
+            hdr->total_chunks = 0;
         }
     }
 }
@@ -170,7 +187,7 @@ template <bool SAVED>
 __global__ void __launch_bounds__(32 * kAdjWarps, SAVED ? 5 : 4)
 k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restrict__ gpos,
           const float* __restrict__ gnrm, uint32_t flags, char* __restrict__ ws, AdjLayout L,
-          const float4* __restrict__ sums) {
+          const float4* __restrict__ sums, uint32_t chunk) {
 #if __CUDA_ARCH__ >= 900
     cudaGridDependencySynchronize();
 #endif
@@ -185,9 +202,10 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
     const PatchAux* aux = reinterpret_cast<const PatchAux*>(ws + L.f.aux);
     const PairCoef* coef = reinterpret_cast<const PairCoef*>(ws + L.f.coef);
     const uint32_t* part_off = reinterpret_cast<const uint32_t*>(ws + L.part_off);
+    const uint32_t* chunk_pre = reinterpret_cast<const uint32_t*>(ws + L.chunk_pre);
     float* partials = reinterpret_cast<float*>(ws + L.partials);
     const uint32_t n = hdr->n_patches;
-    const uint32_t total = hdr->total_tiles;
+    const uint32_t total = hdr->total_chunks;
     const bool pow2 = hm.present && (hm.width & (hm.width - 1)) == 0 && (hm.height & (hm.height - 1)) == 0;
     const bool vec3 = (flags & WT_LAYOUT_VEC3) != 0;
 
@@ -197,121 +215,132 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
     uint32_t q = 0;
     while (t < total) {
         if (lane == 0) t_next = atomicAdd(&hdr->tile_counter, 1u);
-        if (tile_pre[q + 1] <= t) {
+        if (chunk_pre[q + 1] <= t) {
             uint32_t step = 1, lo = q + 1, hi = q + 2;
-            while (hi <= n && tile_pre[hi] <= t) { lo = hi; step <<= 1; hi = lo + step; }
+            while (hi <= n && chunk_pre[hi] <= t) { lo = hi; step <<= 1; hi = lo + step; }
             hi = min(hi, n + 1);
             while (hi - lo > 1) {
                 const uint32_t mid = (lo + hi) >> 1;
-                if (tile_pre[mid] <= t) lo = mid; else hi = mid;
+                if (chunk_pre[mid] <= t) lo = mid; else hi = mid;
             }
             q = lo;
         }
         const uint32_t p = sorted[q];
-        const uint32_t lt = t - tile_pre[q];
-        const uint32_t cols = patches[p].cols;
-        const uint32_t nwaves = patches[p].wave_count;
-        const uint64_t out0 = patches[p].out_offset;
-        const PatchAux a = aux[p];
-        // the forward's tiling: 256-column tiles, each row's last tile narrower
-        const uint32_t tpr = tiles_per_row(cols, 8);
-        const uint32_t row = lt / tpr;
-        const uint32_t c0 = (lt - row * tpr) * 256u;
-        const uint32_t S = min(8u, (cols - c0 + 31u) / 32u);
-        if (nwaves > 0) {
-            const uint64_t rowbase = out0 + (uint64_t)row * cols;
-            if (SAVED) {
-                // ---- phase 1 from the forward's saved sums: park them
-                for (uint32_t j = 0; j < S; ++j) {
-                    const uint32_t col = c0 + lane + 32 * j;
-                    float4* d = gbuf + kGbufF4 * (lane + 32 * j);
-                    if (col < cols) {
-                        d[0] = __ldcs(sums + 2 * (rowbase + col));
-                        d[1] = __ldcs(sums + 2 * (rowbase + col) + 1);
-                    }
-                }
-            } else {
-                // ---- phase 1: forward sums recomputed, vertex per lane
-                float acc[8][8];
-#pragma unroll
-                for (int j = 0; j < 8; ++j)
-#pragma unroll
-                    for (int mm = 0; mm < 8; ++mm) acc[j][mm] = 0.0f;
-                for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
-                    const uint32_t nw = min(32u, nwaves - w0);
-                    __syncwarp();
-                    if (lane < nw) stage_wave(coef[a.pair_offset + w0 + lane], c0, row, wst + kStage * lane);
-                    __syncwarp();
-                    wave_loop_dispatch<8>(S, acc, wst, nw, lane);
-                }
-                // park the eight sums of each vertex
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    if ((uint32_t)j < S) {
+        const uint32_t lc = t - chunk_pre[q];
+        const uint32_t lt0 = lc * chunk;
+        const uint32_t lt1 = min(lt0 + chunk, tile_pre[q + 1] - tile_pre[q]);
+        for (uint32_t lt = lt0; lt < lt1; ++lt) {
+            const uint32_t cols = patches[p].cols;
+            const uint32_t nwaves = patches[p].wave_count;
+            const uint64_t out0 = patches[p].out_offset;
+            const PatchAux a = aux[p];
+            // the forward's tiling: 256-column tiles, each row's last tile narrower
+            const uint32_t tpr = tiles_per_row(cols, 8);
+            const uint32_t row = lt / tpr;
+            const uint32_t c0 = (lt - row * tpr) * 256u;
+            const uint32_t S = min(8u, (cols - c0 + 31u) / 32u);
+            if (nwaves > 0) {
+                const uint64_t rowbase = out0 + (uint64_t)row * cols;
+                if (SAVED) {
+                    // ---- phase 1 from the forward's saved sums: park them
+                    for (uint32_t j = 0; j < S; ++j) {
+                        const uint32_t col = c0 + lane + 32 * j;
                         float4* d = gbuf + kGbufF4 * (lane + 32 * j);
-                        d[0] = make_float4(acc[j][0], acc[j][1], acc[j][2], acc[j][3]);
-                        d[1] = make_float4(acc[j][4], acc[j][5], acc[j][6], acc[j][7]);
+                        if (col < cols) {
+                            d[0] = __ldcs(sums + 2 * (rowbase + col));
+                            d[1] = __ldcs(sums + 2 * (rowbase + col) + 1);
+                        }
+                    }
+                } else {
+                    // ---- phase 1: forward sums recomputed, vertex per lane
+                    float acc[8][8];
+    #pragma unroll
+                    for (int j = 0; j < 8; ++j)
+    #pragma unroll
+                        for (int mm = 0; mm < 8; ++mm) acc[j][mm] = 0.0f;
+                    for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
+                        const uint32_t nw = min(32u, nwaves - w0);
+                        __syncwarp();
+                        if (lane < nw) stage_wave(coef[a.pair_offset + w0 + lane], c0, row, wst + kStage * lane);
+                        __syncwarp();
+                        wave_loop_dispatch<8>(S, acc, wst, nw, lane);
+                    }
+                    // park the eight sums of each vertex
+    #pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        if ((uint32_t)j < S) {
+                            float4* d = gbuf + kGbufF4 * (lane + 32 * j);
+                            d[0] = make_float4(acc[j][0], acc[j][1], acc[j][2], acc[j][3]);
+                            d[1] = make_float4(acc[j][4], acc[j][5], acc[j][6], acc[j][7]);
+                        }
                     }
                 }
-            }
-            // then turn them into the vertex adjoints in a rolled loop (one
-            // copy of that code)
-            const float v = (float)row * a.inv_rm1;
-            const float gx = (a.e1x + v * a.e3x) * a.inv_cm1, gz = (a.e1z + v * a.e3z) * a.inv_cm1;
-            const float xb0 = fmaf((float)c0, gx, v * a.e2x), zb0 = fmaf((float)c0, gz, v * a.e2z);
-            for (uint32_t j = 0; j < S; ++j) {
-                const uint32_t vi = lane + 32 * j;
-                const uint32_t col = c0 + vi;
-                float4* d = gbuf + kGbufF4 * vi;
-                float g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-                if (col < cols) {
-                    const float4 s0 = d[0], s1 = d[1];
-                    const float xl = fmaf((float)vi, gx, xb0), zl = fmaf((float)vi, gz, zb0);
-                    VertexSums sm{s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
-                    vertex_adjoint(sm, xl, zl, a, hm, pow2, gpos, gnrm, rowbase + col, vec3, g);
+                // then turn them into the vertex adjoints in a rolled loop (one
+                // copy of that code)
+                const float v = (float)row * a.inv_rm1;
+                const float gx = (a.e1x + v * a.e3x) * a.inv_cm1, gz = (a.e1z + v * a.e3z) * a.inv_cm1;
+                const float xb0 = fmaf((float)c0, gx, v * a.e2x), zb0 = fmaf((float)c0, gz, v * a.e2z);
+                for (uint32_t j = 0; j < S; ++j) {
+                    const uint32_t vi = lane + 32 * j;
+                    const uint32_t col = c0 + vi;
+                    float4* d = gbuf + kGbufF4 * vi;
+                    float g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                    if (col < cols) {
+                        const float4 s0 = d[0], s1 = d[1];
+                        const float xl = fmaf((float)vi, gx, xb0), zl = fmaf((float)vi, gz, zb0);
+                        VertexSums sm{s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+                        vertex_adjoint(sm, xl, zl, a, hm, pow2, gpos, gnrm, rowbase + col, vec3, g);
+                    }
+                    d[0] = make_float4(g[0], g[1], g[2], g[3]);
+                    d[1] = make_float4(g[4], g[5], g[6], g[7]);
                 }
-                d[0] = make_float4(g[0], g[1], g[2], g[3]);
-                d[1] = make_float4(g[4], g[5], g[6], g[7]);
-            }
-            __syncwarp();
-            // ---- phase 2: wave per lane, records of this tile
-            const uint32_t nvalid0 = min(32u, cols - c0);  // valid lanes at j = 0
-            const uint32_t rec0 = part_off[q] + lt * nwaves;
-            for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
-                // a chunk of nwc <= 32 waves: lanes form 32 / P groups of P
-                // lanes (P = nwc rounded up to a power of two); group g walks
-                // the vertex lanes l = g, g + G, ... and the groups' moments
-                // are combined by a fixed shuffle tree
-                const uint32_t nwc = min(32u, nwaves - w0);
-                uint32_t P = 1;
-                while (P < nwc) P <<= 1;
-                const uint32_t G = 32u / P;
-                const uint32_t wl = lane & (P - 1), grp = lane / P;
-                const uint32_t wi = w0 + wl;
-                const bool active = wl < nwc;
-                const PairCoef k = coef[a.pair_offset + (active ? wi : w0)];
-                float4 st[3];
-                stage_wave(k, c0, row, st);
-                float m[11];
-#pragma unroll
-                for (int i = 0; i < 11; ++i) m[i] = 0.0f;
-                const uint32_t t32 = __float_as_uint(st[0].x), a32 = __float_as_uint(st[0].y);
-                if (S == 8)
-                    wave_moments<8>(gbuf, 8, grp, G, nvalid0, t32, a32, st[0].z, st[0].w, k, xb0, zb0, gx, gz, m);
-                else
-                    wave_moments<0>(gbuf, S, grp, G, nvalid0, t32, a32, st[0].z, st[0].w, k, xb0, zb0, gx, gz, m);
-                for (uint32_t o = P; o < 32; o <<= 1) {
-#pragma unroll
-                    for (int i = 0; i < 11; ++i) m[i] += __shfl_down_sync(0xffffffffu, m[i], o);
+                __syncwarp();
+                // ---- phase 2: wave per lane, records of this tile
+                const uint32_t nvalid0 = min(32u, cols - c0);  // valid lanes at j = 0
+                const uint32_t rec0 = part_off[q] + lc * nwaves;
+                for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
+                    // a chunk of nwc <= 32 waves: lanes form 32 / P groups of P
+                    // lanes (P = nwc rounded up to a power of two); group g walks
+                    // the vertex lanes l = g, g + G, ... and the groups' moments
+                    // are combined by a fixed shuffle tree
+                    const uint32_t nwc = min(32u, nwaves - w0);
+                    uint32_t P = 1;
+                    while (P < nwc) P <<= 1;
+                    const uint32_t G = 32u / P;
+                    const uint32_t wl = lane & (P - 1), grp = lane / P;
+                    const uint32_t wi = w0 + wl;
+                    const bool active = wl < nwc;
+                    const PairCoef k = coef[a.pair_offset + (active ? wi : w0)];
+                    float4 st[3];
+                    stage_wave(k, c0, row, st);
+                    float m[11];
+    #pragma unroll
+                    for (int i = 0; i < 11; ++i) m[i] = 0.0f;
+                    const uint32_t t32 = __float_as_uint(st[0].x), a32 = __float_as_uint(st[0].y);
+                    if (S == 8)
+                        wave_moments<8>(gbuf, 8, grp, G, nvalid0, t32, a32, st[0].z, st[0].w, k, xb0, zb0, gx, gz, m);
+                    else
+                        wave_moments<0>(gbuf, S, grp, G, nvalid0, t32, a32, st[0].z, st[0].w, k, xb0, zb0, gx, gz, m);
+                    for (uint32_t o = P; o < 32; o <<= 1) {
+    #pragma unroll
+                        for (int i = 0; i < 11; ++i) m[i] += __shfl_down_sync(0xffffffffu, m[i], o);
+                    }
+                    if (active && grp == 0) {
+                        // the chunk's tiles add into one record, in tile order
+                        // (the same lane writes it for every tile of the chunk)
+                        float* r = partials + (size_t)kAdjRecord * (rec0 + wi);
+                        if (lt == lt0) {
+    #pragma unroll
+                            for (int i = 0; i < 11; ++i) r[i] = m[i];
+                        } else {
+    #pragma unroll
+                            for (int i = 0; i < 11; ++i) r[i] += m[i];
+                        }
+                    }
                 }
-                if (active && grp == 0) {
-                    float* r = partials + (size_t)kAdjRecord * (rec0 + wi);
-#pragma unroll
-                    for (int i = 0; i < 11; ++i) r[i] = m[i];
-                }
+                __syncwarp();
             }
-            __syncwarp();
-        }
+        }  // tiles of the chunk
         t = __shfl_sync(0xffffffffu, t_next, 0);
     }
 }
@@ -329,13 +358,13 @@ __global__ void __launch_bounds__(32 * kColLanes) k_adj_cols(uint32_t n, const c
 #endif
     __shared__ float red[kColLanes][32];
     const uint32_t* pair_off = reinterpret_cast<const uint32_t*>(ws + L.f.pair_off);
-    const uint32_t* tile_pre = reinterpret_cast<const uint32_t*>(ws + L.f.tile_pre);
+    const uint32_t* chunk_pre = reinterpret_cast<const uint32_t*>(ws + L.chunk_pre);
     const uint32_t* rank = reinterpret_cast<const uint32_t*>(ws + L.rank);
     const uint32_t* part_off = reinterpret_cast<const uint32_t*>(ws + L.part_off);
     const float* partials = reinterpret_cast<const float*>(ws + L.partials);
     const WsHeader* hdr = reinterpret_cast<const WsHeader*>(ws);
     float* colsum = reinterpret_cast<float*>(const_cast<char*>(ws) + L.pair_grad);
-    const bool ran = hdr->total_tiles > 0;
+    const bool ran = hdr->total_chunks > 0;
     const uint32_t cl = threadIdx.x & 31, tl = threadIdx.x >> 5;
     for (uint32_t p = blockIdx.y; p < n; p += gridDim.y) {
         const uint32_t nw = pair_off[p + 1] - pair_off[p];
@@ -343,7 +372,7 @@ __global__ void __launch_bounds__(32 * kColLanes) k_adj_cols(uint32_t n, const c
         const uint32_t col = blockIdx.x * 32 + cl;
         if (blockIdx.x * 32 >= width) continue;  // block-uniform
         const uint32_t qs = rank[p];
-        const uint32_t ntiles = tile_pre[qs + 1] - tile_pre[qs];
+        const uint32_t ntiles = chunk_pre[qs + 1] - chunk_pre[qs];  // records per column
         const float* base = partials + (size_t)kAdjRecord * part_off[qs];
         float sum = 0.0f, comp = 0.0f;
         if (ran && col < width) {
@@ -369,7 +398,10 @@ __global__ void __launch_bounds__(32 * kColLanes) k_adj_cols(uint32_t n, const c
 
 // One warp per wave: lane l takes patches l, l+32, ... that use the wave and
 // adds their closed-form gradients (FP64, from the patch's eleven column
-// sums); the lanes are then combined by a fixed shuffle tree.
+// sums); the lanes are then combined by a fixed shuffle tree, or, when one
+// lane alone holds a contribution (a wave used by one patch), taken from it
+// (GB300's FP64 rate is low: the tree's 40 FP64 adds per wave cost more than
+// the closed form).
 __global__ void __launch_bounds__(256) k_adj_waves(const wt_patch* __restrict__ patches, uint32_t n,
                                                    const wt_wave* __restrict__ waves, uint32_t n_waves,
                                                    const char* __restrict__ ws, AdjLayout L,
@@ -387,10 +419,12 @@ __global__ void __launch_bounds__(256) k_adj_waves(const wt_patch* __restrict__ 
         const double k = isinf(lam) ? 0.0 : kTwoPi / lam;
         const double A = w.amplitude, Q = w.steepness_q, Dx = w.dir_x, Dz = w.dir_z, sp = w.speed;
         double g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        bool has = false;
         for (uint32_t p = lane; p < n; p += 32) {
             const uint32_t nw = pair_off[p + 1] - pair_off[p];  // 0 for invalid patches
             const uint32_t off = patches[p].wave_offset;
             if (nw == 0 || wi < off || wi - off >= nw) continue;
+            has = true;
             const float* m = colsum + (size_t)kAdjRecord * (pair_off[p] + (wi - off));
             const double t = patches[p].time_s;
             const double Mdx = m[0], Mdy = m[1], Mdz = m[2], Mjx = m[3], Mjz = m[4];
@@ -410,9 +444,16 @@ __global__ void __launch_bounds__(256) k_adj_waves(const wt_patch* __restrict__ 
             g[6] += gDx;
             g[7] += gDz;
         }
+        const unsigned holders = __ballot_sync(0xffffffffu, has);
+        if (holders != 0 && (holders & (holders - 1)) == 0) {
+            const int src = __ffs(holders) - 1;
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
-            for (int o = 16; o > 0; o >>= 1) g[i] += __shfl_xor_sync(0xffffffffu, g[i], o);
+            for (int i = 0; i < 8; ++i) g[i] = __shfl_sync(0xffffffffu, g[i], src);
+        } else if (holders != 0) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                for (int o = 16; o > 0; o >>= 1) g[i] += __shfl_xor_sync(0xffffffffu, g[i], o);
+        }
         if (lane == 0) {
             wt_wave_grad o;
             o.d_amplitude = (float)g[0];
@@ -466,14 +507,14 @@ cudaError_t launch_adj_main(int sms, cudaStream_t s, const wt_patch* patches, co
         occ_cache[dev].store(occ, std::memory_order_relaxed);
     }
     return launch_pdl(k_adjoint<SAVED>, dim3(sms * occ), dim3(32 * kAdjWarps), smem, s, patches, hm, gpos, gnrm,
-                      flags, w, L, reinterpret_cast<const float4*>(sums));
+                      flags, w, L, reinterpret_cast<const float4*>(sums), SAVED ? kAdjChunkSaved : kAdjChunkRecompute);
 }
 
 }  // namespace
 
 uint64_t adjoint_records(const wt_patch& p) {
     if (p.cols < 2 || p.rows < 2) return 0;
-    return (uint64_t)p.rows * dev::tiles_per_row(p.cols, 8) * p.wave_count;
+    return (uint64_t)p.rows * dev::tiles_per_row(p.cols, 8) * p.wave_count;  // chunks of one tile
 }
 
 cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
@@ -482,7 +523,8 @@ cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt
                            cudaStream_t s) {
     char* w = static_cast<char*>(ws);
     const int sms = device_sms();
-    cudaError_t e = launch_pdl(k_adj_scan, dim3(1), dim3(1024), 0, s, patches, n_patches, w, L);
+    cudaError_t e = launch_pdl(k_adj_scan, dim3(1), dim3(1024), 0, s, patches, n_patches, w, L,
+                               sums ? kAdjChunkSaved : kAdjChunkRecompute);
     if (e != cudaSuccess) return e;
     e = sums ? launch_adj_main<true>(sms, s, patches, hm, gpos, gnrm, flags, w, L, sums)
              : launch_adj_main<false>(sms, s, patches, hm, gpos, gnrm, flags, w, L, nullptr);

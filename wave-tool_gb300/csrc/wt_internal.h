@@ -25,7 +25,8 @@ struct WsHeader {
     uint32_t total_tiles;
     uint32_t n_patches;
     uint32_t tile_cols;    // vertices per tile row (32 * S)
-    uint32_t pad[58];
+    uint32_t total_chunks; // adjoint: tile chunks in its queue (0 = do not run)
+    uint32_t pad[57];
 };
 static_assert(sizeof(WsHeader) == 256, "header size");
 
@@ -76,15 +77,16 @@ inline WsLayout ws_layout(uint32_t n_patches, uint64_t total_wave_slots) {
 }
 
 // Adjoint workspace: the forward layout (prep stages are shared), then
-// rank    u32[n]      sorted position of each patch
-// partoff u32[n+1]    exclusive prefix of records (tiles x waves) over the sorted order
-// partial float[11 x records]   per-(tile, wave) FP32 partial sums
-// colsum  float[11 x wave slots] per-(patch, wave) sums of the records
+// rank     u32[n]      sorted position of each patch
+// partoff  u32[n+1]    exclusive prefix of records (chunks x waves) over the sorted order
+// chunkpre u32[n+1]    exclusive prefix of tile chunks over the sorted order
+// partial  float[11 x records]   per-(chunk, wave) FP32 partial sums
+// colsum   float[11 x wave slots] per-(patch, wave) sums of the records
 constexpr int kAdjRecord = 11;
 
 struct AdjLayout {
     WsLayout f;
-    size_t rank, part_off, partials, pair_grad, end;
+    size_t rank, part_off, chunk_pre, partials, pair_grad, end;
     uint64_t cap_records;
 };
 
@@ -93,7 +95,8 @@ inline AdjLayout adj_layout(uint32_t n_patches, uint64_t total_wave_slots, uint6
     A.f = ws_layout(n_patches, total_wave_slots);
     size_t o = A.f.end;
     A.rank = o;      o = align_up(o + 4ull * n_patches, 16);
-    A.part_off = o;  o = align_up(o + 4ull * (n_patches + 1), 256);
+    A.part_off = o;  o = align_up(o + 4ull * (n_patches + 1), 16);
+    A.chunk_pre = o; o = align_up(o + 4ull * (n_patches + 1), 256);
     A.partials = o;  o = align_up(o + 4ull * kAdjRecord * records, 256);
     A.pair_grad = o; o = align_up(o + 8ull * 8 * total_wave_slots, 256);
     A.end = o;
@@ -154,7 +157,7 @@ cudaError_t launch_forward_naive(const wt_patch* patches, uint32_t n_patches, co
 bool forward_config_supported(const FwdConfig& cfg);
 
 // ---- adjoint (wt_adjoint.cu) ----------------------------------------------
-// Records (tiles x waves) of one patch, as the adjoint lays them out.
+// Records (tile chunks x waves) of one patch, as the adjoint lays them out.
 uint64_t adjoint_records(const wt_patch& p);
 // sums: NULL (phase 1 recomputes the forward sums) or the forward's saved sums
 cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
