@@ -68,6 +68,8 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
     uint32_t* pair_off = reinterpret_cast<uint32_t*>(ws + L.pair_off);
     uint32_t* tiles = reinterpret_cast<uint32_t*>(ws + L.tiles);
     __shared__ uint32_t bins[kSortBins];
+    constexpr uint32_t kScanSmemOffsets = 4096;
+    __shared__ uint32_t off_s[kScanSmemOffsets];
 
     if (threadIdx.x == 0) {
         hdr->status = 0;
@@ -93,15 +95,22 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
     const uint32_t total_pairs = block_exclusive_scan(pair_off, n);
     if (threadIdx.x == 0) pair_off[n] = total_pairs;
     __syncthreads();
-    // wave validation, one pair per thread; a patch with a bad wave runs no tiles
+    // wave validation, one pair per thread; a patch with a bad wave runs no
+    // tiles.  The owning patch is found by binary search over the offsets,
+    // from a shared-memory copy when they fit (each step a dependent load).
+    const bool off_in_smem = n + 1 <= kScanSmemOffsets;
+    if (off_in_smem)
+        for (uint32_t i = threadIdx.x; i <= n; i += blockDim.x) off_s[i] = pair_off[i];
+    __syncthreads();
+    const uint32_t* off = off_in_smem ? off_s : pair_off;
     for (uint32_t P = threadIdx.x; P < total_pairs; P += blockDim.x) {
         uint32_t lo = 0, hi = n + 1;
         while (lo < hi) {
             const uint32_t mid = (lo + hi) >> 1;
-            if (pair_off[mid] <= P) lo = mid + 1; else hi = mid;
+            if (off[mid] <= P) lo = mid + 1; else hi = mid;
         }
         const uint32_t p = lo - 1;
-        if (!wave_ok(waves[patches[p].wave_offset + (P - pair_off[p])])) {
+        if (!wave_ok(waves[patches[p].wave_offset + (P - off[p])])) {
             flag_error(hdr, WT_ERR_INVALID_ARG, p);
             tiles[p] = 0;
         }
