@@ -305,7 +305,16 @@ def frame_pipeline(wt, workloads, stream, flush):
             "vertex_stage_hbm_frac": stage_bytes / (vms * 1e-3) / 1e9 / hbm_peak, "hbm_peak_source": peak_src}
 
 
-def side_measurements(wt, workloads, surf, pos, nrm, flags, flush, stream, ms_step):
+# FP32 FMA-pipe operations of algorithmic work per (vertex, wave) term in the
+# adjoint: the forward's 10 (recurrence 2 + eight sums), then per wave and
+# vertex the recurrence (2), the eight moments (8), the two projections of the
+# phase adjoint (8), its combination (2) and its two sums (2); the saved-sums
+# adjoint skips the forward's 10.
+ADJ_FMA_PER_TERM = 32
+ADJ_SAVED_FMA_PER_TERM = 22
+
+
+def side_measurements(wt, workloads, surf, pos, nrm, flags, flush, stream, ms_step, fma_s=None):
     """Graph replay of the batched step, adjoint vs forward, the precision
     configuration's throughput and the Adam fit (each reported, not the
     headline)."""
@@ -348,6 +357,10 @@ def side_measurements(wt, workloads, surf, pos, nrm, flags, flush, stream, ms_st
         out[name] = {"terms": w.n_terms, "forward_ms": fms, "adjoint_ms": ams, "adjoint_over_forward": ams / fms,
                      "saving_forward_ms": sfms, "saved_adjoint_ms": sams,
                      "saved_adjoint_over_forward": sams / fms}
+        if fma_s:
+            # the adjoint against its own FMA roofline (whole call, prep and reductions included)
+            out[name]["adjoint_fma_frac"] = w.n_terms * ADJ_FMA_PER_TERM / (ams * 1e-3) / fma_s
+            out[name]["saved_adjoint_fma_frac"] = w.n_terms * ADJ_SAVED_FMA_PER_TERM / (sams * 1e-3) / fma_s
         del sums
     # precision configuration: 2048^2 vertices x 128 waves at three times
     prec = {}
@@ -503,7 +516,7 @@ def run_ours(args):
 
     extras = {}
     if not args.no_extras and rank == 0:
-        extras.update(side_measurements(wt, workloads, surf, pos, nrm, flags, flush, stream, ms_step))
+        extras.update(side_measurements(wt, workloads, surf, pos, nrm, flags, flush, stream, ms_step, fma_s))
         # 256 plain launches (one wt_gerstner_displace per patch)
         for _ in range(2):
             surf.displace(pos, nrm, flags=flags, unbatched=True)

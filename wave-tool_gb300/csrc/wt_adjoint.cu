@@ -43,15 +43,18 @@ constexpr int kAdjWarps = 4;                 // warps per block
 // the column sums that read them back) shrink by this factor, against a
 // coarser queue.  Measured on 64 uneven patches: 2 tiles per chunk make the
 // recomputing adjoint 1.6 % faster than 1, while the saved-sums adjoint (less
-// work per tile) is 1.5 % slower at 2; 4 and 8 are slower for both.  The
-// workspace holds records for chunks of 1.
+// work per tile) is 1.5 % slower at 2; 4 and 8 are slower for both.  With
+// fewer than kAdjChunkMinTilesPerWarp tiles per resident warp the queue would
+// run dry, so chunks stay single tiles (one 512^2 patch: 1024 tiles for 2432
+// warps).  The workspace holds records for chunks of 1.
 constexpr uint32_t kAdjChunkRecompute = 2;
 constexpr uint32_t kAdjChunkSaved = 1;
+constexpr uint32_t kAdjChunkMinTilesPerWarp = 8;
 constexpr int kGbufVerts = 256;              // vertices per tile (32 lanes x S <= 8)
 constexpr int kGbufF4 = 2;                   // float4 per parked vertex
 
 __global__ void __launch_bounds__(1024) k_adj_scan(const wt_patch* __restrict__ patches, uint32_t n, char* ws,
-                                                   AdjLayout L, uint32_t chunk) {
+                                                   AdjLayout L, uint32_t chunk_max, uint32_t min_tiles) {
 #if __CUDA_ARCH__ >= 900
     cudaGridDependencySynchronize();
 #endif
@@ -62,6 +65,7 @@ __global__ void __launch_bounds__(1024) k_adj_scan(const wt_patch* __restrict__ 
     uint32_t* rank = reinterpret_cast<uint32_t*>(ws + L.rank);
     uint32_t* part_off = reinterpret_cast<uint32_t*>(ws + L.part_off);
     uint32_t* chunk_pre = reinterpret_cast<uint32_t*>(ws + L.chunk_pre);
+    const uint32_t chunk = hdr->total_tiles >= min_tiles ? chunk_max : 1u;
     for (uint32_t q = threadIdx.x; q < n; q += blockDim.x) {
         const uint32_t p = sorted[q];
         rank[p] = q;
@@ -78,6 +82,7 @@ __global__ void __launch_bounds__(1024) k_adj_scan(const wt_patch* __restrict__ 
         part_off[n] = total;
         chunk_pre[n] = chunks;
         hdr->total_chunks = chunks;
+        hdr->adj_chunk = chunk;
         if ((uint64_t)total > L.cap_records || total == 0xffffffffu || hdr->total_tiles == 0) {
             // the device patches need more records than the host copy said
             // (or the prep refused them)
@@ -187,7 +192,7 @@ template <bool SAVED>
 __global__ void __launch_bounds__(32 * kAdjWarps, SAVED ? 5 : 4)
 k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restrict__ gpos,
           const float* __restrict__ gnrm, uint32_t flags, char* __restrict__ ws, AdjLayout L,
-          const float4* __restrict__ sums, uint32_t chunk) {
+          const float4* __restrict__ sums) {
 #if __CUDA_ARCH__ >= 900
     cudaGridDependencySynchronize();
 #endif
@@ -206,6 +211,7 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
     float* partials = reinterpret_cast<float*>(ws + L.partials);
     const uint32_t n = hdr->n_patches;
     const uint32_t total = hdr->total_chunks;
+    const uint32_t chunk = hdr->adj_chunk;
     const bool pow2 = hm.present && (hm.width & (hm.width - 1)) == 0 && (hm.height & (hm.height - 1)) == 0;
     const bool vec3 = (flags & WT_LAYOUT_VEC3) != 0;
 
@@ -486,28 +492,38 @@ cudaError_t launch_pdl(K kernel, dim3 grid, dim3 block, size_t smem, cudaStream_
     return cudaLaunchKernelEx(&lc, kernel, args...);
 }
 
-// The persistent main kernel: one grid of SMs x resident blocks (the
-// occupancy is read once per device and instantiation).
+constexpr size_t kAdjSmem = sizeof(float4) * kAdjWarps * (32 * kStage + kGbufVerts * kGbufF4);
+
+// Resident blocks per SM of the main kernel (read once per device and
+// variant; sets its shared-memory attribute on the way).
 template <bool SAVED>
-cudaError_t launch_adj_main(int sms, cudaStream_t s, const wt_patch* patches, const HmDev& hm, const float* gpos,
-                            const float* gnrm, uint32_t flags, char* w, const AdjLayout& L, const float* sums) {
-    constexpr size_t smem = sizeof(float4) * kAdjWarps * (32 * kStage + kGbufVerts * kGbufF4);
+cudaError_t adj_occupancy(int* occ_out) {
     static std::atomic<int> occ_cache[64];
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     int occ = occ_cache[dev].load(std::memory_order_relaxed);
     if (occ == 0) {
-        cudaError_t e = cudaFuncSetAttribute(k_adjoint<SAVED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(k_adjoint<SAVED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kAdjSmem);
         if (e != cudaSuccess) return e;
         int o = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_adjoint<SAVED>, 32 * kAdjWarps, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_adjoint<SAVED>, 32 * kAdjWarps, kAdjSmem);
         if (e != cudaSuccess) return e;
         occ = o < 1 ? 1 : o;
         occ_cache[dev].store(occ, std::memory_order_relaxed);
     }
-    return launch_pdl(k_adjoint<SAVED>, dim3(sms * occ), dim3(32 * kAdjWarps), smem, s, patches, hm, gpos, gnrm,
-                      flags, w, L, reinterpret_cast<const float4*>(sums), SAVED ? kAdjChunkSaved : kAdjChunkRecompute);
+    *occ_out = occ;
+    return cudaSuccess;
+}
+
+// The persistent main kernel: one grid of SMs x resident blocks.
+template <bool SAVED>
+cudaError_t launch_adj_main(int sms, int occ, cudaStream_t s, const wt_patch* patches, const HmDev& hm,
+                            const float* gpos, const float* gnrm, uint32_t flags, char* w, const AdjLayout& L,
+                            const float* sums) {
+    return launch_pdl(k_adjoint<SAVED>, dim3(sms * occ), dim3(32 * kAdjWarps), kAdjSmem, s, patches, hm, gpos,
+                      gnrm, flags, w, L, reinterpret_cast<const float4*>(sums));
 }
 
 }  // namespace
@@ -523,11 +539,15 @@ cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt
                            cudaStream_t s) {
     char* w = static_cast<char*>(ws);
     const int sms = device_sms();
-    cudaError_t e = launch_pdl(k_adj_scan, dim3(1), dim3(1024), 0, s, patches, n_patches, w, L,
-                               sums ? kAdjChunkSaved : kAdjChunkRecompute);
+    int occ = 1;
+    cudaError_t e = sums ? adj_occupancy<true>(&occ) : adj_occupancy<false>(&occ);
     if (e != cudaSuccess) return e;
-    e = sums ? launch_adj_main<true>(sms, s, patches, hm, gpos, gnrm, flags, w, L, sums)
-             : launch_adj_main<false>(sms, s, patches, hm, gpos, gnrm, flags, w, L, nullptr);
+    const uint32_t min_tiles = kAdjChunkMinTilesPerWarp * (uint32_t)(sms * occ * kAdjWarps);
+    e = launch_pdl(k_adj_scan, dim3(1), dim3(1024), 0, s, patches, n_patches, w, L,
+                   sums ? kAdjChunkSaved : kAdjChunkRecompute, min_tiles);
+    if (e != cudaSuccess) return e;
+    e = sums ? launch_adj_main<true>(sms, occ, s, patches, hm, gpos, gnrm, flags, w, L, sums)
+             : launch_adj_main<false>(sms, occ, s, patches, hm, gpos, gnrm, flags, w, L, nullptr);
     if (e != cudaSuccess) return e;
     const dim3 cg((max_waves_per_patch * kAdjRecord + 31) / 32, n_patches < 65535u ? n_patches : 65535u);
     e = launch_pdl(k_adj_cols, cg, dim3(32 * kColLanes), 0, s, n_patches, static_cast<const char*>(ws), L);

@@ -26,7 +26,8 @@ struct WsHeader {
     uint32_t n_patches;
     uint32_t tile_cols;    // vertices per tile row (32 * S)
     uint32_t total_chunks; // adjoint: tile chunks in its queue (0 = do not run)
-    uint32_t pad[57];
+    uint32_t adj_chunk;    // adjoint: tiles per chunk
+    uint32_t pad[56];
 };
 static_assert(sizeof(WsHeader) == 256, "header size");
 
