@@ -182,3 +182,29 @@ def test_saving_forward_outputs_and_batched_saved_adjoint(wt, oracle, gpu):
     _check(b, a, tol=2e-5)
     with pytest.raises(wt.WtError):
         surf.displace(flags=wt.WT_PHASE_FP32_NAIVE, sums=sums)
+
+
+def test_chunked_records_match_single_tile_records(wt, gpu):
+    """With at least 8 tiles per resident warp the recomputing adjoint takes
+    tiles two at a time into one record (header field adj_chunk = 2); its
+    gradients agree with the saved-sums adjoint (single-tile records) to FP32
+    rounding, and repeat bit for bit."""
+    import torch
+    from wave_tool_gb300 import workloads
+    w = workloads.config3(n_patches=64, seed=41)
+    surf = wt.Surface(w.patches, w.waves, wt.heightmap_from(w.heightmap))
+    sums = torch.empty((surf.n_vertices, 8), dtype=torch.float32, device="cuda")
+    surf.displace(flags=0, sums=sums)
+    gp, gn = _upstream(surf.n_vertices, 9)
+    gp, gn = gp.cuda(), gn.cuda()
+    a = surf.adjoint(gp, gn).clone()
+    torch.cuda.synchronize()
+    hdr = surf.adj_workspace[:32].cpu().numpy().view(np.uint32)
+    assert hdr[7] == 2, f"adj_chunk {hdr[7]}: the workload did not take the chunked path"
+    b = surf.adjoint(gp, gn).clone()
+    c = surf.adjoint(gp, gn, sums=sums)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+    hdr = surf.adj_workspace[:32].cpu().numpy().view(np.uint32)
+    assert hdr[7] == 1
+    _check(a.cpu().numpy().astype(np.float64), c.cpu().numpy().astype(np.float64), tol=2e-5)

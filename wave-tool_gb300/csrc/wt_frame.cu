@@ -27,7 +27,6 @@ using wt::StageOut;
 
 #define WT_HD __host__ __device__ inline
 
-constexpr double kPi = 3.14159265358979323846;
 
 // Constants of the reference's projected grid (src/render-engine.cpp).
 constexpr double kFrustumPad = 1.2;          // SAFETY_PADDING_SCALAR, :826
@@ -81,7 +80,7 @@ WT_HD void sincos_pi(double x, double* s, double* c) {
 #ifdef __CUDA_ARCH__
     sincospi(x, s, c);
 #else
-    sincos(x * kPi, s, c);
+    sincos(x * 3.14159265358979323846, s, c);
 #endif
 }
 
