@@ -34,6 +34,7 @@ using namespace wt::dev;
 
 constexpr uint32_t kNoPatch = 0xffffffffu;
 constexpr int kSortBins = 4096;
+constexpr uint32_t kRankSortMax = 64;
 
 __device__ __forceinline__ void flag_error(WsHeader* h, uint32_t code, uint32_t patch) {
     atomicCAS(&h->status, 0u, code);
@@ -48,6 +49,87 @@ __device__ bool wave_ok(const wt_wave& w) {
            finitef(w.steepness_q) && finitef(w.speed) && finitef(w.phase);
 }
 
+__device__ __forceinline__ unsigned long long to_fixed_turns(double turns) {
+    double f = turns - floor(turns);                 // [0, 1)
+    double hi = floor(f * 4294967296.0);             // < 2^32
+    double lo = floor((f * 4294967296.0 - hi) * 4294967296.0);
+    return ((unsigned long long)hi << 32) | (unsigned long long)lo;
+}
+
+// positive remainder of x by m (FP64)
+__device__ __forceinline__ double pmod(double x, double m) {
+    double r = x - m * floor(x / m);
+    return r >= m ? r - m : (r < 0.0 ? r + m : r);
+}
+
+// FP64 constants of wave w on patch Pt (the phase on the patch's bilinear grid
+// as 64-bit fixed-point turns, and the FP32 coefficients of the eight sums).
+__device__ PairCoef make_pair_coef(const wt_patch& Pt, const wt_wave w) {
+    double lam = w.wavelength;
+    double inv_lam = isinf(lam) ? 0.0 : 1.0 / lam;     // k / 2pi
+    double k = kTwoPi * inv_lam;
+    double Dx = w.dir_x, Dz = w.dir_z, A = w.amplitude, Q = w.steepness_q;
+    double blx = Pt.bl[0], blz = Pt.bl[1];
+    double e1x = (double)Pt.br[0] - blx, e1z = (double)Pt.br[1] - blz;
+    double e2x = (double)Pt.tl[0] - blx, e2z = (double)Pt.tl[1] - blz;
+    double e3x = (double)Pt.tr[0] - Pt.tl[0] - Pt.br[0] + blx;
+    double e3z = (double)Pt.tr[1] - Pt.tl[1] - Pt.br[1] + blz;
+    const double inv_cm1 = 1.0 / (double)(Pt.cols - 1), inv_rm1 = 1.0 / (double)(Pt.rows - 1);
+    // theta / 2pi at (col, row) = t00 + col*ta + row*tb + col*row*tg
+    double t00 = (Dx * blx + Dz * blz) * inv_lam + (double)w.speed * Pt.time_s * inv_lam +
+                 (double)w.phase * (1.0 / kTwoPi);
+    double ta = (Dx * e1x + Dz * e1z) * inv_lam * inv_cm1;
+    double tb = (Dx * e2x + Dz * e2z) * inv_lam * inv_rm1;
+    double tg = (Dx * e3x + Dz * e3z) * inv_lam * (inv_cm1 * inv_rm1);
+    PairCoef c;
+    c.t00 = to_fixed_turns(t00);
+    c.ta = to_fixed_turns(ta);
+    c.tb = to_fixed_turns(tb);
+    c.tg = to_fixed_turns(tg);
+    c.qadx = (float)(Q * A * Dx);
+    c.a = (float)A;
+    c.qadz = (float)(Q * A * Dz);
+    c.akdx = (float)(A * k * Dx);
+    c.akdz = (float)(A * k * Dz);
+    c.qakxx = (float)(Q * A * k * Dx * Dx);
+    c.qakxz = (float)(Q * A * k * Dx * Dz);
+    c.qakzz = (float)(Q * A * k * Dz * Dz);
+    return c;
+}
+
+// Per-patch constants: local frame, steps, texel origin reduced by the wrap
+// period in FP64, bounce, first coefficient slot.
+__device__ PatchAux make_patch_aux(const wt_patch& Pt, const HmDev& hm, uint32_t pair_offset) {
+    double blx = Pt.bl[0], blz = Pt.bl[1];
+    PatchAux a;
+    a.e1x = (float)((double)Pt.br[0] - blx);
+    a.e1z = (float)((double)Pt.br[1] - blz);
+    a.e2x = (float)((double)Pt.tl[0] - blx);
+    a.e2z = (float)((double)Pt.tl[1] - blz);
+    a.e3x = (float)((double)Pt.tr[0] - Pt.tl[0] - Pt.br[0] + blx);
+    a.e3z = (float)((double)Pt.tr[1] - Pt.tl[1] - Pt.br[1] + blz);
+    a.blx = Pt.bl[0];
+    a.blz = Pt.bl[1];
+    a.inv_cm1 = Pt.cols > 1 ? 1.0f / (float)(Pt.cols - 1) : 0.0f;
+    a.inv_rm1 = Pt.rows > 1 ? 1.0f / (float)(Pt.rows - 1) : 0.0f;
+    if (hm.present) {
+        double W = hm.width, H = hm.height;
+        double pu = hm.wrap == WT_WRAP_MIRRORED_REPEAT ? 2.0 * W : W;
+        double pv = hm.wrap == WT_WRAP_MIRRORED_REPEAT ? 2.0 * H : H;
+        // texel coordinate of the world point X: sample_scale*W*X - 0.5;
+        // the BL part is reduced by the wrap period in FP64
+        a.hu0 = (float)(pmod((double)hm.sample_scale * W * blx, pu) - 0.5);
+        a.hv0 = (float)(pmod(-(double)hm.sample_scale * H * blz, pv) - 0.5);
+        a.su = (float)((double)hm.sample_scale * W);
+        a.sv = (float)(-(double)hm.sample_scale * H);
+    } else {
+        a.hu0 = a.hv0 = a.su = a.sv = 0.0f;
+    }
+    a.y_offset = Pt.y_offset;
+    a.pair_offset = pair_offset;
+    return a;
+}
+
 // ---- stage 1: validation, prefix sums, LPT order ---------------------------
 __device__ __forceinline__ bool patch_ok(const wt_patch& P, uint32_t n_waves, uint64_t out_capacity) {
     const uint64_t verts = (uint64_t)P.cols * P.rows;
@@ -58,10 +140,14 @@ __device__ __forceinline__ bool patch_ok(const wt_patch& P, uint32_t n_waves, ui
            isfinite(P.time_s) && finitef(P.y_offset);
 }
 
+// fuse_coef: also form the per-(patch, wave) and per-patch constants here
+// (small tables: the host passes it when n_patches * n_waves <= 1024, one
+// pair per thread), so that no second prep kernel runs.
 __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__ patches, uint32_t n,
                                                     const wt_wave* __restrict__ waves, uint32_t n_waves,
                                                     uint64_t out_capacity, uint64_t coef_capacity,
-                                                    uint32_t tile_cols, char* ws, WsLayout L) {
+                                                    uint32_t tile_cols, char* ws, WsLayout L, HmDev hm,
+                                                    int fuse_coef) {
     WsHeader* hdr = reinterpret_cast<WsHeader*>(ws);
     uint32_t* sorted = reinterpret_cast<uint32_t*>(ws + L.sorted);
     uint32_t* tile_pre = reinterpret_cast<uint32_t*>(ws + L.tile_pre);
@@ -78,7 +164,11 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
         hdr->n_patches = n;
         hdr->tile_cols = tile_cols;
     }
-    for (int i = threadIdx.x; i < kSortBins; i += blockDim.x) bins[i] = 0;
+    // up to kRankSortMax patches are ordered by rank (their keys in bins[]),
+    // more by a counting sort over the bins
+    const bool rank_sort = n <= kRankSortMax;
+    if (!rank_sort)
+        for (int i = threadIdx.x; i < kSortBins; i += blockDim.x) bins[i] = 0;
     __syncthreads();
 
     // structural validation; pair_off <- wave counts of the patches that pass
@@ -89,7 +179,8 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
         pair_off[p] = ok ? P.wave_count : 0u;
         tiles[p] = ok ? P.rows * tiles_per_row(P.cols, tile_cols / 32) : 0u;
         const uint32_t key = P.wave_count < kSortBins ? P.wave_count : kSortBins - 1;
-        atomicAdd(&bins[kSortBins - 1 - key], 1u);  // descending wave count
+        if (rank_sort) bins[p] = key;
+        else atomicAdd(&bins[kSortBins - 1 - key], 1u);  // descending wave count
     }
     __syncthreads();
     const uint32_t total_pairs = block_exclusive_scan(pair_off, n);
@@ -128,14 +219,23 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
         for (uint32_t p = threadIdx.x; p <= n; p += blockDim.x) tile_pre[p] = 0;
         return;
     }
-    // counting sort by descending wave count (bin order), ties in any order:
-    // the order only schedules tiles, results do not depend on it
-    block_exclusive_scan(bins, kSortBins);
-    __syncthreads();
-    for (uint32_t p = threadIdx.x; p < n; p += blockDim.x) {
-        const uint32_t wc = patches[p].wave_count;
-        const uint32_t key = wc < kSortBins ? wc : kSortBins - 1;
-        sorted[atomicAdd(&bins[kSortBins - 1 - key], 1u)] = p;
+    // sort by descending wave count, ties in any order: the order only
+    // schedules tiles, results do not depend on it
+    if (rank_sort) {
+        for (uint32_t p = threadIdx.x; p < n; p += blockDim.x) {
+            const uint32_t key = bins[p];
+            uint32_t rank = 0;
+            for (uint32_t q = 0; q < n; ++q) rank += bins[q] > key || (bins[q] == key && q < p);
+            sorted[rank] = p;
+        }
+    } else {
+        block_exclusive_scan(bins, kSortBins);
+        __syncthreads();
+        for (uint32_t p = threadIdx.x; p < n; p += blockDim.x) {
+            const uint32_t wc = patches[p].wave_count;
+            const uint32_t key = wc < kSortBins ? wc : kSortBins - 1;
+            sorted[atomicAdd(&bins[kSortBins - 1 - key], 1u)] = p;
+        }
     }
     __syncthreads();
     for (uint32_t q = threadIdx.x; q < n; q += blockDim.x) tile_pre[q] = tiles[sorted[q]];
@@ -145,19 +245,20 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
         tile_pre[n] = total_tiles;
         hdr->total_tiles = total_tiles;
     }
-}
-
-__device__ __forceinline__ unsigned long long to_fixed_turns(double turns) {
-    double f = turns - floor(turns);                 // [0, 1)
-    double hi = floor(f * 4294967296.0);             // < 2^32
-    double lo = floor((f * 4294967296.0 - hi) * 4294967296.0);
-    return ((unsigned long long)hi << 32) | (unsigned long long)lo;
-}
-
-// positive remainder of x by m (FP64)
-__device__ __forceinline__ double pmod(double x, double m) {
-    double r = x - m * floor(x / m);
-    return r >= m ? r - m : (r < 0.0 ? r + m : r);
+    if (fuse_coef) {
+        PatchAux* aux = reinterpret_cast<PatchAux*>(ws + L.aux);
+        PairCoef* coef = reinterpret_cast<PairCoef*>(ws + L.coef);
+        for (uint32_t P = threadIdx.x; P < total_pairs; P += blockDim.x) {
+            uint32_t lo = 0, hi = n + 1;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (off[mid] <= P) lo = mid + 1; else hi = mid;
+            }
+            const wt_patch& Pt = patches[lo - 1];
+            coef[P] = make_pair_coef(Pt, waves[Pt.wave_offset + (P - off[lo - 1])]);
+        }
+        for (uint32_t p = threadIdx.x; p < n; p += blockDim.x) aux[p] = make_patch_aux(patches[p], hm, off[p]);
+    }
 }
 
 // ---- stage 2: FP64 constants per (patch, wave) and per patch ---------------
@@ -188,69 +289,10 @@ __global__ void __launch_bounds__(256) k_prep_coef(const wt_patch* __restrict__ 
         }
         uint32_t p = lo - 1;
         const wt_patch& Pt = patches[p];
-        const wt_wave w = waves[Pt.wave_offset + (P - pair_off[p])];
-        double lam = w.wavelength;
-        double inv_lam = isinf(lam) ? 0.0 : 1.0 / lam;     // k / 2pi
-        double k = kTwoPi * inv_lam;
-        double Dx = w.dir_x, Dz = w.dir_z, A = w.amplitude, Q = w.steepness_q;
-        double blx = Pt.bl[0], blz = Pt.bl[1];
-        double e1x = (double)Pt.br[0] - blx, e1z = (double)Pt.br[1] - blz;
-        double e2x = (double)Pt.tl[0] - blx, e2z = (double)Pt.tl[1] - blz;
-        double e3x = (double)Pt.tr[0] - Pt.tl[0] - Pt.br[0] + blx;
-        double e3z = (double)Pt.tr[1] - Pt.tl[1] - Pt.br[1] + blz;
-        const double inv_cm1 = 1.0 / (double)(Pt.cols - 1), inv_rm1 = 1.0 / (double)(Pt.rows - 1);
-        // theta / 2pi at (col, row) = t00 + col*ta + row*tb + col*row*tg
-        double t00 = (Dx * blx + Dz * blz) * inv_lam + (double)w.speed * Pt.time_s * inv_lam +
-                     (double)w.phase * (1.0 / kTwoPi);
-        double ta = (Dx * e1x + Dz * e1z) * inv_lam * inv_cm1;
-        double tb = (Dx * e2x + Dz * e2z) * inv_lam * inv_rm1;
-        double tg = (Dx * e3x + Dz * e3z) * inv_lam * (inv_cm1 * inv_rm1);
-        PairCoef c;
-        c.t00 = to_fixed_turns(t00);
-        c.ta = to_fixed_turns(ta);
-        c.tb = to_fixed_turns(tb);
-        c.tg = to_fixed_turns(tg);
-        c.qadx = (float)(Q * A * Dx);
-        c.a = (float)A;
-        c.qadz = (float)(Q * A * Dz);
-        c.akdx = (float)(A * k * Dx);
-        c.akdz = (float)(A * k * Dz);
-        c.qakxx = (float)(Q * A * k * Dx * Dx);
-        c.qakxz = (float)(Q * A * k * Dx * Dz);
-        c.qakzz = (float)(Q * A * k * Dz * Dz);
-        coef[P] = c;
+        coef[P] = make_pair_coef(Pt, waves[Pt.wave_offset + (P - pair_off[p])]);
     }
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
-        const wt_patch& Pt = patches[p];
-        double blx = Pt.bl[0], blz = Pt.bl[1];
-        PatchAux a;
-        a.e1x = (float)((double)Pt.br[0] - blx);
-        a.e1z = (float)((double)Pt.br[1] - blz);
-        a.e2x = (float)((double)Pt.tl[0] - blx);
-        a.e2z = (float)((double)Pt.tl[1] - blz);
-        a.e3x = (float)((double)Pt.tr[0] - Pt.tl[0] - Pt.br[0] + blx);
-        a.e3z = (float)((double)Pt.tr[1] - Pt.tl[1] - Pt.br[1] + blz);
-        a.blx = Pt.bl[0];
-        a.blz = Pt.bl[1];
-        a.inv_cm1 = Pt.cols > 1 ? 1.0f / (float)(Pt.cols - 1) : 0.0f;
-        a.inv_rm1 = Pt.rows > 1 ? 1.0f / (float)(Pt.rows - 1) : 0.0f;
-        if (hm.present) {
-            double W = hm.width, H = hm.height;
-            double pu = hm.wrap == WT_WRAP_MIRRORED_REPEAT ? 2.0 * W : W;
-            double pv = hm.wrap == WT_WRAP_MIRRORED_REPEAT ? 2.0 * H : H;
-            // texel coordinate of the world point X: sample_scale*W*X - 0.5;
-            // the BL part is reduced by the wrap period in FP64
-            a.hu0 = (float)(pmod((double)hm.sample_scale * W * blx, pu) - 0.5);
-            a.hv0 = (float)(pmod(-(double)hm.sample_scale * H * blz, pv) - 0.5);
-            a.su = (float)((double)hm.sample_scale * W);
-            a.sv = (float)(-(double)hm.sample_scale * H);
-        } else {
-            a.hu0 = a.hv0 = a.su = a.sv = 0.0f;
-        }
-        a.y_offset = Pt.y_offset;
-        a.pair_offset = pair_off[p];
-        aux[p] = a;
-    }
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride)
+        aux[p] = make_patch_aux(patches[p], hm, pair_off[p]);
 }
 
 // ---- stage 3: the persistent forward kernel --------------------------------
@@ -478,9 +520,13 @@ cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wa
     // coefficient capacity = what the caller's workspace holds past the fixed part
     // (the header records the real total; the scan refuses to overflow it)
     uint64_t coef_cap = (L.end - L.coef) / sizeof(PairCoef);
-    k_prep_scan<<<1, 1024, 0, s>>>(patches, n_patches, waves, n_waves, out_capacity, coef_cap, tile_cols, w, L);
+    // at most 1024 (patch, wave) pairs: the scan kernel forms the constants too
+    const int fuse = (uint64_t)n_patches * n_waves <= 1024u;
+    k_prep_scan<<<1, 1024, 0, s>>>(patches, n_patches, waves, n_waves, out_capacity, coef_cap, tile_cols, w, L,
+                                   hm, fuse);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (fuse) return cudaSuccess;
     const int sms = sm_count();
     if (sms <= 0) return cudaErrorInvalidDevice;
     cudaLaunchConfig_t lc = {};
