@@ -76,3 +76,35 @@ def test_projected_grid_async_and_unorm8_reject_bad_arguments(wt, L):
     assert L.wt_heightmap_from_unorm8(FAKE, 16, 16, 4, 64, 2, FAKE, None) == E   # flip flag
     assert L.wt_heightmap_from_unorm8(None, 16, 16, 4, 64, 1, FAKE, None) == E
     assert L.wt_heightmap_from_unorm8(FAKE, 0, 16, 4, 64, 1, FAKE, None) == E
+
+
+def test_saving_and_stage_entry_points_reject_bad_arguments(wt, L):
+    """wt_gerstner_displace_saving / _stage and wt_gerstner_adjoint_saved:
+    their own arguments are checked before the shared ones and before any
+    CUDA call."""
+    E, U = wt.abi.WT_ERR_INVALID_ARG, wt.abi.WT_ERR_UNSUPPORTED
+    # displace_saving(patches, n, waves, nw, hm, pos, nrm, cap, flags, sums, ws, bytes, stream)
+    assert L.wt_gerstner_displace_saving(FAKE, 1, FAKE, 1, None, FAKE, FAKE, 10, 0, None, FAKE, 1 << 20, None) == E
+    assert L.wt_gerstner_displace_saving(FAKE, 1, FAKE, 1, None, FAKE, FAKE, 10, 0, ODD, FAKE, 1 << 20, None) == E
+    assert L.wt_gerstner_displace_saving(FAKE, 1, FAKE, 1, None, FAKE, FAKE, 10, wt.WT_PHASE_FP32_NAIVE, FAKE,
+                                         FAKE, 1 << 20, None) == U
+    L.wt_gerstner_displace_saving(FAKE, 1, FAKE, 1, None, FAKE, FAKE, 10, 0, None, FAKE, 1 << 20, None)
+    assert b"sums" in L.wt_last_error()
+    # adjoint_saved(host_patches, patches, n, waves, nw, hm, d_pos, d_nrm, cap, flags, sums, grad, ws, bytes, stream)
+    assert L.wt_gerstner_adjoint_saved(FAKE, FAKE, 1, FAKE, 1, None, FAKE, FAKE, 10, 0, None, FAKE, FAKE,
+                                       1 << 20, None) == E
+    assert L.wt_gerstner_adjoint_saved(FAKE, FAKE, 1, FAKE, 1, None, FAKE, FAKE, 10, 0, ODD, FAKE, FAKE,
+                                       1 << 20, None) == E
+    # displace_stage(patches, n, waves, nw, hm, view, pos, nrm, cap, flags, outputs, ws, bytes, stream)
+    so = wt.CStageOutputs(FAKE, FAKE, FAKE, FAKE, FAKE)
+    stage = L.wt_gerstner_displace_stage
+    assert stage(FAKE, 1, FAKE, 1, None, None, None, None, 10, 0, C.byref(so), FAKE, 1 << 20, None) == E  # no view
+    assert stage(FAKE, 1, FAKE, 1, None, FAKE, None, None, 10, 0, None, FAKE, 1 << 20, None) == E  # no outputs
+    assert stage(FAKE, 1, FAKE, 1, None, FAKE, None, None, 10, wt.WT_OUT_DISPLACEMENT, C.byref(so), FAKE,
+                 1 << 20, None) == E
+    for field in ("clip", "view", "facing", "nrm_yaw"):
+        bad = wt.CStageOutputs(FAKE, FAKE, FAKE, FAKE, FAKE)
+        setattr(bad, field, ODD)
+        assert stage(FAKE, 1, FAKE, 1, None, FAKE, None, None, 10, 0, C.byref(bad), FAKE, 1 << 20, None) == E, field
+    bad = wt.CStageOutputs(FAKE, FAKE + 4, FAKE, FAKE, FAKE)  # ndc0 needs 8-byte alignment
+    assert stage(FAKE, 1, FAKE, 1, None, FAKE, None, None, 10, 0, C.byref(bad), FAKE, 1 << 20, None) == E
