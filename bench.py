@@ -51,6 +51,8 @@ def parse_args():
     ap.add_argument("--mode", choices=["forward", "adjoint", "frame"], default="forward",
                     help="'adjoint' times only wt_gerstner_adjoint on 64 uneven patches, 'frame' only the "
                          "camera-to-pixels water frame (for profiling)")
+    ap.add_argument("--no-heightmap", action="store_true",
+                    help="the batched workload without its noise layer (for instruction-mix comparisons)")
     ap.add_argument("--saved-sums", action="store_true",
                     help="with --mode adjoint: time wt_gerstner_adjoint_saved on a saving forward's sums")
     ap.add_argument("--tuning", default="auto",
@@ -401,6 +403,8 @@ def run_ours(args):
     from wave_tool_gb300 import workloads
 
     w = workloads.config3(n_patches=args.patches, seed=2 + rank)
+    if args.no_heightmap:
+        w.heightmap = None
     hm = wt.heightmap_from(w.heightmap)
     surf = wt.Surface(w.patches, w.waves, hm)
     surf.n_terms_cache = w.n_terms
@@ -464,7 +468,7 @@ def run_ours(args):
     epos, enrm = surf.alloc_outputs(e2e_flags)
     hpos = torch.empty(epos.shape, dtype=epos.dtype, pin_memory=True)
     hnrm = torch.empty(enrm.shape, dtype=enrm.dtype, pin_memory=True)
-    htex = hm.texels.cpu().pin_memory()
+    htex = hm.texels.cpu().pin_memory() if hm is not None else None
     hw = torch.from_numpy(np.ascontiguousarray(w.waves).view(np.uint8).reshape(-1)).pin_memory()
     cum = np.cumsum(w.patches["cols"].astype(np.int64) * w.patches["rows"] * w.patches["wave_count"])
     cuts = [0] + [int(np.searchsorted(cum, cum[-1] * (g + 1) / E2E_GROUPS)) + 1 for g in range(E2E_GROUPS - 1)] + \
@@ -479,11 +483,12 @@ def run_ours(args):
         gs = wt.Surface(sub, w.waves, hm)
         hp_g = torch.from_numpy(np.ascontiguousarray(sub).view(np.uint8).reshape(-1)).pin_memory()
         groups.append((gs, hp_g, o0, o1, torch.cuda.Stream()))
-    h2d = htex.numel() * 4 + sum(g[1].numel() + hw.numel() for g in groups)
+    h2d = (htex.numel() * 4 if htex is not None else 0) + sum(g[1].numel() + hw.numel() for g in groups)
     d2h = hpos.numel() * 4 + hnrm.numel() * 4
 
     def e2e_step():
-        hm.texels.copy_(htex, non_blocking=True)
+        if htex is not None:
+            hm.texels.copy_(htex, non_blocking=True)
         main = torch.cuda.current_stream()
         for gs, hp_g, o0, o1, st in groups:
             st.wait_stream(main)
@@ -594,7 +599,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (SplitMix64 seed 2 + rank)",
             "config": {"workload": w.name, "patches": args.patches, "vertices": verts, "terms_per_step": terms,
-                       "waves_per_patch": "8..64", "grid_side": "64..1024 log-uniform", "heightmap": "512^2 noise",
+                       "waves_per_patch": "8..64", "grid_side": "64..1024 log-uniform", "heightmap": "none" if args.no_heightmap else "512^2 noise",
                        "outputs": "float4 displacement + float4 normal (e2e: packed vec3 world position + "
                                   "normal, the reference's vertex-array layout)", "phase": "FP64-reduced",
                        "l2": "256 MiB buffer zeroed between timed steps (outside the per-step events)",
