@@ -290,6 +290,21 @@ def frame_pipeline(wt, workloads, stream, flush):
     fsms = _event_ms(F["displace_stage"], 20, stream, flush)
     rms = _event_ms(raster, 20, stream, flush)
     sms = _event_ms(shade, 20, stream, flush)
+    # the noise layer animated per frame (64 terms over 512^2 texels): what a
+    # frame adds when it resynthesises the heightmap at the frame time
+    hw = workloads.config2().heightmap
+    nterms = wt.to_device(hw.terms)
+    nrates = torch.linspace(-2.0, 2.0, len(hw.terms), device="cuda")
+    ntex = torch.empty((hw.height, hw.width), dtype=torch.float32, device="cuda")
+    nws = wt.empty_bytes(wt.noise_workspace_bytes(len(hw.terms), hw.width, hw.height))
+    nclock = [0.0]
+
+    def noise_frame():
+        nclock[0] += 1.0 / 60.0
+        wt.noise_synth(nterms, hw.width, hw.height, rates=nrates, time_s=nclock[0], out=ntex, workspace=nws)
+    for _ in range(3):
+        noise_frame()
+    nms = _event_ms(noise_frame, 20, stream, flush)
     covered = float(((frags & 0xffffffff) != 0).float().mean())
     stage_bytes = n * (2 * 16 + 16 + 8 + 3 * 16)  # reads pos + nrm, writes clip, ndc0, view, facing, nrm_yaw
     try:
@@ -300,6 +315,7 @@ def frame_pipeline(wt, workloads, stream, flush):
     return {"vertices": n, "terms": n * F["waves"], "viewport": [VW, VH], "water_pixels_frac": covered,
             "displace_tuning": F["tuning"],
             "frame_graph_ms": fms, "frame_graph_unfused_ms": graph_ms[False], "raster_ms": rms, "shade_ms": sms,
+            "noise_512sq_64terms_animated_ms": nms,
             "displace_with_fused_stage_ms": fsms,
             "frames_per_s": 1e3 / fms, "projected_grid_kernel_ms": gms, "displace_ms": dms,
             "vertex_stage_ms": vms, "vertex_stage_bytes": stage_bytes,

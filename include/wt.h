@@ -268,12 +268,26 @@ wt_status wt_grid_indices(uint32_t cols, uint32_t rows, uint32_t base_vertex,
 
 /* Tileable noise heightmap: sum of integer-wavenumber sinusoids over a
  * width x height texel grid, then normalised to [0, 1] (min -> 0, max -> 1)
- * so the reference's 2*(r - 0.5) mapping (water-grid.vert:106-111) holds.
- * terms: device array.  Needs 16 bytes of workspace.  No reference
- * counterpart: the reference loads a fixed PNG (render-engine.cpp:1308-1322). */
+ * so the reference's 2*(r - 0.5) mapping (water-grid.vert:106-111) holds:
+ *   h(i, j) = sum_m a_m sin(2 pi (kx_m i / width + ky_m j / height) + phase_m).
+ * terms: device array.  workspace: wt_noise_workspace_size bytes (the
+ * separable factor tables, 8 bytes per term and texel row / column, and the
+ * min / max).  No reference counterpart: the reference loads a fixed PNG
+ * (render-engine.cpp:1308-1322). */
+wt_status wt_noise_workspace_size(uint32_t n_terms, uint32_t width, uint32_t height, size_t* bytes);
 wt_status wt_noise_synth(const wt_noise_term* terms, uint32_t n_terms,
                          uint32_t width, uint32_t height, float* texels_out,
                          void* workspace, size_t workspace_bytes, wt_stream stream);
+
+/* The same heightmap animated in time: term m's phase advances by rates[m]
+ * radians per second, phase_m + rates[m] * time_s (FP64, reduced mod 2 pi
+ * before the sine), so that calling it every frame with the frame time
+ * animates the noise layer (the "animate the heightmap displacement values
+ * over time" TODO at water-grid.vert:113).  rates: device array or NULL
+ * (static).  Same workspace as wt_noise_synth. */
+wt_status wt_noise_synth_animated(const wt_noise_term* terms, uint32_t n_terms, const float* rates,
+                                  double time_s, uint32_t width, uint32_t height, float* texels_out,
+                                  void* workspace, size_t workspace_bytes, wt_stream stream);
 
 /* ---- frame set-up and the rest of the vertex stage ----------------------- */
 

@@ -24,10 +24,11 @@ void wto_grid_indices(uint32_t cols, uint32_t rows, uint32_t base_vertex, uint32
     }
 }
 
-/* h(i, j) = sum_m a_m sin(2*pi*(kx_m*i/width + ky_m*j/height) + psi_m), then
- * (h - min) / (max - min).  Integer wavenumbers make it tile. */
-void wto_noise_f64(const wt_noise_term* terms, uint32_t n_terms, uint32_t width,
-                   uint32_t height, double* out) {
+/* h(i, j) = sum_m a_m sin(2*pi*(kx_m*i/width + ky_m*j/height) + psi_m + r_m*t),
+ * then (h - min) / (max - min).  Integer wavenumbers make it tile; rates
+ * (NULL = none) animate it in time. */
+void wto_noise_f64_at(const wt_noise_term* terms, uint32_t n_terms, const float* rates, double time_s,
+                      uint32_t width, uint32_t height, double* out) {
     const double two_pi = 6.283185307179586476925286766559;
     double lo = INFINITY, hi = -INFINITY;
     for (uint32_t j = 0; j < height; ++j)
@@ -38,7 +39,8 @@ void wto_noise_f64(const wt_noise_term* terms, uint32_t n_terms, uint32_t width,
                 long long ni = ((long long)terms[m].kx * i) % (long long)width;
                 long long nj = ((long long)terms[m].ky * j) % (long long)height;
                 double turns = (double)ni / width + (double)nj / height;
-                h += (double)terms[m].amplitude * sin(two_pi * turns + (double)terms[m].phase);
+                double psi = (double)terms[m].phase + (rates ? (double)rates[m] * time_s : 0.0);
+                h += (double)terms[m].amplitude * sin(two_pi * turns + psi);
             }
             out[(size_t)j * width + i] = h;
             if (h < lo) lo = h;
@@ -47,4 +49,9 @@ void wto_noise_f64(const wt_noise_term* terms, uint32_t n_terms, uint32_t width,
     double span = hi - lo;
     size_t n = (size_t)width * height;
     for (size_t v = 0; v < n; ++v) out[v] = span > 0.0 ? (out[v] - lo) / span : 0.0;
+}
+
+void wto_noise_f64(const wt_noise_term* terms, uint32_t n_terms, uint32_t width,
+                   uint32_t height, double* out) {
+    wto_noise_f64_at(terms, n_terms, NULL, 0.0, width, height, out);
 }

@@ -90,6 +90,7 @@ def lib():
             f.restype = C.c_uint64
         _lib.wto_grid_indices.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, vp]
         _lib.wto_noise_f64.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, vp]
+        _lib.wto_noise_f64_at.argtypes = [vp, C.c_uint32, vp, C.c_double, C.c_uint32, C.c_uint32, vp]
         _lib.wto_wave_to_reference.argtypes = [vp, C.POINTER(RefWave)]
         for f in (_lib.wto_projected_grid_f32, _lib.wto_projected_grid_f64):
             f.argtypes = [vp, vp, vp, vp, C.POINTER(C.c_uint32)]
@@ -359,10 +360,11 @@ def grid_indices(cols, rows, base=0):
     return out
 
 
-def noise_f64(terms, width, height):
+def noise_f64(terms, width, height, rates=None, time_s=0.0):
     out = np.zeros((height, width))
     t = np.ascontiguousarray(terms)
-    lib().wto_noise_f64(_ptr(t), len(t), width, height, _ptr(out))
+    r = None if rates is None else np.ascontiguousarray(rates, dtype=np.float32)
+    lib().wto_noise_f64_at(_ptr(t), len(t), None if r is None else _ptr(r), float(time_s), width, height, _ptr(out))
     return out
 
 

@@ -139,7 +139,10 @@ void wto_wave_to_reference(const wt_wave* w, wto_ref_wave* out);
 /* src/program.cpp:686-717 generalised to cols x rows and a base vertex. */
 void wto_grid_indices(uint32_t cols, uint32_t rows, uint32_t base_vertex, uint32_t* out);
 
-/* FP64 noise heightmap normalised to [0, 1]. */
+/* FP64 noise heightmap normalised to [0, 1]; the _at form with per-term phase
+ * rates (radians per second, NULL = none) at time_s. */
+void wto_noise_f64_at(const wt_noise_term* terms, uint32_t n_terms, const float* rates, double time_s,
+                      uint32_t width, uint32_t height, double* out);
 void wto_noise_f64(const wt_noise_term* terms, uint32_t n_terms, uint32_t width,
                    uint32_t height, double* out);
 

@@ -40,6 +40,38 @@ def test_noise_matches_f64(wt, oracle, gpu):
             assert got.min() == 0.0 and got.max() == 1.0
 
 
+@pytest.mark.parametrize("time_s", [0.0, 1.7, 3.0e4])
+def test_animated_noise_matches_f64(wt, oracle, gpu, time_s):
+    """wt_noise_synth_animated: each term's phase advanced by its rate x t
+    (FP64 reduction on the device) against the FP64 restatement."""
+    from wave_tool_gb300 import workloads
+    for (w, h, n, k, seed) in ((512, 512, 64, 32, 4), (37, 21, 9, 5, 5)):
+        terms = workloads.noise_terms(workloads.SplitMix64(seed), n=n, kmax=k)
+        rng = np.random.default_rng(seed)
+        rates = rng.uniform(-3.0, 3.0, n).astype(np.float32)
+        got = wt.noise_synth(terms, w, h, rates=rates, time_s=time_s).cpu().numpy()
+        exp = oracle.noise_f64(terms, w, h, rates=rates, time_s=time_s)
+        assert np.abs(got - exp).max() < 2e-5
+        assert got.min() == 0.0 and got.max() == 1.0
+
+
+def test_animated_noise_period_and_workspace(wt, gpu):
+    """Rates of whole turns per second: the layer at t = 1 s is the layer at
+    t = 0; a workspace below wt_noise_workspace_size is refused."""
+    import torch
+    from wave_tool_gb300 import workloads
+    terms = workloads.noise_terms(workloads.SplitMix64(8), n=16, kmax=8)
+    rates = (2.0 * np.pi * np.arange(1, 17)).astype(np.float32)
+    a = wt.noise_synth(terms, 64, 48, rates=rates, time_s=0.0)
+    b = wt.noise_synth(terms, 64, 48, rates=rates, time_s=1.0)
+    assert float((a - b).abs().max()) < 2e-5
+    need = wt.noise_workspace_bytes(16, 64, 48)
+    assert need == 256 + 8 * 16 * (64 + 48)
+    with pytest.raises(wt.WtError):
+        wt.noise_synth(terms, 64, 48, workspace=wt.empty_bytes(need - 16))
+    del torch
+
+
 def test_device_side_validation(wt, gpu):
     """Invalid patches are skipped and reported with the first bad index."""
     import torch

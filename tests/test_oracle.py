@@ -294,3 +294,21 @@ def test_adjoint_oracle_matches_finite_differences(oracle):
             fd = (loss(wp)[0] - loss(wm)[0]) / (2 * fd_h)
             an = grad[i, f]
             assert abs(fd - an) <= 2e-3 * max(1.0, abs(an)), (i, name, fd, an)
+
+
+def test_noise_animation_restatement(oracle):
+    """The FP64 noise at time t with rates r equals the static noise with the
+    phases advanced by r t; whole turns per second repeat every second."""
+    import numpy as np
+    from wave_tool_gb300 import workloads
+    terms = workloads.noise_terms(workloads.SplitMix64(3), n=12, kmax=6)
+    rates = np.linspace(-2.0, 2.0, 12).astype(np.float32)
+    moved = terms.copy()
+    moved["phase"] = (terms["phase"].astype(np.float64) + rates.astype(np.float64) * 0.75).astype(np.float32)
+    a = oracle.noise_f64(terms, 20, 12, rates=rates, time_s=0.75)
+    b = oracle.noise_f64(moved, 20, 12)
+    assert np.abs(a - b).max() < 1e-6
+    whole = (2.0 * np.pi * np.arange(1, 13)).astype(np.float32)
+    c = oracle.noise_f64(terms, 20, 12, rates=whole, time_s=1.0)
+    d = oracle.noise_f64(terms, 20, 12)
+    assert np.abs(c - d).max() < 1e-5

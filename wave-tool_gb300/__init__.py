@@ -36,6 +36,7 @@ EXPORTED = [
     "wt_projected_grid", "wt_projected_grid_async", "wt_vertex_stage", "wt_heightmap_from_unorm8",
     "wt_water_raster", "wt_water_raster_workspace_size", "wt_water_shade",
     "wt_gerstner_displace_saving", "wt_gerstner_adjoint_saved", "wt_gerstner_displace_stage",
+    "wt_noise_workspace_size", "wt_noise_synth_animated",
 ]
 
 
@@ -119,6 +120,8 @@ def lib():
                                                  C.POINTER(CStageOutputs), vp, sz, vp]
         L.wt_grid_indices.argtypes = [u32, u32, u32, vp, vp]
         L.wt_noise_synth.argtypes = [vp, u32, u32, u32, vp, vp, sz, vp]
+        L.wt_noise_workspace_size.argtypes = [u32, u32, u32, C.POINTER(sz)]
+        L.wt_noise_synth_animated.argtypes = [vp, u32, vp, C.c_double, u32, u32, vp, vp, sz, vp]
         L.wt_wave_from_reference.argtypes = [C.c_float] * 6 + [u32, C.POINTER(CWave)]
         L.wt_measure_peaks.argtypes = [vp, sz, C.POINTER(C.c_double), C.POINTER(C.c_double), vp]
         L.wt_set_tuning.argtypes = [C.POINTER(CTuning)]
@@ -342,14 +345,32 @@ def grid_indices(cols: int, rows: int, base_vertex: int = 0, stream=None):
     return out
 
 
-def noise_synth(terms: np.ndarray, width: int, height: int, stream=None):
+def noise_workspace_bytes(n_terms: int, width: int, height: int) -> int:
+    out = C.c_size_t()
+    check(lib().wt_noise_workspace_size(n_terms, width, height, C.byref(out)))
+    return out.value
+
+
+def noise_synth(terms: np.ndarray, width: int, height: int, stream=None, rates=None, time_s: float = 0.0,
+                out=None, workspace=None):
+    """The noise heightmap (h, w) on the device; with `rates` (radians per
+    second per term, host array or device tensor) the layer at `time_s`."""
     torch = _torch()
-    assert terms.dtype == NOISE_TERM_DTYPE
-    t = to_device(terms)
-    out = torch.empty((height, width), dtype=torch.float32, device="cuda")
-    ws = empty_bytes(256)
-    check(lib().wt_noise_synth(t.data_ptr(), len(terms), width, height, out.data_ptr(), ws.data_ptr(),
-                               ws.numel(), stream_handle(stream)))
+    if isinstance(terms, np.ndarray):
+        assert terms.dtype == NOISE_TERM_DTYPE
+        t = to_device(terms)
+    else:
+        t = terms
+    n = t.numel() // NOISE_TERM_DTYPE.itemsize if t.dtype == torch.uint8 else len(terms)
+    if out is None:
+        out = torch.empty((height, width), dtype=torch.float32, device="cuda")
+    if workspace is None:
+        workspace = empty_bytes(noise_workspace_bytes(n, width, height))
+    r = None
+    if rates is not None:
+        r = rates if hasattr(rates, "data_ptr") else torch.as_tensor(np.asarray(rates, np.float32), device="cuda")
+    check(lib().wt_noise_synth_animated(t.data_ptr(), n, _ptr(r), float(time_s), width, height, out.data_ptr(),
+                                        workspace.data_ptr(), workspace.numel(), stream_handle(stream)))
     return out
 
 

@@ -341,17 +341,38 @@ wt_status wt_grid_indices(uint32_t cols, uint32_t rows, uint32_t base_vertex, ui
     return WT_OK;
 }
 
-wt_status wt_noise_synth(const wt_noise_term* terms, uint32_t n_terms, uint32_t width, uint32_t height,
-                         float* texels_out, void* workspace, size_t workspace_bytes, wt_stream stream) {
+wt_status wt_noise_workspace_size(uint32_t n_terms, uint32_t width, uint32_t height, size_t* bytes) {
+    if (!bytes) return fail(WT_ERR_INVALID_ARG, "bytes is NULL");
+    if (width < 1 || height < 1 || width > 32768 || height > 32768)
+        return fail(WT_ERR_INVALID_ARG, "noise size %ux%u outside [1, 32768]", width, height);
+    *bytes = wt::noise_workspace_bytes(n_terms, width, height);
+    return WT_OK;
+}
+
+wt_status wt_noise_synth_animated(const wt_noise_term* terms, uint32_t n_terms, const float* rates, double time_s,
+                                  uint32_t width, uint32_t height, float* texels_out, void* workspace,
+                                  size_t workspace_bytes, wt_stream stream) {
     if (width < 1 || height < 1 || width > 32768 || height > 32768)
         return fail(WT_ERR_INVALID_ARG, "noise size %ux%u outside [1, 32768]", width, height);
     if (n_terms > 0 && !terms) return fail(WT_ERR_INVALID_ARG, "terms is NULL");
+    if (terms && !aligned(terms, 4)) return fail(WT_ERR_INVALID_ARG, "terms not 4-byte aligned");
+    if (rates && !aligned(rates, 4)) return fail(WT_ERR_INVALID_ARG, "rates not 4-byte aligned");
+    if (!std::isfinite(time_s)) return fail(WT_ERR_INVALID_ARG, "time_s not finite");
     if (!texels_out || !aligned(texels_out, 4)) return fail(WT_ERR_INVALID_ARG, "texels_out NULL or misaligned");
     if (!workspace || !aligned(workspace, 16)) return fail(WT_ERR_INVALID_ARG, "workspace NULL or misaligned");
-    if (workspace_bytes < 16) return fail(WT_ERR_NOMEM, "noise needs 16 bytes of workspace");
-    cudaError_t e = wt::launch_noise(terms, n_terms, width, height, texels_out, workspace, (cudaStream_t)stream);
+    const size_t need = wt::noise_workspace_bytes(n_terms, width, height);
+    if (workspace_bytes < need)
+        return fail(WT_ERR_NOMEM, "noise needs %zu bytes of workspace (wt_noise_workspace_size)", need);
+    cudaError_t e = wt::launch_noise(terms, n_terms, rates, time_s, width, height, texels_out, workspace,
+                                     (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "noise launch");
     return WT_OK;
+}
+
+wt_status wt_noise_synth(const wt_noise_term* terms, uint32_t n_terms, uint32_t width, uint32_t height,
+                         float* texels_out, void* workspace, size_t workspace_bytes, wt_stream stream) {
+    return wt_noise_synth_animated(terms, n_terms, nullptr, 0.0, width, height, texels_out, workspace,
+                                   workspace_bytes, stream);
 }
 
 wt_status wt_heightmap_from_unorm8(const uint8_t* pixels, uint32_t width, uint32_t height, uint32_t channels,

@@ -176,8 +176,10 @@ int sm_count();
 cudaError_t launch_indices(uint32_t cols, uint32_t rows, uint32_t base, uint32_t* out, cudaStream_t s);
 cudaError_t launch_unorm8(const uint8_t* px, uint32_t w, uint32_t h, uint32_t channels, uint64_t stride,
                           uint32_t flip, float* out, cudaStream_t s);
-cudaError_t launch_noise(const wt_noise_term* terms, uint32_t n_terms, uint32_t w, uint32_t h,
-                         float* out, void* ws, cudaStream_t s);
+// rates: NULL or per-term phase rates (radians per second) at time t
+cudaError_t launch_noise(const wt_noise_term* terms, uint32_t n_terms, const float* rates, double t, uint32_t w,
+                         uint32_t h, float* out, void* ws, cudaStream_t s);
+size_t noise_workspace_bytes(uint32_t n_terms, uint32_t w, uint32_t h);
 cudaError_t measure_peaks(void* scratch, size_t bytes, double* fma, double* sin, cudaStream_t s);
 
 }  // namespace wt

@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(256) k_unorm8(const uint8_t* __restrict__ px, 
 }
 
 // ---- noise heightmap -------------------------------------------------------
+constexpr size_t kNoiseHeader = 256;  // workspace: min / max, then the factor tables
 __device__ __forceinline__ uint32_t ordered(float f) {
     uint32_t b = __float_as_uint(f);
     return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
@@ -59,41 +60,87 @@ __global__ void k_noise_init(uint32_t* mm) {
     mm[1] = 0u;           // max (ordered)
 }
 
-// h(i, j) = sum a sin(2*pi*((kx*i mod W)/W + (ky*j mod H)/H) + psi): the
-// integer products are reduced exactly before the turn is formed.
-__global__ void __launch_bounds__(256) k_noise(const wt_noise_term* __restrict__ terms, uint32_t n_terms, uint32_t W,
-                                               uint32_t H, float* __restrict__ out, uint32_t* mm) {
-    __shared__ float4 st[256];
-    const uint32_t i = blockIdx.x * 16 + (threadIdx.x & 15);
-    const uint32_t j = blockIdx.y * 16 + (threadIdx.x >> 4);
-    const bool in = i < W && j < H;
-    float h = 0.0f;
-    for (uint32_t b = 0; b < n_terms; b += 256) {
+// h(i, j) = sum_m a_m sin(x_m(i) + y_m(j)),
+//   x_m(i) = 2 pi (kx_m i mod W) / W,  y_m(j) = 2 pi (ky_m j mod H) / H + psi_m + rate_m t,
+// is separable: sin(x + y) = sin x cos y + cos x sin y.  k_noise_tables forms,
+// once per term, the column factors (sin x, cos x) for every column and the
+// row factors a (cos y, sin y) for every row (integer products reduced
+// exactly, the time-shifted row turn reduced in FP64, sines by FP32
+// sincospi); k_noise_tiles then spends two FMAs per texel and term.
+constexpr uint32_t kNoiseTile = 32;     // texels per block side (16 x 16 threads, 2 x 2 each)
+constexpr uint32_t kNoiseChunk = 32;    // terms staged in shared memory at a time
+
+__global__ void __launch_bounds__(256) k_noise_tables(const wt_noise_term* __restrict__ terms, uint32_t n_terms,
+                                                      const float* __restrict__ rates, double t, uint32_t W,
+                                                      uint32_t H, float2* __restrict__ col, float2* __restrict__ row) {
+    const uint64_t per = (uint64_t)W + H, n = per * n_terms;
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t m = (uint32_t)(k / per);
+        const uint32_t r = (uint32_t)(k - (uint64_t)m * per);
+        const wt_noise_term tm = terms[m];
+        float sn, cs;
+        if (r < W) {
+            long long ni = ((long long)tm.kx * r) % (long long)W;
+            ni += ni < 0 ? W : 0;
+            sincospif(2.0f * (float)((double)ni / W), &sn, &cs);
+            col[(size_t)m * W + r] = make_float2(sn, cs);
+        } else {
+            const uint32_t j = r - W;
+            long long nj = ((long long)tm.ky * j) % (long long)H;
+            nj += nj < 0 ? H : 0;
+            // the row's turn: exact fraction plus (psi + rate t) / 2 pi,
+            // reduced mod 1 in FP64 (t may be large), then an FP32 sincospi
+            double turns = (double)nj / H + ((double)tm.phase + (rates ? (double)rates[m] * t : 0.0)) *
+                                                (0.5 / 3.14159265358979323846);
+            turns -= floor(turns);
+            sincospif(2.0f * (float)turns, &sn, &cs);
+            row[(size_t)m * H + j] = make_float2(tm.amplitude * cs, tm.amplitude * sn);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_noise_tiles(const float2* __restrict__ col, const float2* __restrict__ row,
+                                                     uint32_t n_terms, uint32_t W, uint32_t H,
+                                                     float* __restrict__ out, uint32_t* mm) {
+    __shared__ float2 sc[kNoiseChunk][kNoiseTile], sr[kNoiseChunk][kNoiseTile];
+    const uint32_t tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const uint32_t i0 = blockIdx.x * kNoiseTile, j0 = blockIdx.y * kNoiseTile;
+    float h[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+    for (uint32_t m0 = 0; m0 < n_terms; m0 += kNoiseChunk) {
+        const uint32_t nm = min(kNoiseChunk, n_terms - m0);
         __syncthreads();
-        if (b + threadIdx.x < n_terms) {
-            wt_noise_term t = terms[b + threadIdx.x];
-            float sp, cp;
-            sincosf(t.phase, &sp, &cp);
-            st[threadIdx.x] = make_float4(__int_as_float(t.kx), __int_as_float(t.ky), t.amplitude * cp,
-                                          t.amplitude * sp);
+        for (uint32_t e = threadIdx.x; e < kNoiseChunk * kNoiseTile; e += blockDim.x) {
+            const uint32_t m = e / kNoiseTile, q = e - m * kNoiseTile;
+            const bool tm = m < nm;
+            sc[m][q] = tm && i0 + q < W ? col[(size_t)(m0 + m) * W + i0 + q] : make_float2(0.0f, 0.0f);
+            sr[m][q] = tm && j0 + q < H ? row[(size_t)(m0 + m) * H + j0 + q] : make_float2(0.0f, 0.0f);
         }
         __syncthreads();
-        const uint32_t nb = min(256u, n_terms - b);
-        for (uint32_t m = 0; m < nb; ++m) {
-            float4 t = st[m];
-            long long ni = ((long long)__float_as_int(t.x) * i) % (long long)W;
-            long long nj = ((long long)__float_as_int(t.y) * j) % (long long)H;
-            ni += ni < 0 ? W : 0;
-            nj += nj < 0 ? H : 0;
-            float turns = (float)ni / (float)W + (float)nj / (float)H;
-            float s, c;
-            sincospif(2.0f * turns, &s, &c);
-            // a sin(x + psi) = (a cos psi) sin x + (a sin psi) cos x
-            h = fmaf(t.z, s, fmaf(t.w, c, h));
+        for (uint32_t m = 0; m < nm; ++m) {
+#pragma unroll
+            for (int b = 0; b < 2; ++b) {
+                const float2 y = sr[m][2 * ty + b];
+#pragma unroll
+                for (int a = 0; a < 2; ++a) {
+                    const float2 x = sc[m][2 * tx + a];
+                    h[b][a] = fmaf(x.x, y.x, fmaf(x.y, y.y, h[b][a]));
+                }
+            }
         }
     }
     // block min / max, then one atomic each
-    float lo = in ? h : INFINITY, hi = in ? h : -INFINITY;
+    float lo = INFINITY, hi = -INFINITY;
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+            const uint32_t i = i0 + 2 * tx + a, j = j0 + 2 * ty + b;
+            if (i < W && j < H) {
+                lo = fminf(lo, h[b][a]);
+                hi = fmaxf(hi, h[b][a]);
+                out[(size_t)j * W + i] = h[b][a];
+            }
+        }
     for (int o = 16; o > 0; o >>= 1) {
         lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
         hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
@@ -102,15 +149,14 @@ __global__ void __launch_bounds__(256) k_noise(const wt_noise_term* __restrict__
         atomicMin(mm, ordered(lo));
         atomicMax(mm + 1, ordered(hi));
     }
-    if (in) out[(size_t)j * W + i] = h;
 }
 
 __global__ void __launch_bounds__(256) k_noise_norm(float* __restrict__ out, size_t n, const uint32_t* mm) {
     const float lo = unordered(mm[0]), hi = unordered(mm[1]);
     const float span = hi - lo;
-    const float inv = span > 0.0f ? 1.0f / span : 0.0f;
+    // a correctly rounded division maps the extremes to exactly 0 and 1
     for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x)
-        out[v] = (out[v] - lo) * inv;
+        out[v] = span > 0.0f ? (out[v] - lo) / span : 0.0f;
 }
 
 // ---- peak probes -----------------------------------------------------------
@@ -166,16 +212,27 @@ cudaError_t launch_unorm8(const uint8_t* px, uint32_t w, uint32_t h, uint32_t ch
     return cudaGetLastError();
 }
 
-cudaError_t launch_noise(const wt_noise_term* terms, uint32_t n_terms, uint32_t w, uint32_t h, float* out,
-                         void* ws, cudaStream_t s) {
+cudaError_t launch_noise(const wt_noise_term* terms, uint32_t n_terms, const float* rates, double t, uint32_t w,
+                         uint32_t h, float* out, void* ws, cudaStream_t s) {
     uint32_t* mm = static_cast<uint32_t*>(ws);
+    float2* col = reinterpret_cast<float2*>(static_cast<char*>(ws) + kNoiseHeader);
+    float2* row = col + (size_t)n_terms * w;
     k_noise_init<<<1, 1, 0, s>>>(mm);
-    dim3 grid((w + 15) / 16, (h + 15) / 16);
-    k_noise<<<grid, 256, 0, s>>>(terms, n_terms, w, h, out, mm);
+    const uint64_t entries = (uint64_t)n_terms * ((uint64_t)w + h);
+    if (entries > 0) {
+        const uint64_t tb = (entries + 255) / 256;
+        k_noise_tables<<<(unsigned)(tb < 65536 ? tb : 65536), 256, 0, s>>>(terms, n_terms, rates, t, w, h, col, row);
+    }
+    dim3 grid((w + kNoiseTile - 1) / kNoiseTile, (h + kNoiseTile - 1) / kNoiseTile);
+    k_noise_tiles<<<grid, 256, 0, s>>>(col, row, n_terms, w, h, out, mm);
     size_t n = (size_t)w * h;
     unsigned blocks = (unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
     k_noise_norm<<<blocks, 256, 0, s>>>(out, n, mm);
     return cudaGetLastError();
+}
+
+size_t noise_workspace_bytes(uint32_t n_terms, uint32_t w, uint32_t h) {
+    return kNoiseHeader + sizeof(float2) * (size_t)n_terms * ((size_t)w + h);
 }
 
 cudaError_t measure_peaks(void* scratch, size_t bytes, double* fma, double* sin_rate, cudaStream_t s) {
