@@ -108,6 +108,40 @@ def test_device_side_validation(wt, gpu):
     assert st == wt.abi.WT_ERR_INVALID_ARG and first == 3
 
 
+@pytest.mark.parametrize("bad_kind", ["nan_wavelength", "inf_amplitude", "zero_wavelength"])
+def test_bad_waves_in_large_tables(wt, gpu, bad_kind):
+    """More (patch, wave) pairs than the scan block has threads (the shared
+    bitmask validation): a patch using a bad wave is skipped and reported
+    (the smallest such index), patches sharing no bad wave still run, and
+    two patches sharing the bad wave are both skipped."""
+    import torch
+    from wave_tool_gb300 import workloads
+    w = workloads.config3(n_patches=40, seed=13)
+    assert int(w.patches["wave_count"].sum()) > 1024
+    good = wt.Surface(w.patches, w.waves)
+    ref, _ = good.displace()
+    patches = w.patches.copy()
+    victim = 17
+    wv = int(patches[victim]["wave_offset"]) + 3
+    patches[29]["wave_offset"] = patches[victim]["wave_offset"]   # 29 shares 17's waves
+    patches[29]["wave_count"] = min(int(patches[29]["wave_count"]), int(patches[victim]["wave_count"]))
+    waves = w.waves.copy()
+    field, value = {"nan_wavelength": ("wavelength", np.nan), "inf_amplitude": ("amplitude", np.inf),
+                    "zero_wavelength": ("wavelength", 0.0)}[bad_kind]
+    waves[wv][field] = value
+    s = wt.Surface(patches, waves)
+    pos, nrm = s.alloc_outputs()
+    pos.fill_(-7.0)
+    s.displace(pos, nrm)
+    st, first = s.status()
+    assert st == wt.abi.WT_ERR_INVALID_ARG and first == victim
+    for p in (victim, 29):
+        o = int(patches[p]["out_offset"])
+        assert float(pos[o, 0]) == -7.0
+    o0, n0 = int(patches[0]["out_offset"]), int(patches[0]["cols"] * patches[0]["rows"])
+    assert torch.equal(pos[o0:o0 + n0], ref[o0:o0 + n0])
+
+
 def test_workspace_too_small_for_wave_slots(wt, gpu):
     import ctypes as C
     from wave_tool_gb300 import workloads

@@ -33,7 +33,8 @@ namespace {
 using namespace wt::dev;
 
 constexpr uint32_t kNoPatch = 0xffffffffu;
-constexpr int kSortBins = 4096;
+constexpr int kSortBins = 1024;         // wave counts >= 1023 share the last bin
+constexpr uint32_t kWaveMaskWords = 512;  // waves validated into a shared bitmask up to 16384
 constexpr uint32_t kRankSortMax = 64;
 
 __device__ __forceinline__ void flag_error(WsHeader* h, uint32_t code, uint32_t patch) {
@@ -148,6 +149,13 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
                                                     uint64_t out_capacity, uint64_t coef_capacity,
                                                     uint32_t tile_cols, char* ws, WsLayout L, HmDev hm,
                                                     int fuse_coef) {
+#if __CUDA_ARCH__ >= 900
+    // the coefficient kernel does not read what this one writes (it forms its
+    // own offsets and waits for this grid before it completes): let it start
+    // (with the constants formed here the next kernel is the forward, which
+    // waits at its start anyway)
+    if (!fuse_coef) cudaTriggerProgrammaticLaunchCompletion();
+#endif
     WsHeader* hdr = reinterpret_cast<WsHeader*>(ws);
     uint32_t* sorted = reinterpret_cast<uint32_t*>(ws + L.sorted);
     uint32_t* tile_pre = reinterpret_cast<uint32_t*>(ws + L.tile_pre);
@@ -156,6 +164,7 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
     __shared__ uint32_t bins[kSortBins];
     constexpr uint32_t kScanSmemOffsets = 4096;
     __shared__ uint32_t off_s[kScanSmemOffsets];
+    __shared__ uint32_t good_wave[kWaveMaskWords];  // bit w: wave w passes wave_ok
 
     if (threadIdx.x == 0) {
         hdr->status = 0;
@@ -186,24 +195,52 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
     const uint32_t total_pairs = block_exclusive_scan(pair_off, n);
     if (threadIdx.x == 0) pair_off[n] = total_pairs;
     __syncthreads();
-    // wave validation, one pair per thread; a patch with a bad wave runs no
-    // tiles.  The owning patch is found by binary search over the offsets,
-    // from a shared-memory copy when they fit (each step a dependent load).
+    // wave validation; a patch with a bad wave runs no tiles.  More pairs
+    // than threads and up to 16384 waves: each wave once, coalesced, into a
+    // shared bitmask (a warp's 32 waves are one word), then each patch tests
+    // its range of bits.  Otherwise one pair per thread, the owning patch
+    // found by binary search.
     const bool off_in_smem = n + 1 <= kScanSmemOffsets;
     if (off_in_smem)
         for (uint32_t i = threadIdx.x; i <= n; i += blockDim.x) off_s[i] = pair_off[i];
-    __syncthreads();
     const uint32_t* off = off_in_smem ? off_s : pair_off;
-    for (uint32_t P = threadIdx.x; P < total_pairs; P += blockDim.x) {
-        uint32_t lo = 0, hi = n + 1;
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (off[mid] <= P) lo = mid + 1; else hi = mid;
+    if (total_pairs > blockDim.x && n_waves <= 32u * kWaveMaskWords) {
+        const uint32_t nw_round = (n_waves + 31u) & ~31u;
+#pragma unroll 4
+        for (uint32_t w = threadIdx.x; w < nw_round; w += blockDim.x) {
+            const bool good = w < n_waves && wave_ok(waves[w]);
+            const uint32_t word = __ballot_sync(0xffffffffu, good);
+            if ((threadIdx.x & 31) == 0) good_wave[w >> 5] = word;
         }
-        const uint32_t p = lo - 1;
-        if (!wave_ok(waves[patches[p].wave_offset + (P - off[p])])) {
-            flag_error(hdr, WT_ERR_INVALID_ARG, p);
-            tiles[p] = 0;
+        __syncthreads();
+        for (uint32_t p = threadIdx.x; p < n; p += blockDim.x) {
+            if (off[p + 1] == off[p]) continue;  // invalid patch (or no waves)
+            const uint32_t w0 = patches[p].wave_offset, w1 = w0 + (off[p + 1] - off[p]);
+            bool bad = false;
+            for (uint32_t w = w0; w < w1 && !bad;) {
+                const uint32_t bit = w & 31u, take = min(32u - bit, w1 - w);
+                const uint32_t want = (take == 32u ? 0xffffffffu : ((1u << take) - 1u)) << bit;
+                bad = (good_wave[w >> 5] & want) != want;
+                w += take;
+            }
+            if (bad) {
+                flag_error(hdr, WT_ERR_INVALID_ARG, p);
+                tiles[p] = 0;
+            }
+        }
+    } else {
+        __syncthreads();
+        for (uint32_t P = threadIdx.x; P < total_pairs; P += blockDim.x) {
+            uint32_t lo = 0, hi = n + 1;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (off[mid] <= P) lo = mid + 1; else hi = mid;
+            }
+            const uint32_t p = lo - 1;
+            if (!wave_ok(waves[patches[p].wave_offset + (P - off[p])])) {
+                flag_error(hdr, WT_ERR_INVALID_ARG, p);
+                tiles[p] = 0;
+            }
         }
     }
     const bool nomem = total_pairs > coef_capacity;
@@ -262,23 +299,39 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
 }
 
 // ---- stage 2: FP64 constants per (patch, wave) and per patch ---------------
+// Up to kSmemOffsets - 1 patches each block forms the wave-count prefix of
+// the structurally valid patches itself, so this kernel runs alongside the
+// scan kernel and waits for it only before it completes (the forward kernel
+// waits for this one); with more patches it waits first and reads the scan's
+// prefix.
 __global__ void __launch_bounds__(256) k_prep_coef(const wt_patch* __restrict__ patches, uint32_t n,
-                                                   const wt_wave* __restrict__ waves, HmDev hm, char* ws,
-                                                   WsLayout L) {
-#if __CUDA_ARCH__ >= 900
-    cudaGridDependencySynchronize();
-#endif
+                                                   const wt_wave* __restrict__ waves, uint32_t n_waves,
+                                                   uint64_t out_capacity, uint64_t coef_capacity, HmDev hm,
+                                                   char* ws, WsLayout L) {
     const uint32_t* pair_off_g = reinterpret_cast<const uint32_t*>(ws + L.pair_off);
     PatchAux* aux = reinterpret_cast<PatchAux*>(ws + L.aux);
     PairCoef* coef = reinterpret_cast<PairCoef*>(ws + L.coef);
     constexpr uint32_t kSmemOffsets = 4096;
     __shared__ uint32_t off_s[kSmemOffsets];
-    const bool in_smem = n + 1 <= kSmemOffsets;
-    if (in_smem)
-        for (uint32_t i = threadIdx.x; i <= n; i += blockDim.x) off_s[i] = pair_off_g[i];
-    __syncthreads();
-    const uint32_t* pair_off = in_smem ? off_s : pair_off_g;
-    const uint32_t total = pair_off[n];
+    const bool own = n + 1 <= kSmemOffsets;
+    uint32_t total;
+    if (own) {
+        for (uint32_t p = threadIdx.x; p < n; p += blockDim.x) {
+            const wt_patch P = patches[p];
+            off_s[p] = patch_ok(P, n_waves, out_capacity) ? P.wave_count : 0u;
+        }
+        __syncthreads();
+        total = block_exclusive_scan(off_s, n);
+        if (threadIdx.x == 0) off_s[n] = total;
+        __syncthreads();
+        if (total > coef_capacity) total = 0;  // the scan kernel reports the shortfall
+    } else {
+#if __CUDA_ARCH__ >= 900
+        cudaGridDependencySynchronize();
+#endif
+        total = pair_off_g[n];  // 0 when the workspace is short
+    }
+    const uint32_t* pair_off = own ? off_s : pair_off_g;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t P = blockIdx.x * blockDim.x + threadIdx.x; P < total; P += stride) {
         // owning patch: last p with pair_off[p] <= P
@@ -293,6 +346,11 @@ __global__ void __launch_bounds__(256) k_prep_coef(const wt_patch* __restrict__ 
     }
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride)
         aux[p] = make_patch_aux(patches[p], hm, pair_off[p]);
+#if __CUDA_ARCH__ >= 900
+    // complete only after the scan kernel: whatever waits for this grid then
+    // sees both (a no-op when already waited for above)
+    if (own) cudaGridDependencySynchronize();
+#endif
 }
 
 // ---- stage 3: the persistent forward kernel --------------------------------
@@ -538,7 +596,8 @@ cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wa
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     lc.attrs = attr;
     lc.numAttrs = 1;
-    return cudaLaunchKernelEx(&lc, k_prep_coef, patches, n_patches, waves, hm, w, L);
+    return cudaLaunchKernelEx(&lc, k_prep_coef, patches, n_patches, waves, n_waves, out_capacity, coef_cap, hm, w,
+                              L);
 }
 
 bool forward_config_supported(const FwdConfig& c) {
