@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(32 * kColLanes) k_adj_cols(uint32_t n, const c
     const uint32_t* part_off = reinterpret_cast<const uint32_t*>(ws + L.part_off);
     const float* partials = reinterpret_cast<const float*>(ws + L.partials);
     const WsHeader* hdr = reinterpret_cast<const WsHeader*>(ws);
-    float* colsum = reinterpret_cast<float*>(const_cast<char*>(ws) + L.pair_grad);
+    float* colsum = reinterpret_cast<float*>(const_cast<char*>(ws) + L.colsum);
     const bool ran = hdr->total_chunks > 0;
     const uint32_t cl = threadIdx.x & 31, tl = threadIdx.x >> 5;
     for (uint32_t p = blockIdx.y; p < n; p += gridDim.y) {
@@ -402,28 +402,74 @@ __global__ void __launch_bounds__(32 * kColLanes) k_adj_cols(uint32_t n, const c
     }
 }
 
+// Closed-form FP64 gradient of every (patch, wave) pair from its eleven
+// column sums, one pair per thread (GB300's FP64 rate is low: a warp per
+// wave with one busy lane spent 16 us here on 64 patches).
+__global__ void __launch_bounds__(256) k_adj_pairs(const wt_patch* __restrict__ patches, uint32_t n,
+                                                   const wt_wave* __restrict__ waves, const char* __restrict__ ws,
+                                                   AdjLayout L) {
+#if __CUDA_ARCH__ >= 900
+    cudaGridDependencySynchronize();
+#endif
+    const uint32_t* pair_off_g = reinterpret_cast<const uint32_t*>(ws + L.f.pair_off);
+    const float* colsum = reinterpret_cast<const float*>(ws + L.colsum);
+    double* g64 = reinterpret_cast<double*>(const_cast<char*>(ws) + L.pair_g64);
+    constexpr uint32_t kSmemOffsets = 4096;
+    __shared__ uint32_t off_s[kSmemOffsets];
+    const bool in_smem = n + 1 <= kSmemOffsets;
+    if (in_smem)
+        for (uint32_t i = threadIdx.x; i <= n; i += blockDim.x) off_s[i] = pair_off_g[i];
+    __syncthreads();
+    const uint32_t* pair_off = in_smem ? off_s : pair_off_g;
+    const uint32_t total = pair_off[n];
+    for (uint32_t P = blockIdx.x * blockDim.x + threadIdx.x; P < total; P += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = n + 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (pair_off[mid] <= P) lo = mid + 1; else hi = mid;
+        }
+        const uint32_t p = lo - 1;
+        const wt_wave w = waves[patches[p].wave_offset + (P - pair_off[p])];
+        const double lam = w.wavelength;
+        const double k = isinf(lam) ? 0.0 : kTwoPi / lam;
+        const double A = w.amplitude, Q = w.steepness_q, Dx = w.dir_x, Dz = w.dir_z, sp = w.speed;
+        const float* m = colsum + (size_t)kAdjRecord * P;
+        const double t = patches[p].time_s;
+        const double Mdx = m[0], Mdy = m[1], Mdz = m[2], Mjx = m[3], Mjz = m[4];
+        const double Mxx = m[5], Mxz = m[6], Mzz = m[7], T0 = m[8];
+        const double Xw = (double)m[9] + (double)patches[p].bl[0] * T0;
+        const double Zw = (double)m[10] + (double)patches[p].bl[1] * T0;
+        const double P3 = Dx * Dx * Mxx + Dx * Dz * Mxz + Dz * Dz * Mzz;
+        const double gk = A * (Dx * Mjx + Dz * Mjz + Q * P3) + Dx * Xw + Dz * Zw + sp * t * T0;
+        const double gDx = Q * A * Mdx + A * k * Mjx + Q * A * k * (2.0 * Dx * Mxx + Dz * Mxz) + k * Xw;
+        const double gDz = Q * A * Mdz + A * k * Mjz + Q * A * k * (2.0 * Dz * Mzz + Dx * Mxz) + k * Zw;
+        double* g = g64 + 8 * (size_t)P;
+        g[0] = Q * (Dx * Mdx + Dz * Mdz) + k * (Dx * Mjx + Dz * Mjz) + Mdy + Q * k * P3;
+        g[1] = isinf(lam) ? 0.0 : -gk * k / lam;
+        g[2] = -Dz * gDx + Dx * gDz;
+        g[3] = A * (Dx * Mdx + Dz * Mdz + k * P3);
+        g[4] = T0;
+        g[5] = k * t * T0;
+        g[6] = gDx;
+        g[7] = gDz;
+    }
+}
+
 // One warp per wave: lane l takes patches l, l+32, ... that use the wave and
-// adds their closed-form gradients (FP64, from the patch's eleven column
-// sums); the lanes are then combined by a fixed shuffle tree, or, when one
-// lane alone holds a contribution (a wave used by one patch), taken from it
-// (GB300's FP64 rate is low: the tree's 40 FP64 adds per wave cost more than
-// the closed form).
+// adds their pair gradients; the lanes are then combined by a fixed shuffle
+// tree, or, when one lane alone holds a contribution (a wave used by one
+// patch), taken from it.
 __global__ void __launch_bounds__(256) k_adj_waves(const wt_patch* __restrict__ patches, uint32_t n,
-                                                   const wt_wave* __restrict__ waves, uint32_t n_waves,
-                                                   const char* __restrict__ ws, AdjLayout L,
+                                                   uint32_t n_waves, const char* __restrict__ ws, AdjLayout L,
                                                    wt_wave_grad* __restrict__ grad) {
 #if __CUDA_ARCH__ >= 900
     cudaGridDependencySynchronize();
 #endif
     const uint32_t* pair_off = reinterpret_cast<const uint32_t*>(ws + L.f.pair_off);
-    const float* colsum = reinterpret_cast<const float*>(ws + L.pair_grad);
+    const double* g64 = reinterpret_cast<const double*>(ws + L.pair_g64);
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < n_waves; wi += warps) {
-        const wt_wave w = waves[wi];
-        const double lam = w.wavelength;
-        const double k = isinf(lam) ? 0.0 : kTwoPi / lam;
-        const double A = w.amplitude, Q = w.steepness_q, Dx = w.dir_x, Dz = w.dir_z, sp = w.speed;
         double g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         bool has = false;
         for (uint32_t p = lane; p < n; p += 32) {
@@ -431,24 +477,9 @@ __global__ void __launch_bounds__(256) k_adj_waves(const wt_patch* __restrict__ 
             const uint32_t off = patches[p].wave_offset;
             if (nw == 0 || wi < off || wi - off >= nw) continue;
             has = true;
-            const float* m = colsum + (size_t)kAdjRecord * (pair_off[p] + (wi - off));
-            const double t = patches[p].time_s;
-            const double Mdx = m[0], Mdy = m[1], Mdz = m[2], Mjx = m[3], Mjz = m[4];
-            const double Mxx = m[5], Mxz = m[6], Mzz = m[7], T0 = m[8];
-            const double Xw = (double)m[9] + (double)patches[p].bl[0] * T0;
-            const double Zw = (double)m[10] + (double)patches[p].bl[1] * T0;
-            const double P3 = Dx * Dx * Mxx + Dx * Dz * Mxz + Dz * Dz * Mzz;
-            const double gk = A * (Dx * Mjx + Dz * Mjz + Q * P3) + Dx * Xw + Dz * Zw + sp * t * T0;
-            const double gDx = Q * A * Mdx + A * k * Mjx + Q * A * k * (2.0 * Dx * Mxx + Dz * Mxz) + k * Xw;
-            const double gDz = Q * A * Mdz + A * k * Mjz + Q * A * k * (2.0 * Dz * Mzz + Dx * Mxz) + k * Zw;
-            g[0] += Q * (Dx * Mdx + Dz * Mdz) + k * (Dx * Mjx + Dz * Mjz) + Mdy + Q * k * P3;
-            g[1] += isinf(lam) ? 0.0 : -gk * k / lam;
-            g[2] += -Dz * gDx + Dx * gDz;
-            g[3] += A * (Dx * Mdx + Dz * Mdz + k * P3);
-            g[4] += T0;
-            g[5] += k * t * T0;
-            g[6] += gDx;
-            g[7] += gDz;
+            const double* q = g64 + 8 * (size_t)(pair_off[p] + (wi - off));
+#pragma unroll
+            for (int i = 0; i < 8; ++i) g[i] += q[i];
         }
         const unsigned holders = __ballot_sync(0xffffffffu, has);
         if (holders != 0 && (holders & (holders - 1)) == 0) {
@@ -554,7 +585,10 @@ cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt
     if (e != cudaSuccess) return e;
     const unsigned wb = (n_waves + 7) / 8 < (unsigned)sms * 16 ? (n_waves + 7) / 8 : (unsigned)sms * 16;
     if (wb == 0) return cudaSuccess;
-    return launch_pdl(k_adj_waves, dim3(wb), dim3(256), 0, s, patches, n_patches, waves, n_waves,
+    e = launch_pdl(k_adj_pairs, dim3((unsigned)sms), dim3(256), 0, s, patches, n_patches, waves,
+                   static_cast<const char*>(ws), L);
+    if (e != cudaSuccess) return e;
+    return launch_pdl(k_adj_waves, dim3(wb), dim3(256), 0, s, patches, n_patches, n_waves,
                       static_cast<const char*>(ws), L, grad);
 }
 

@@ -83,11 +83,12 @@ inline WsLayout ws_layout(uint32_t n_patches, uint64_t total_wave_slots) {
 // chunkpre u32[n+1]    exclusive prefix of tile chunks over the sorted order
 // partial  float[11 x records]   per-(chunk, wave) FP32 partial sums
 // colsum   float[11 x wave slots] per-(patch, wave) sums of the records
+// pairg    double[8 x wave slots] per-(patch, wave) closed-form gradients
 constexpr int kAdjRecord = 11;
 
 struct AdjLayout {
     WsLayout f;
-    size_t rank, part_off, chunk_pre, partials, pair_grad, end;
+    size_t rank, part_off, chunk_pre, partials, colsum, pair_g64, end;
     uint64_t cap_records;
 };
 
@@ -99,7 +100,8 @@ inline AdjLayout adj_layout(uint32_t n_patches, uint64_t total_wave_slots, uint6
     A.part_off = o;  o = align_up(o + 4ull * (n_patches + 1), 16);
     A.chunk_pre = o; o = align_up(o + 4ull * (n_patches + 1), 256);
     A.partials = o;  o = align_up(o + 4ull * kAdjRecord * records, 256);
-    A.pair_grad = o; o = align_up(o + 8ull * 8 * total_wave_slots, 256);
+    A.colsum = o;    o = align_up(o + 4ull * kAdjRecord * total_wave_slots, 256);
+    A.pair_g64 = o;  o = align_up(o + 8ull * 8 * total_wave_slots, 256);
     A.end = o;
     A.cap_records = records;
     return A;
