@@ -186,10 +186,9 @@ __device__ __forceinline__ void wave_moments(const float4* __restrict__ gbuf, ui
 
 // SAVED: phase 1 reads the forward's saved sums instead of recomputing them
 // (a compile-time switch, so that the recomputing kernel carries no test);
-// without the recompute's 64 accumulators the kernel fits 96 registers, and
-// 5 blocks (20 warps) per SM instead of 4 run it 7.6 % faster.
+// both forms fit 96 registers and run 5 blocks (20 warps) per SM.
 template <bool SAVED>
-__global__ void __launch_bounds__(32 * kAdjWarps, SAVED ? 5 : 4)
+__global__ void __launch_bounds__(32 * kAdjWarps, 5)
 k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restrict__ gpos,
           const float* __restrict__ gnrm, uint32_t flags, char* __restrict__ ws, AdjLayout L,
           const float4* __restrict__ sums) {
@@ -258,26 +257,34 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
                         }
                     }
                 } else {
-                    // ---- phase 1: forward sums recomputed, vertex per lane
-                    float acc[8][8];
-    #pragma unroll
-                    for (int j = 0; j < 8; ++j)
-    #pragma unroll
-                        for (int mm = 0; mm < 8; ++mm) acc[j][mm] = 0.0f;
-                    for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
-                        const uint32_t nw = min(32u, nwaves - w0);
-                        __syncwarp();
-                        if (lane < nw) stage_wave(coef[a.pair_offset + w0 + lane], c0, row, wst + kStage * lane);
-                        __syncwarp();
-                        wave_loop_dispatch<8>(S, acc, wst, nw, lane);
-                    }
-                    // park the eight sums of each vertex
-    #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        if ((uint32_t)j < S) {
-                            float4* d = gbuf + kGbufF4 * (lane + 32 * j);
-                            d[0] = make_float4(acc[j][0], acc[j][1], acc[j][2], acc[j][3]);
-                            d[1] = make_float4(acc[j][4], acc[j][5], acc[j][6], acc[j][7]);
+                    // ---- phase 1: forward sums recomputed, vertex per lane, in
+                    // two 128-column halves of 4 vertices per lane (the forward's
+                    // 4-vertex tiles; half the accumulator registers, so the
+                    // kernel fits 5 blocks per SM)
+                    for (uint32_t h = 0; h < 2; ++h) {
+                        const uint32_t Sh = h == 0 ? min(S, 4u) : (S > 4u ? S - 4u : 0u);
+                        if (Sh == 0) break;
+                        const uint32_t ch = c0 + 128u * h;
+                        float acc[4][8];
+#pragma unroll
+                        for (int j = 0; j < 4; ++j)
+#pragma unroll
+                            for (int mm = 0; mm < 8; ++mm) acc[j][mm] = 0.0f;
+                        for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
+                            const uint32_t nw = min(32u, nwaves - w0);
+                            __syncwarp();
+                            if (lane < nw) stage_wave(coef[a.pair_offset + w0 + lane], ch, row, wst + kStage * lane);
+                            __syncwarp();
+                            wave_loop_dispatch<4>(Sh, acc, wst, nw, lane);
+                        }
+                        // park the eight sums of each vertex
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            if ((uint32_t)j < Sh) {
+                                float4* d = gbuf + kGbufF4 * (lane + 32 * (4 * h + j));
+                                d[0] = make_float4(acc[j][0], acc[j][1], acc[j][2], acc[j][3]);
+                                d[1] = make_float4(acc[j][4], acc[j][5], acc[j][6], acc[j][7]);
+                            }
                         }
                     }
                 }
@@ -320,7 +327,7 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
                     float4 st[3];
                     stage_wave(k, c0, row, st);
                     float m[11];
-    #pragma unroll
+#pragma unroll
                     for (int i = 0; i < 11; ++i) m[i] = 0.0f;
                     const uint32_t t32 = __float_as_uint(st[0].x), a32 = __float_as_uint(st[0].y);
                     if (S == 8)
@@ -328,7 +335,7 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
                     else
                         wave_moments<0>(gbuf, S, grp, G, nvalid0, t32, a32, st[0].z, st[0].w, k, xb0, zb0, gx, gz, m);
                     for (uint32_t o = P; o < 32; o <<= 1) {
-    #pragma unroll
+#pragma unroll
                         for (int i = 0; i < 11; ++i) m[i] += __shfl_down_sync(0xffffffffu, m[i], o);
                     }
                     if (active && grp == 0) {
@@ -336,10 +343,10 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
                         // (the same lane writes it for every tile of the chunk)
                         float* r = partials + (size_t)kAdjRecord * (rec0 + wi);
                         if (lt == lt0) {
-    #pragma unroll
+#pragma unroll
                             for (int i = 0; i < 11; ++i) r[i] = m[i];
                         } else {
-    #pragma unroll
+#pragma unroll
                             for (int i = 0; i < 11; ++i) r[i] += m[i];
                         }
                     }
