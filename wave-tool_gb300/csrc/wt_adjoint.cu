@@ -53,45 +53,6 @@ constexpr uint32_t kAdjChunkMinTilesPerWarp = 8;
 constexpr int kGbufVerts = 256;              // vertices per tile (32 lanes x S <= 8)
 constexpr int kGbufF4 = 2;                   // float4 per parked vertex
 
-__global__ void __launch_bounds__(1024) k_adj_scan(const wt_patch* __restrict__ patches, uint32_t n, char* ws,
-                                                   AdjLayout L, uint32_t chunk_max, uint32_t min_tiles) {
-#if __CUDA_ARCH__ >= 900
-    cudaGridDependencySynchronize();
-#endif
-    WsHeader* hdr = reinterpret_cast<WsHeader*>(ws);
-    const uint32_t* sorted = reinterpret_cast<const uint32_t*>(ws + L.f.sorted);
-    const uint32_t* tile_pre = reinterpret_cast<const uint32_t*>(ws + L.f.tile_pre);
-    const uint32_t* pair_off = reinterpret_cast<const uint32_t*>(ws + L.f.pair_off);
-    uint32_t* rank = reinterpret_cast<uint32_t*>(ws + L.rank);
-    uint32_t* part_off = reinterpret_cast<uint32_t*>(ws + L.part_off);
-    uint32_t* chunk_pre = reinterpret_cast<uint32_t*>(ws + L.chunk_pre);
-    const uint32_t chunk = hdr->total_tiles >= min_tiles ? chunk_max : 1u;
-    for (uint32_t q = threadIdx.x; q < n; q += blockDim.x) {
-        const uint32_t p = sorted[q];
-        rank[p] = q;
-        const uint32_t chunks = (tile_pre[q + 1] - tile_pre[q] + chunk - 1) / chunk;
-        chunk_pre[q] = chunks;
-        const uint64_t rec = (uint64_t)chunks * (pair_off[p + 1] - pair_off[p]);
-        part_off[q] = rec > 0xffffffffull ? 0xffffffffu : (uint32_t)rec;
-    }
-    __syncthreads();
-    const uint32_t total = block_exclusive_scan(part_off, n);
-    __syncthreads();  // every thread has read the first scan's total
-    const uint32_t chunks = block_exclusive_scan(chunk_pre, n);
-    if (threadIdx.x == 0) {
-        part_off[n] = total;
-        chunk_pre[n] = chunks;
-        hdr->total_chunks = chunks;
-        hdr->adj_chunk = chunk;
-        if ((uint64_t)total > L.cap_records || total == 0xffffffffu || hdr->total_tiles == 0) {
-            // the device patches need more records than the host copy said
-            // (or the prep refused them)
-            if (hdr->total_tiles != 0) atomicCAS(&hdr->status, 0u, (uint32_t)WT_ERR_NOMEM);
-            hdr->total_chunks = 0;
-        }
-    }
-}
-
 // Adjoints of the eight sums at one vertex.  Order: dx, dy, dz, jx, jz, sxx,
 // sxz, szz.  See oracle/gerstner_f64.c:wto_adjoint_f64 for the same algebra.
 __device__ __forceinline__ void vertex_adjoint(const VertexSums& s, float xl, float zl, const PatchAux& a,
@@ -566,6 +527,18 @@ cudaError_t launch_adj_main(int sms, int occ, cudaStream_t s, const wt_patch* pa
 
 }  // namespace
 
+cudaError_t adjoint_scan_args(bool saved, const AdjLayout& L, AdjScanArgs* out) {
+    const int sms = device_sms();
+    if (sms <= 0) return cudaErrorInvalidDevice;
+    int occ = 1;
+    cudaError_t e = saved ? adj_occupancy<true>(&occ) : adj_occupancy<false>(&occ);
+    if (e != cudaSuccess) return e;
+    out->L = L;
+    out->chunk_max = saved ? kAdjChunkSaved : kAdjChunkRecompute;
+    out->min_tiles = kAdjChunkMinTilesPerWarp * (uint32_t)(sms * occ * kAdjWarps);
+    return cudaSuccess;
+}
+
 uint64_t adjoint_records(const wt_patch& p) {
     if (p.cols < 2 || p.rows < 2) return 0;
     return (uint64_t)p.rows * dev::tiles_per_row(p.cols, 8) * p.wave_count;  // chunks of one tile
@@ -579,10 +552,6 @@ cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt
     const int sms = device_sms();
     int occ = 1;
     cudaError_t e = sums ? adj_occupancy<true>(&occ) : adj_occupancy<false>(&occ);
-    if (e != cudaSuccess) return e;
-    const uint32_t min_tiles = kAdjChunkMinTilesPerWarp * (uint32_t)(sms * occ * kAdjWarps);
-    e = launch_pdl(k_adj_scan, dim3(1), dim3(1024), 0, s, patches, n_patches, w, L,
-                   sums ? kAdjChunkSaved : kAdjChunkRecompute, min_tiles);
     if (e != cudaSuccess) return e;
     e = sums ? launch_adj_main<true>(sms, occ, s, patches, hm, gpos, gnrm, flags, w, L, sums)
              : launch_adj_main<false>(sms, occ, s, patches, hm, gpos, gnrm, flags, w, L, nullptr);

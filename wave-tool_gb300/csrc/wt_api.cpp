@@ -302,7 +302,10 @@ static wt_status run_adjoint(const wt_patch* host_patches, const wt_patch* patch
         cudaError_t e = cudaMemsetAsync(grad_out, 0, sizeof(wt_wave_grad) * n_waves, s);
         return e == cudaSuccess ? WT_OK : cuda_fail(e, "clearing grad_out");
     }
-    cudaError_t e = wt::launch_prep(patches, n_patches, waves, n_waves, P.hm, out_capacity, 256u, workspace, L.f, s);
+    wt::AdjScanArgs args;
+    cudaError_t e = wt::adjoint_scan_args(sums != nullptr, L, &args);
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint set-up");
+    e = wt::launch_prep(patches, n_patches, waves, n_waves, P.hm, out_capacity, 256u, workspace, L.f, s, &args);
     if (e != cudaSuccess) return cuda_fail(e, "prep launch");
     uint32_t maxw = 0;
     for (uint32_t i = 0; i < n_patches; ++i) maxw = host_patches[i].wave_count > maxw ? host_patches[i].wave_count : maxw;

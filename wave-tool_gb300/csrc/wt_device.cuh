@@ -50,6 +50,47 @@ static __device__ uint32_t block_exclusive_scan(uint32_t* a, uint32_t n) {
     return carry;
 }
 
+// The adjoint's queue set-up, by one block after the prep's scans (needs
+// sorted, tile_pre and pair_off, and the header's total_tiles): each patch's
+// sorted rank, its chunks of tiles (chunk_max tiles per chunk when there are
+// at least min_tiles tiles, else single tiles) and the exclusive prefixes of
+// chunks and of records (chunks x waves) over the sorted order.
+__device__ inline void adj_scan_body(char* ws, const AdjLayout& L, uint32_t n, uint32_t chunk_max,
+                                     uint32_t min_tiles) {
+    WsHeader* hdr = reinterpret_cast<WsHeader*>(ws);
+    const uint32_t* sorted = reinterpret_cast<const uint32_t*>(ws + L.f.sorted);
+    const uint32_t* tile_pre = reinterpret_cast<const uint32_t*>(ws + L.f.tile_pre);
+    const uint32_t* pair_off = reinterpret_cast<const uint32_t*>(ws + L.f.pair_off);
+    uint32_t* rank = reinterpret_cast<uint32_t*>(ws + L.rank);
+    uint32_t* part_off = reinterpret_cast<uint32_t*>(ws + L.part_off);
+    uint32_t* chunk_pre = reinterpret_cast<uint32_t*>(ws + L.chunk_pre);
+    const uint32_t chunk = hdr->total_tiles >= min_tiles ? chunk_max : 1u;
+    for (uint32_t q = threadIdx.x; q < n; q += blockDim.x) {
+        const uint32_t p = sorted[q];
+        rank[p] = q;
+        const uint32_t chunks = (tile_pre[q + 1] - tile_pre[q] + chunk - 1) / chunk;
+        chunk_pre[q] = chunks;
+        const uint64_t rec = (uint64_t)chunks * (pair_off[p + 1] - pair_off[p]);
+        part_off[q] = rec > 0xffffffffull ? 0xffffffffu : (uint32_t)rec;
+    }
+    __syncthreads();
+    const uint32_t total = block_exclusive_scan(part_off, n);
+    __syncthreads();  // every thread has read the first scan's total
+    const uint32_t chunks = block_exclusive_scan(chunk_pre, n);
+    if (threadIdx.x == 0) {
+        part_off[n] = total;
+        chunk_pre[n] = chunks;
+        hdr->total_chunks = chunks;
+        hdr->adj_chunk = chunk;
+        if ((uint64_t)total > L.cap_records || total == 0xffffffffu || hdr->total_tiles == 0) {
+            // the device patches need more records than the host copy said
+            // (or the prep refused them)
+            if (hdr->total_tiles != 0) atomicCAS(&hdr->status, 0u, (uint32_t)WT_ERR_NOMEM);
+            hdr->total_chunks = 0;
+        }
+    }
+}
+
 // Tiling of a patch row (forward and adjoint): tiles of 32*smax columns, the
 // row's last tile only as many 32-column blocks as the row still needs (so a
 // row is padded to a multiple of 32 columns, not of 32*smax).

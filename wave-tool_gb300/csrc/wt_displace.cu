@@ -148,7 +148,8 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
                                                     const wt_wave* __restrict__ waves, uint32_t n_waves,
                                                     uint64_t out_capacity, uint64_t coef_capacity,
                                                     uint32_t tile_cols, char* ws, WsLayout L, HmDev hm,
-                                                    int fuse_coef) {
+                                                    int fuse_coef, int do_adj, AdjLayout AL,
+                                                    uint32_t adj_chunk_max, uint32_t adj_min_tiles) {
 #if __CUDA_ARCH__ >= 900
     // the coefficient kernel does not read what this one writes (it forms its
     // own offsets and waits for this grid before it completes): let it start
@@ -252,6 +253,7 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
             atomicCAS(&hdr->status, 0u, (uint32_t)WT_ERR_NOMEM);
             hdr->total_tiles = 0;
             pair_off[n] = 0;
+            if (do_adj) hdr->total_chunks = 0;
         }
         for (uint32_t p = threadIdx.x; p <= n; p += blockDim.x) tile_pre[p] = 0;
         return;
@@ -295,6 +297,10 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
             coef[P] = make_pair_coef(Pt, waves[Pt.wave_offset + (P - off[lo - 1])]);
         }
         for (uint32_t p = threadIdx.x; p < n; p += blockDim.x) aux[p] = make_patch_aux(patches[p], hm, off[p]);
+    }
+    if (do_adj) {
+        __syncthreads();  // sorted, tile_pre and the header's total_tiles are complete
+        adj_scan_body(ws, AL, n, adj_chunk_max, adj_min_tiles);
     }
 }
 
@@ -573,15 +579,17 @@ cudaError_t launch_fwd_t(const FwdConfig& cfg, const wt_patch* patches, const Hm
 
 cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
                         const HmDev& hm, uint64_t out_capacity, uint32_t tile_cols, void* ws,
-                        const WsLayout& L, cudaStream_t s) {
+                        const WsLayout& L, cudaStream_t s, const AdjScanArgs* adj) {
     char* w = static_cast<char*>(ws);
     // coefficient capacity = what the caller's workspace holds past the fixed part
     // (the header records the real total; the scan refuses to overflow it)
     uint64_t coef_cap = (L.end - L.coef) / sizeof(PairCoef);
     // at most 1024 (patch, wave) pairs: the scan kernel forms the constants too
     const int fuse = (uint64_t)n_patches * n_waves <= 1024u;
+    const AdjScanArgs none{};
+    const AdjScanArgs& A = adj ? *adj : none;
     k_prep_scan<<<1, 1024, 0, s>>>(patches, n_patches, waves, n_waves, out_capacity, coef_cap, tile_cols, w, L,
-                                   hm, fuse);
+                                   hm, fuse, adj ? 1 : 0, A.L, A.chunk_max, A.min_tiles);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (fuse) return cudaSuccess;

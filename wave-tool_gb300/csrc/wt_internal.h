@@ -144,11 +144,20 @@ struct HmDev {
     int present;
 };
 
+// The adjoint's queue set-up (ranks, chunk and record prefixes), formed by the
+// prep's scan kernel when the prep runs for an adjoint.
+struct AdjScanArgs {
+    AdjLayout L;
+    uint32_t chunk_max;  // tiles per chunk when there are enough tiles
+    uint32_t min_tiles;  // below this many tiles, chunks of one tile
+};
+
 // ---- launchers (wt_displace.cu) -------------------------------------------
 // tile_cols: tile width (each row's last tile narrower, see tiles_per_row)
 cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
                         uint32_t n_waves, const HmDev& hm, uint64_t out_capacity,
-                        uint32_t tile_cols, void* ws, const WsLayout& L, cudaStream_t s);
+                        uint32_t tile_cols, void* ws, const WsLayout& L, cudaStream_t s,
+                        const AdjScanArgs* adj = nullptr);
 // pos may be NULL only with x.view set
 cudaError_t launch_forward(const FwdConfig& cfg, const wt_patch* patches, uint32_t n_patches,
                            const HmDev& hm, float* pos, float* nrm, uint32_t flags, void* ws,
@@ -162,7 +171,10 @@ bool forward_config_supported(const FwdConfig& cfg);
 // ---- adjoint (wt_adjoint.cu) ----------------------------------------------
 // Records (tile chunks x waves) of one patch, as the adjoint lays them out.
 uint64_t adjoint_records(const wt_patch& p);
-// sums: NULL (phase 1 recomputes the forward sums) or the forward's saved sums
+// The scan arguments of an adjoint over layout L (saved: from saved sums).
+cudaError_t adjoint_scan_args(bool saved, const AdjLayout& L, AdjScanArgs* out);
+// sums: NULL (phase 1 recomputes the forward sums) or the forward's saved sums;
+// the prep ran with adjoint_scan_args
 cudaError_t launch_adjoint(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
                            uint32_t max_waves_per_patch, const HmDev& hm, const float* gpos, const float* gnrm,
                            uint32_t flags, wt_wave_grad* grad, void* ws, const AdjLayout& L, const float* sums,
