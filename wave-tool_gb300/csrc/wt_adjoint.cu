@@ -2,21 +2,23 @@
 // to every wave's parameters (no reference counterpart; the forward it
 // differentiates is water-grid.vert:74-111, see wt_displace.cu).
 //
-// After the shared prep stages (validation, LPT order, FP64 phase constants):
-//   k_adj_scan   (1 block)   rank of each patch, prefix of (tile, wave) records
-//   k_adjoint    (persistent) per tile:
-//       phase 1, one vertex per lane (as the forward): recompute the eight
-//       wave sums, the heightmap sample and the normal, and turn dL/dpos and
-//       dL/dnrm into the adjoints of the eight sums; park them with the
-//       vertex's local grid position in shared memory;
+// After the shared prep stages (validation, LPT order, FP64 phase constants;
+// the scan kernel also ranks the patches and lays out the chunk queue and the
+// records, wt_device.cuh:adj_scan_body):
+//   k_adjoint    (persistent) per chunk of 1 or 2 tiles, per tile:
+//       phase 1, one vertex per lane (as the forward, in two 4-vertex
+//       halves): recompute the eight wave sums (or read the forward's saved
+//       ones), the heightmap sample and the normal, and turn dL/dpos and
+//       dL/dnrm into the adjoints of the eight sums, parked in shared memory;
 //       phase 2, one wave per lane: walk the tile's vertices (broadcast from
 //       shared memory), regenerate the wave's sin/cos there (MUFU start +
-//       Chebyshev steps) and accumulate 11 per-wave moments; write them as
-//       the tile's record for that wave (no cross-lane reduction).
-//   k_adj_cols   column sums of each patch's records over its tiles (FP32
+//       Chebyshev steps) and accumulate 11 per-wave moments; add them into
+//       the chunk's record for that wave (no cross-lane reduction).
+//   k_adj_cols   column sums of each patch's records over its chunks (FP32
 //                Kahan, fixed order)
-//   k_adj_waves  one warp per wave: closed-form gradient in FP64 for each
-//                patch that uses the wave, combined in a fixed order.
+//   k_adj_pairs  closed-form FP64 gradient per (patch, wave) pair, one per thread
+//   k_adj_waves  one warp per wave: the pair gradients of the patches that
+//                use the wave, added in a fixed order.
 // Every sum has a fixed order, so the result is bitwise reproducible.
 //
 // With g_q the adjoint of sum q per vertex and (c, s) the wave's cos/sin

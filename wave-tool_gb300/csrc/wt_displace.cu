@@ -6,19 +6,22 @@
 // upload of src/render-engine.cpp:1057-1110 (steepness already normalised by
 // the caller, :1073).
 //
-// Three launches, all stream-ordered and graph-capturable:
-//   k_prep_scan  (1 block)   validate patches, prefix sums, LPT sort of
-//                            patches by wave count, tile queue reset
+// Three launches (two when the table has at most 1024 (patch, wave) pairs),
+// all stream-ordered and graph-capturable:
+//   k_prep_scan  (1 block)   validate patches and waves, prefix sums, LPT sort
+//                            of patches by wave count, tile queue reset
 //   k_prep_coef  (grid)      FP64 per-(patch, wave) phase constants in 64-bit
 //                            fixed-point turns + FP32 sum coefficients;
-//                            per-patch local frame
+//                            per-patch local frame; runs alongside the scan
 //   k_forward    (persistent) one tile = one patch row segment of 32*S
 //                            vertices per warp; lane l owns columns
 //                            c0 + l + 32 j, j < S.  Per wave: one MUFU sincos
-//                            per lane, then S-1 exact-step rotations on the
-//                            FMA pipe; 8 FMAs accumulate displacement and the
-//                            surface Jacobian.  Epilogue: heightmap bilerp +
-//                            gradient, exact normal, streaming float4 stores.
+//                            per lane, an exact rotation to the second vertex,
+//                            then the Chebyshev recurrence on the FMA pipe; 8
+//                            FMAs accumulate displacement and the surface
+//                            Jacobian.  Epilogue: heightmap bilerp +
+//                            gradient, exact normal, streaming stores (and,
+//                            by variant, the wave sums or the vertex stage).
 #include <cuda_runtime.h>
 
 #include <atomic>
