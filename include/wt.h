@@ -226,9 +226,11 @@ wt_status wt_gerstner_displace_unbatched(const wt_patch* host_patches,
  * a wave add up).  The gradient is the same for world and displacement
  * outputs.  `host_patches` is a host copy of the device patch table (the
  * per-tile partial sums are laid out from it; wt_adjoint_workspace_size gives
- * the workspace).  Deterministic: per-tile FP32 partial sums are reduced in
- * FP64 in a fixed order.  No reference counterpart (the reference has no
- * derivatives); the forward it differentiates is water-grid.vert:74-111. */
+ * the workspace).  Deterministic: the FP32 partial sums of each run of one or
+ * two tiles are summed with Kahan compensation in a fixed order, and the
+ * per-wave gradients are formed and added in FP64 in a fixed order.  No
+ * reference counterpart (the reference has no derivatives); the forward it
+ * differentiates is water-grid.vert:74-111. */
 wt_status wt_gerstner_adjoint(const wt_patch* host_patches, const wt_patch* patches, uint32_t n_patches,
                               const wt_wave* waves, uint32_t n_waves,
                               const wt_heightmap* hm,
