@@ -36,7 +36,22 @@ def test_adam_fit_reduces_loss(wt, gpu):
     target, start = workloads.config4()
     r = fit.fit_waves(target.patches, target.waves, start, steps=60, lr=1e-2)
     assert np.isfinite(r["loss_last"])
-    assert r["loss_last"] < 0.5 * r["loss_first"], r
+    assert r["loss_last"] < 0.2 * r["loss_first"], {k: r[k] for k in ("loss_first", "loss_last")}
+
+
+@pytest.mark.parametrize("seed", [3, 10, 12])
+def test_adam_fit_recovers_the_hidden_waves(wt, gpu, seed):
+    """The full adjoint-fit configuration (seed 3) and two other draws of it:
+    500 Adam steps from the perturbed start (A, lambda, Q +-10 %, direction
+    +-10 degrees, phase +-0.5 rad) recover the 16 hidden waves (median errors;
+    the plain loss falls from above 1 to about 1e-4)."""
+    from wave_tool_gb300 import fit, workloads
+    target, start = workloads.config4(seed)
+    r = fit.fit_waves(target.patches, target.waves, start, steps=500, lr=1e-2)
+    e = fit.parameter_errors(r["fitted"], target.waves)
+    assert r["loss_last"] < 2e-3 and r["loss_first"] > 0.5, (r["loss_first"], r["loss_last"])
+    assert e["amplitude_rel"] < 1e-2 and e["wavelength_rel"] < 1e-3 and e["steepness_rel"] < 5e-2, e
+    assert e["direction_deg"] < 0.1 and e["phase_rad"] < 1e-2, e
 
 
 def test_cuda_graph_replay_equals_eager(wt, gpu):

@@ -8,6 +8,14 @@ runs Adam on (log A, log lambda, direction angle, log Q, phase) against an
 L2 height + normal loss — the adjoint-fit configuration (512 x 512 grid,
 16 hidden waves, 10 % / 10 degree / 0.5 rad perturbed start, 500 steps).
 No reference counterpart: the reference only animates hand-set waves.
+
+The loss is first restricted to a growing window.  A wave whose wavelength
+starts 10 % off has a phase error that grows as dk * r across the patch (tens
+of radians over 100 m for a 2 m wave), so the whole-patch loss holds no descent
+direction back to it and Adam shrinks its amplitude instead.  Inside a
+Gaussian window a few metres wide around each patch centre the phase error is
+under a radian; the window then widens geometrically, no faster than the
+wavelengths converge, and the last steps use the plain loss.
 """
 from __future__ import annotations
 
@@ -71,11 +79,42 @@ def waves_to_fields(waves: np.ndarray, device="cuda"):
     return torch.from_numpy(np.ascontiguousarray(waves).view(np.float32).reshape(-1, 8).copy()).to(device)
 
 
+def window_r2(patches: np.ndarray, n_vertices: int) -> np.ndarray:
+    """Squared distance (m^2) of each output vertex's grid point from its
+    patch's centre, in output order (vertex out_offset + row * cols + col at
+    the bilerp of the corners, water-grid.vert:87-91); 0 for vertices no patch
+    writes."""
+    r2 = np.zeros(n_vertices, np.float32)
+    for p in patches:
+        cols, rows = int(p["cols"]), int(p["rows"])
+        u = np.arange(cols, dtype=np.float64) / max(cols - 1, 1)
+        v = np.arange(rows, dtype=np.float64) / max(rows - 1, 1)
+        bl, br, tl, tr = (p[k].astype(np.float64) for k in ("bl", "br", "tl", "tr"))
+        bot = bl[None, :] + u[:, None] * (br - bl)[None, :]  # [cols, 2]
+        top = tl[None, :] + u[:, None] * (tr - tl)[None, :]
+        xz = bot[None, :, :] + v[:, None, None] * (top - bot)[None, :, :]  # [rows, cols, 2]
+        c = 0.25 * (bl + br + tl + tr)
+        o = int(p["out_offset"])
+        r2[o:o + rows * cols] = ((xz - c) ** 2).sum(-1).reshape(-1)
+    return r2
+
+
 def fit_waves(patches: np.ndarray, target_waves: np.ndarray, start_waves: np.ndarray, steps: int = 500,
-              lr: float = 1e-2, normal_weight: float = 1.0, log_every: int = 0):
+              lr: float = 1e-2, normal_weight: float = 1.0, log_every: int = 0, phase_lr: float | None = None,
+              window_start: float | None = 2.5, window_steps: int | None = None):
     """Adam on (log A, log lambda, angle, log Q, phase) of start_waves to match
     the heights (y displacement) and normals of target_waves.  Speed is kept.
-    Returns a dict with the loss history, timings and the fitted waves."""
+
+    The phase learns at phase_lr (default 10 * lr): its starting error
+    includes dk * speed * t, several radians for the short waves.  With
+    window_start (m) set, the per-vertex loss is weighted by
+    exp(-r^2 / (2 sigma^2)) (normalised to mean 1), r the distance from the
+    patch centre, sigma growing geometrically from window_start to 2.8 patch
+    half-diagonals over window_steps steps (default 70 % of the steps); the
+    remaining steps use the plain loss.  None: the plain loss throughout.
+
+    Returns a dict: loss_first / loss_last (the plain loss of the starting and
+    the fitted waves), the training-loss history, timings and the fitted waves."""
     torch = _torch()
     dev = torch.device("cuda")
     tgt = Surface(patches, target_waves)
@@ -91,16 +130,41 @@ def fit_waves(patches: np.ndarray, target_waves: np.ndarray, start_waves: np.nda
     logQ = torch.log(f0[:, 4].clamp_min(1e-12)).clone().requires_grad_(True)
     ph = f0[:, 6].clone().requires_grad_(True)
     speed = f0[:, 5].clone()
-    opt = torch.optim.Adam([logA, logL, ang, logQ, ph], lr=lr)
+    opt = torch.optim.Adam([{"params": [logA, logL, ang, logQ], "lr": lr},
+                            {"params": [ph], "lr": 10.0 * lr if phase_lr is None else phase_lr}])
+    if window_start is not None:
+        r2 = torch.from_numpy(window_r2(patches, surf.n_vertices)).to(dev)
+        half_diag = max(0.5 * math.hypot(float(p["tr"][0] - p["bl"][0]), float(p["tr"][1] - p["bl"][1]))
+                        for p in patches)
+        sigma_end = max(2.8 * half_diag, window_start)
+        wsteps = max(1, int(round(0.7 * steps)) if window_steps is None else window_steps)
+
+    def fields_now():
+        return torch.stack([logA.exp(), logL.exp(), ang.cos(), ang.sin(), logQ.exp(), speed, ph,
+                            torch.zeros_like(ph)], 1)
+
+    def plain_loss():
+        with torch.no_grad():
+            pos, nrm = GerstnerFunction.apply(fields_now(), surf, WT_OUT_DISPLACEMENT)
+            ey = ((pos[:, 1] - y_t) ** 2).mean() / y_scale
+            return float(ey + normal_weight * ((nrm[:, :3] - n_t) ** 2).sum(1).mean())
+
+    loss_first = plain_loss()
     hist = []
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for it in range(steps):
         opt.zero_grad(set_to_none=True)
-        fields = torch.stack([logA.exp(), logL.exp(), ang.cos(), ang.sin(), logQ.exp(), speed, ph,
-                              torch.zeros_like(ph)], 1)
-        pos, nrm = GerstnerFunction.apply(fields, surf, WT_OUT_DISPLACEMENT)
-        loss = ((pos[:, 1] - y_t) ** 2).mean() / y_scale + normal_weight * ((nrm[:, :3] - n_t) ** 2).sum(1).mean()
+        pos, nrm = GerstnerFunction.apply(fields_now(), surf, WT_OUT_DISPLACEMENT)
+        ey = (pos[:, 1] - y_t) ** 2 / y_scale
+        en = ((nrm[:, :3] - n_t) ** 2).sum(1)
+        if window_start is not None and it < wsteps:
+            sigma = window_start * (sigma_end / window_start) ** (it / wsteps)
+            wgt = torch.exp(r2 * (-0.5 / (sigma * sigma)))
+            wgt = wgt / wgt.mean()
+            loss = (wgt * (ey + normal_weight * en)).mean()
+        else:
+            loss = (ey + normal_weight * en).mean()
         loss.backward()
         opt.step()
         if log_every and it % log_every == 0:
@@ -110,12 +174,12 @@ def fit_waves(patches: np.ndarray, target_waves: np.ndarray, start_waves: np.nda
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     hist = [(i, float(l)) for i, l in hist]
+    loss_last = plain_loss()
     fitted = np.zeros(len(start_waves), WAVE_DTYPE)
     with torch.no_grad():
-        fields = torch.stack([logA.exp(), logL.exp(), ang.cos(), ang.sin(), logQ.exp(), speed, ph,
-                              torch.zeros_like(ph)], 1).cpu().numpy()
+        fields = fields_now().cpu().numpy()
     fitted.view(np.float32).reshape(-1, 8)[:] = fields
-    return {"loss_first": hist[0][1], "loss_last": hist[-1][1], "history": hist, "seconds": dt,
+    return {"loss_first": loss_first, "loss_last": loss_last, "history": hist, "seconds": dt,
             "ms_per_step": 1e3 * dt / steps, "fitted": fitted}
 
 
@@ -133,4 +197,4 @@ def parameter_errors(fitted: np.ndarray, target: np.ndarray) -> dict:
     }
 
 
-__all__ = ["GerstnerFunction", "fit_waves", "waves_to_fields", "parameter_errors", "math"]
+__all__ = ["GerstnerFunction", "fit_waves", "waves_to_fields", "parameter_errors", "window_r2"]

@@ -177,12 +177,13 @@ def config3(n_patches: int = 256, seed: int = 2, spacing: float = 0.2) -> Worklo
                     np.array(waves, dtype=WAVE_DTYPE), hm)
 
 
-def config4() -> tuple[Workload, np.ndarray]:
+def config4(seed: int = 3) -> tuple[Workload, np.ndarray]:
     """Adjoint fit: 512 x 512 vertices over 100 m x 100 m, a hidden 16-wave set
     (lambda log-uniform [1, 30] m, A = lambda/100 * U[0.5,1], +-90 deg), t = 10 s.
     Returns the target workload and the perturbed starting waves: A, lambda, Q
-    scaled by U[0.9, 1.1], direction rotated U[-10, 10] deg, phase + U[-0.5, 0.5]."""
-    rng = SplitMix64(3)
+    scaled by U[0.9, 1.1], direction rotated U[-10, 10] deg, phase + U[-0.5, 0.5].
+    Other seeds give other draws of the same distributions."""
+    rng = SplitMix64(seed)
     n = 16
     hidden = np.array(waves_wide(rng, n, lam=(1.0, 30.0)), dtype=WAVE_DTYPE)
     patches = np.array([square_patch(0.0, 0.0, 50.0, 512, 0, n, 10.0, 0)], dtype=PATCH_DTYPE)
