@@ -147,6 +147,19 @@ __device__ __forceinline__ void wave_moments(const float4* __restrict__ gbuf, ui
     }
 }
 
+// Waves of the next phase-2 chunk, out of rem still to do: 32 while at least
+// 32 remain; else the rest when it fills its power-of-two lane group to
+// within an eighth (or is at most 3); else the largest power of two below it.
+// A chunk's lanes idle where its waves fall short of the power of two, so a
+// remainder of 20 waves runs as 16 + 4 (20 lanes' work) instead of as one
+// 32-lane group.
+__device__ __forceinline__ uint32_t adj_chunk_waves(uint32_t rem) {
+    if (rem >= 32u) return 32u;
+    if (rem <= 3u) return rem;
+    const uint32_t P = 1u << (32 - __clz(rem - 1u));  // smallest power of two >= rem
+    return 8u * (P - rem) <= P ? rem : P >> 1;
+}
+
 // SAVED: phase 1 reads the forward's saved sums instead of recomputing them
 // (a compile-time switch, so that the recomputing kernel carries no test);
 // both forms fit 96 registers and run 5 blocks (20 warps) per SM.
@@ -228,11 +241,11 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
                         const uint32_t Sh = h == 0 ? min(S, 4u) : (S > 4u ? S - 4u : 0u);
                         if (Sh == 0) break;
                         const uint32_t ch = c0 + 128u * h;
-                        float acc[4][8];
+                        float2 acc[4][4];
 #pragma unroll
                         for (int j = 0; j < 4; ++j)
 #pragma unroll
-                            for (int mm = 0; mm < 8; ++mm) acc[j][mm] = 0.0f;
+                            for (int mm = 0; mm < 4; ++mm) acc[j][mm] = make_float2(0.0f, 0.0f);
                         for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
                             const uint32_t nw = min(32u, nwaves - w0);
                             __syncwarp();
@@ -245,8 +258,9 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
                         for (int j = 0; j < 4; ++j) {
                             if ((uint32_t)j < Sh) {
                                 float4* d = gbuf + kGbufF4 * (lane + 32 * (4 * h + j));
-                                d[0] = make_float4(acc[j][0], acc[j][1], acc[j][2], acc[j][3]);
-                                d[1] = make_float4(acc[j][4], acc[j][5], acc[j][6], acc[j][7]);
+                                const VertexSums v = sums_of(acc[j]);
+                                d[0] = make_float4(v.dx, v.dy, v.dz, v.jx);
+                                d[1] = make_float4(v.jz, v.sxx, v.sxz, v.szz);
                             }
                         }
                     }
@@ -274,12 +288,12 @@ k_adjoint(const wt_patch* __restrict__ patches, HmDev hm, const float* __restric
                 // ---- phase 2: wave per lane, records of this tile
                 const uint32_t nvalid0 = min(32u, cols - c0);  // valid lanes at j = 0
                 const uint32_t rec0 = part_off[q] + lc * nwaves;
-                for (uint32_t w0 = 0; w0 < nwaves; w0 += 32) {
+                for (uint32_t w0 = 0, nwc = 0; w0 < nwaves; w0 += nwc) {
                     // a chunk of nwc <= 32 waves: lanes form 32 / P groups of P
                     // lanes (P = nwc rounded up to a power of two); group g walks
                     // the vertex lanes l = g, g + G, ... and the groups' moments
                     // are combined by a fixed shuffle tree
-                    const uint32_t nwc = min(32u, nwaves - w0);
+                    nwc = adj_chunk_waves(nwaves - w0);
                     uint32_t P = 1;
                     while (P < nwc) P <<= 1;
                     const uint32_t G = 32u / P;

@@ -241,13 +241,24 @@ __device__ __forceinline__ uint32_t hi32_round(unsigned long long x) {
 
 // Per-wave staging in shared memory (3 float4 per wave, up to 32 waves per warp):
 //   [0] t32, a32 (fixed-point turns), cos d, sin d      d = one 32-column step
-//   [1] Q*A*Dx, A, Q*A*Dz, A*k*Dx
-//   [2] A*k*Dz, Q*A*k*Dx^2, Q*A*k*Dx*Dz, Q*A*k*Dz^2
+//   [1] Q*A*Dx, A,  Q*A*Dz, Q*A*k*Dx^2
+//   [2] A*k*Dx, Q*A*k*Dx*Dz,  A*k*Dz, Q*A*k*Dz^2
+// i.e. four (cos coefficient, sin coefficient) pairs, one per pair of sums
+// (dx, dy), (dz, sxx), (jx, sxz), (jz, szz): each pair of sums takes one paired
+// FP32 FMA (__ffma2_rn, sm_100+) of its coefficients with (cos, sin) of the
+// vertex, two correctly rounded FMAs in one instruction.
 // Lane l's vertices j = 0..S-1 sit at columns c0 + l + 32 j.  Vertex 0 takes
 // a MUFU sincos of its exact start phase, vertex 1 an exact rotation by d, and
 // vertices j >= 2 the Chebyshev recurrence x[j] = 2 cos(d) x[j-1] - x[j-2]
-// (one FMA per value; its error grows at most linearly in j).
+// (one FMA per value, cos and sin paired; its error grows at most linearly
+// in j).
 constexpr int kStage = 3;
+
+// The eight sums of one vertex as the wave loop accumulates them:
+//   p[0] = (dx, dy)  p[1] = (dz, sxx)  p[2] = (jx, sxz)  p[3] = (jz, szz)
+__device__ __forceinline__ VertexSums sums_of(const float2 (&p)[4]) {
+    return VertexSums{p[0].x, p[0].y, p[1].x, p[2].x, p[3].x, p[1].y, p[2].y, p[3].y};
+}
 
 // One lane's share of the staging: wave constants for the tile at (c0, row).
 __device__ __forceinline__ void stage_wave(const PairCoef& c, uint32_t c0, uint32_t row, float4* __restrict__ d) {
@@ -266,16 +277,19 @@ __device__ __forceinline__ void stage_wave(const PairCoef& c, uint32_t c0, uint3
     sd = fmaf(cd, eps, sd);
     cd = cdn;
     d[0] = make_float4(__uint_as_float(t32), __uint_as_float(a32), cd, sd);
-    d[1] = make_float4(c.qadx, c.a, c.qadz, c.akdx);
-    d[2] = make_float4(c.akdz, c.qakxx, c.qakxz, c.qakzz);
+    d[1] = make_float4(c.qadx, c.a, c.qadz, c.qakxx);
+    d[2] = make_float4(c.akdx, c.qakxz, c.akdz, c.qakzz);
 }
 
 // The wave loop of one tile for a compile-time S: sums of nw staged waves
-// into acc[0..S-1].
+// into acc[0..S-1] (pairs as in sums_of).
+// Two waves per iteration with 4 vertices per lane, one with 8 (two would
+// spill at the 8-vertex shapes' 128 registers).
 template <int S, int SMAX>
-__device__ __forceinline__ void wave_loop(float (&acc)[SMAX][8], const float4* __restrict__ wst, uint32_t nw,
+__device__ __forceinline__ void wave_loop(float2 (&acc)[SMAX][4], const float4* __restrict__ wst, uint32_t nw,
                                           uint32_t lane) {
-#pragma unroll 2
+    constexpr int kUnroll = SMAX <= 4 ? 2 : 1;
+#pragma unroll kUnroll
     for (uint32_t i = 0; i < nw; ++i) {
         const float4 w0v = wst[kStage * i];
         const float4 w1 = wst[kStage * i + 1];
@@ -283,27 +297,26 @@ __device__ __forceinline__ void wave_loop(float (&acc)[SMAX][8], const float4* _
         const uint32_t tl = __float_as_uint(w0v.x) + lane * __float_as_uint(w0v.y);
         const float ang = (float)(int)tl * kTurnToRad;
         const float cd = w0v.z, sd = w0v.w, tc = 2.0f * cd;
-        float c, s, cp = 0.0f, sp = 0.0f;
-        __sincosf(ang, &s, &c);
+        const float2 k0 = make_float2(w1.x, w1.y), k1 = make_float2(w1.z, w1.w);
+        const float2 k2 = make_float2(w2.x, w2.y), k3 = make_float2(w2.z, w2.w);
+        const float2 tc2 = make_float2(tc, tc);
+        float2 x, xp = make_float2(0.0f, 0.0f);  // (cos, sin) at vertex j and j - 1
+        __sincosf(ang, &x.y, &x.x);
 #pragma unroll
         for (int j = 0; j < S; ++j) {
             if (j == 1) {
-                const float cn = fmaf(c, cd, -s * sd);
-                const float sn = fmaf(s, cd, c * sd);
-                cp = c; sp = s; c = cn; s = sn;
+                const float2 xn = make_float2(fmaf(x.x, cd, -x.y * sd), fmaf(x.y, cd, x.x * sd));
+                xp = x;
+                x = xn;
             } else if (j >= 2) {
-                const float cn = fmaf(tc, c, -cp);
-                const float sn = fmaf(tc, s, -sp);
-                cp = c; sp = s; c = cn; s = sn;
+                const float2 xn = __ffma2_rn(tc2, x, make_float2(-xp.x, -xp.y));
+                xp = x;
+                x = xn;
             }
-            acc[j][0] = fmaf(w1.x, c, acc[j][0]);
-            acc[j][1] = fmaf(w1.y, s, acc[j][1]);
-            acc[j][2] = fmaf(w1.z, c, acc[j][2]);
-            acc[j][3] = fmaf(w1.w, c, acc[j][3]);
-            acc[j][4] = fmaf(w2.x, c, acc[j][4]);
-            acc[j][5] = fmaf(w2.y, s, acc[j][5]);
-            acc[j][6] = fmaf(w2.z, s, acc[j][6]);
-            acc[j][7] = fmaf(w2.w, s, acc[j][7]);
+            acc[j][0] = __ffma2_rn(k0, x, acc[j][0]);
+            acc[j][1] = __ffma2_rn(k1, x, acc[j][1]);
+            acc[j][2] = __ffma2_rn(k2, x, acc[j][2]);
+            acc[j][3] = __ffma2_rn(k3, x, acc[j][3]);
         }
     }
 }
@@ -316,7 +329,7 @@ namespace dev {
 
 // The wave loop for the tile's S (warp-uniform), compile-time in each branch.
 template <int SMAX>
-__device__ __forceinline__ void wave_loop_dispatch(uint32_t S, float (&acc)[SMAX][8], const float4* __restrict__ wst,
+__device__ __forceinline__ void wave_loop_dispatch(uint32_t S, float2 (&acc)[SMAX][4], const float4* __restrict__ wst,
                                                    uint32_t nw, uint32_t lane) {
     if (SMAX == 4) {
         switch (S) {

@@ -431,11 +431,11 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
         const uint32_t c0 = (lt - row * tpr) * 32u * SMAX;
         const uint32_t S = min((uint32_t)SMAX, (cols - c0 + 31u) / 32u);  // the row's last tile is narrower
 
-        float acc[SMAX][8];
+        float2 acc[SMAX][4];
 #pragma unroll
         for (int j = 0; j < SMAX; ++j)
 #pragma unroll
-            for (int m = 0; m < 8; ++m) acc[j][m] = 0.0f;
+            for (int m = 0; m < 4; ++m) acc[j][m] = make_float2(0.0f, 0.0f);
 
         for (uint32_t w0 = 0; w0 < nwaves; w0 += chunk) {
             const uint32_t nw = min(chunk, nwaves - w0);
@@ -459,8 +459,8 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
 #pragma unroll
             for (int j = 0; j < SMAX; ++j) {
                 if ((uint32_t)j < S) {
-                    ebuf[(2 * j) * 32 + lane] = make_float4(acc[j][0], acc[j][1], acc[j][2], acc[j][3]);
-                    ebuf[(2 * j + 1) * 32 + lane] = make_float4(acc[j][4], acc[j][5], acc[j][6], acc[j][7]);
+                    ebuf[(2 * j) * 32 + lane] = make_float4(acc[j][0].x, acc[j][0].y, acc[j][1].x, acc[j][1].y);
+                    ebuf[(2 * j + 1) * 32 + lane] = make_float4(acc[j][2].x, acc[j][2].y, acc[j][3].x, acc[j][3].y);
                 }
             }
 #pragma unroll 1
@@ -470,8 +470,10 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
                     const float4 s0 = ebuf[(2 * j) * 32 + lane], s1 = ebuf[(2 * j + 1) * 32 + lane];
                     const float xl = fmaf(32.0f * (float)j, gx, xb);
                     const float zl = fmaf(32.0f * (float)j, gz, zb);
-                    VertexSums s{s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
-                    finish_vertex<MODE>(s, xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums, su, so);
+                    const float2 pr[4] = {make_float2(s0.x, s0.y), make_float2(s0.z, s0.w), make_float2(s1.x, s1.y),
+                                          make_float2(s1.z, s1.w)};
+                    finish_vertex<MODE>(sums_of(pr), xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums, su,
+                                        so);
                 }
             }
         } else {
@@ -481,9 +483,8 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
                 if ((uint32_t)j < S && col < cols) {
                     const float xl = fmaf(32.0f * j, gx, xb);
                     const float zl = fmaf(32.0f * j, gz, zb);
-                    VertexSums s{acc[j][0], acc[j][1], acc[j][2], acc[j][3],
-                                 acc[j][4], acc[j][5], acc[j][6], acc[j][7]};
-                    finish_vertex<MODE>(s, xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums, su, so);
+                    finish_vertex<MODE>(sums_of(acc[j]), xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums,
+                                        su, so);
                 }
             }
         }
