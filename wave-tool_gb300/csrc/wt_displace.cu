@@ -18,10 +18,11 @@
 //                            c0 + l + 32 j, j < S.  Per wave: one MUFU sincos
 //                            per lane, an exact rotation to the second vertex,
 //                            then the Chebyshev recurrence on the FMA pipe; 8
-//                            FMAs accumulate displacement and the surface
-//                            Jacobian.  Epilogue: heightmap bilerp +
-//                            gradient, exact normal, streaming stores (and,
-//                            by variant, the wave sums or the vertex stage).
+//                            FMAs, issued as 4 paired FP32 FMAs, accumulate
+//                            displacement and the surface Jacobian.  Epilogue:
+//                            heightmap bilerp + gradient, exact normal,
+//                            streaming stores (and, by variant, the wave sums
+//                            or the vertex stage).
 #include <cuda_runtime.h>
 
 #include <atomic>
