@@ -1,8 +1,10 @@
 """Benchmark of the Gerstner water-surface path on GB300.
 
 Metric: Gerstner terms/s = sum over patches of (vertices x waves) per second,
-at <= 1e-5 relative displacement error vs FP64 (the error bound is enforced by
-tests/; this file only times).  Workload: the batched configuration — 256
+at <= 1e-5 relative displacement error vs FP64 (enforced by tests/, and
+measured here on the timed table after the timed region: sampled rows of every
+patch against the FP64 oracle, the `accuracy` field).  Workload: the batched
+configuration — 256
 independent patches, grid side log-uniform in [64, 1024], 8..64 waves each,
 t U[0, 1e3] s, with the 512^2 noise heightmap layer — as one persistent
 launch.  A step = the three launches of one wt_gerstner_displace call
@@ -12,14 +14,15 @@ launch.  A step = the three launches of one wt_gerstner_displace call
 
 Prints one JSON line (rank 0).  Under torchrun each rank runs its own
 256-patch workload (seed 2 + rank; weak scaling, no collective on the data
-path) and the step time is the max over ranks.
+path) and the step time is the max over ranks; with --split the ranks share
+ONE 256-patch table, each running its LPT shard of the patches (strong
+scaling), and the value is the table's terms over the max step time.
 """
 from __future__ import annotations
 
 import argparse
 import json
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -35,8 +38,8 @@ import __graft_entry__  # noqa: E402
 
 METRIC = "Gerstner terms/s (verts x waves) at <=1e-5 rel err vs FP64; batched persistent launch"
 UNIT = "terms/s"
-PROFILE_TRAFFIC = ROOT / "profiles" / "forward_config3_ncu.md"
-E2E_GROUPS = 4  # streams the end-to-end step is split over
+PROFILE_TRAFFIC = ROOT / "profiles" / "forward_traffic.json"
+E2E_GROUPS = 16  # streams the end-to-end step is split over (0.945 / 0.957 / 0.964 of the D2H link with 4 / 8 / 16)
 
 
 def parse_args():
@@ -57,6 +60,11 @@ def parse_args():
                     help="with --mode adjoint: time wt_gerstner_adjoint_saved on a saving forward's sums")
     ap.add_argument("--tuning", default="auto",
                     help="'auto' (autotune before timing) or WARPS,CHUNK[,VPL,EPI] to fix the launch shape")
+    ap.add_argument("--split", action="store_true",
+                    help="under torchrun: the ranks share one table, each its LPT shard of the patches")
+    ap.add_argument("--e2e-groups", type=int, default=E2E_GROUPS,
+                    help="stream groups of the end-to-end step (copy-back of one overlaps the next's kernel)")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 check of the timed table")
     return ap.parse_args()
 
 
@@ -119,36 +127,72 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(load), "power_w_max": pmax}
 
 
-def traffic_from_profile():
-    """DRAM bytes per forward launch from the committed ncu summary, if any."""
+def traffic_from_profile(tuning, vertices):
+    """DRAM bytes of one forward launch of the tuned shape: the bytes per
+    vertex an ncu capture of that kernel measured (profiles/forward_traffic.json,
+    keyed by the kernel's launch shape) times this launch's vertices; None
+    when no capture of the shape exists."""
     if not PROFILE_TRAFFIC.exists():
         return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", PROFILE_TRAFFIC.read_text())
-    return float(m.group(1)) if m else None
+    try:
+        rec = json.loads(PROFILE_TRAFFIC.read_text())
+    except ValueError:
+        return None
+    key = (f"warps={tuning['warps_per_block']},vpl={tuning['max_vertices_per_lane']},"
+           f"epi={tuning['epilogue_in_shared']}")
+    r = rec.get("shapes", {}).get(key)
+    return None if r is None else r["dram_bytes_per_vertex"] * vertices
 
 
-def cpu_sample(w, target_s: float, threads: int, analytic: bool = False):
-    """Runs the oracle's FP32 restatement of the reference shader (5 surface
-    evaluations per vertex, central-difference normals; with `analytic`, one
-    evaluation per vertex with Jacobian normals) over the first rows of every
-    patch, rows chosen so the run lasts about target_s."""
-    from oracle import oracle as O
-    import types
-    hmp = None
-    tex = None
-    if w.heightmap is not None:
-        tex = O.noise_f64(w.heightmap.terms, w.heightmap.width, w.heightmap.height).astype(np.float32)
-        hmp = types.SimpleNamespace(sample_scale=w.heightmap.sample_scale, disp_scale=w.heightmap.disp_scale,
-                                    wrap=w.heightmap.wrap)
-    t0 = time.perf_counter()
-    O.cpu_baseline(w.patches, w.waves, tex, hmp, row_limit=1, threads=threads, analytic=analytic)
-    probe = time.perf_counter() - t0
-    rows = max(1, min(int(target_s / max(probe, 1e-3)), int(w.patches["rows"].max())))
-    t0 = time.perf_counter()
-    nv, _, _ = O.cpu_baseline(w.patches, w.waves, tex, hmp, row_limit=rows, threads=threads, analytic=analytic)
-    dt = time.perf_counter() - t0
-    terms = int(sum(min(rows, int(p["rows"])) * int(p["cols"]) * int(p["wave_count"]) for p in w.patches))
-    return terms / dt, dt, rows, terms
+class CpuWorkload:
+    """The timed CPU restatement of the reference shader (the oracle's
+    reference_mode.c built for speed, oracle/_build/libcpu_timed.so) over the
+    benchmark's table: 5 surface evaluations per vertex, central-difference
+    normals (with `analytic`, one evaluation per vertex and Jacobian normals),
+    on the rows r = phase + k * stride of EVERY patch, so a sample is spread
+    evenly over each patch and `stride` consecutive phases cover the table."""
+
+    def __init__(self, w):
+        from oracle import oracle as O
+        import types
+        self.O, self.w = O, w
+        self.tex = self.hmp = None
+        if w.heightmap is not None:
+            self.tex = O.noise_f64(w.heightmap.terms, w.heightmap.width, w.heightmap.height).astype(np.float32)
+            self.hmp = types.SimpleNamespace(sample_scale=w.heightmap.sample_scale,
+                                             disp_scale=w.heightmap.disp_scale, wrap=w.heightmap.wrap)
+        n = int(w.n_vertices)
+        self.out = (np.zeros((n, 4), np.float32), np.zeros((n, 4), np.float32))
+        from oracle import build as ob
+        self.flags = " ".join(ob.TIMED_CFLAGS)
+
+    def run(self, stride, phase, threads, analytic=False):
+        t0 = time.perf_counter()
+        _, terms = self.O.cpu_baseline_rows(self.w.patches, self.w.waves, self.tex, self.hmp, stride, phase, threads,
+                                            analytic, out=self.out)
+        return terms, time.perf_counter() - t0
+
+    def stride_for(self, seconds, threads, analytic=False):
+        """Row stride whose sample takes about `seconds` (probed on every
+        64th row)."""
+        terms, dt = self.run(64, 0, threads, analytic)
+        full = dt * self.w.n_terms / max(terms, 1)
+        return max(1, int(np.ceil(full / max(seconds, 1e-3))))
+
+
+def every_nth(n: int) -> str:
+    if n == 1:
+        return "every row"
+    suffix = "th" if 10 <= n % 100 <= 20 else {1: "st", 2: "nd", 3: "rd"}.get(n % 10, "th")
+    return f"every {n}{suffix} row"
+
+
+def cpu_sample(cw, target_s: float, threads: int, analytic: bool = False):
+    """One bounded sample of about target_s: every stride-th row of every
+    patch (phase stride // 2).  Returns (terms/s, seconds, stride, terms)."""
+    stride = cw.stride_for(target_s, threads, analytic)
+    terms, dt = cw.run(stride, stride // 2, threads, analytic)
+    return terms / dt, dt, stride, terms
 
 
 def run_reference(args):
@@ -162,23 +206,30 @@ def run_reference(args):
     from wave_tool_gb300 import workloads
     w = workloads.config3(n_patches=args.patches, seed=2)
     threads = os.cpu_count() or 1
-    per_step = max(1.0, args.cpu_seconds / max(1, args.steps))
-    rates, dts = [], []
+    cw = CpuWorkload(w)
+    per_step = max(0.5, args.cpu_seconds / max(1, args.steps))
+    stride = cw.stride_for(per_step, threads)
+    terms_t, secs, dts = 0, 0.0, []
     for i in range(args.warmup + args.steps):
-        r, dt, rows, terms = cpu_sample(w, per_step, threads)
+        terms, dt = cw.run(stride, i % stride, threads)   # phases cycle: `stride` steps cover the table
         if i >= args.warmup:
-            rates.append(r)
+            terms_t += terms
+            secs += dt
             dts.append(dt)
-    value = statistics.median(rates)
-    sample = f"first {rows} rows of each of the {args.patches} patches ({terms} terms) per step"
+    value = terms_t / secs
+    covered = min(1.0, args.steps / stride)
+    sample = (f"per step {every_nth(stride)} of each of the {args.patches} patches (rows phase + k*{stride}, phase "
+              f"cycling 0..{stride - 1}, so {stride} steps cover the whole table; the {args.steps} timed steps "
+              f"covered {covered:.0%} of its rows, {terms_t} terms in {secs:.1f} s)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(dts),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": w.name, "patches": args.patches, "terms": w.n_terms,
-                   "implementation": "FP32 restatement of water-grid.vert (5 evaluations/vertex, FD normals), "
-                                     "POSIX threads on all host cores"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "config": workload_config(args, w, world, args.split and world > 1),
+        "implementation": "FP32 restatement of water-grid.vert (5 evaluations/vertex, FD normals, FP32 phase), "
+                          f"gcc {cw.flags}, POSIX threads on all host cores",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "build": f"gcc {cw.flags}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     del wt
@@ -406,6 +457,59 @@ def side_measurements(wt, workloads, surf, pos, nrm, flags, flush, stream, ms_st
     return out
 
 
+def workload_config(args, w, world, split=False):
+    """The `config` object of both arms' lines: the workload only."""
+    return {"workload": w.name.split("_shard")[0], "patches": args.patches, "vertices": w.n_vertices,
+            "terms_per_step": w.n_terms, "waves_per_patch": "8..64", "grid_side": "64..1024 log-uniform",
+            "heightmap": "none" if args.no_heightmap else "512^2 noise",
+            "parallelism": (f"split x{world} (one {args.patches}-patch table, LPT shards of its patches)"
+                            if split else f"weak x{world} (each GPU its own {args.patches} patches)")}
+
+
+def timed_table_accuracy(w, hm, pos, nrm):
+    """The path's error metric measured on the outputs of the timed table:
+    the first, the last and six spread rows of EVERY patch against the FP64
+    oracle (the checker; run after the timed region)."""
+    from oracle import build as ob, oracle as O
+    ob.build_oracle()
+    tex = hm.texels.cpu().numpy() if hm is not None else None
+    t0 = time.perf_counter()
+    acc = O.accuracy_sampled_rows(w.patches, w.waves, pos.cpu().numpy(), nrm.cpu().numpy(), tex, w.heightmap)
+    acc["bound"] = 1e-5
+    acc["within_bound"] = bool(acc["max_rel_err"] <= 1e-5)
+    acc["check_s"] = time.perf_counter() - t0
+    acc["note"] = ("outputs of the last timed step; displacement error max|d32 - d64| / max|d64| over the checked "
+                   "vertices (per_patch_max_rel_err: the worst single patch), normal angle excluding samples within "
+                   "1e-3 texel of a heightmap cell edge")
+    return acc
+
+
+def measure_link(dev):
+    """Host link bandwidth: 1 GiB device <-> pinned host cudaMemcpyAsync, best
+    of 5 each way (CUDA events)."""
+    import torch
+    n = 1 << 30
+    d = torch.empty(n, dtype=torch.uint8, device=dev)
+    h = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    d.fill_(1)
+    out = {}
+    for name, fn in (("d2h_gbs", lambda: h.copy_(d, non_blocking=True)),
+                     ("h2d_gbs", lambda: d.copy_(h, non_blocking=True))):
+        fn()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(5):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            best = min(best, a.elapsed_time(b))
+        out[name] = n / (best * 1e-3) / 1e9
+    del d, h
+    return out
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -418,7 +522,17 @@ def run_ours(args):
     wt.lib()
     from wave_tool_gb300 import workloads
 
-    w = workloads.config3(n_patches=args.patches, seed=2 + rank)
+    split = args.split and world > 1
+    if split:
+        # one table for every rank; each rank runs its LPT shard of the patches
+        from wave_tool_gb300 import sharding
+        full = workloads.config3(n_patches=args.patches, seed=2)
+        mine, _ = sharding.shard_patches(full.patches, world, rank)
+        w = workloads.Workload(f"{full.name}_shard{rank}of{world}", mine, full.waves, full.heightmap)
+        table_terms = full.n_terms
+    else:
+        w = workloads.config3(n_patches=args.patches, seed=2 + rank)
+        table_terms = None
     if args.no_heightmap:
         w.heightmap = None
     hm = wt.heightmap_from(w.heightmap)
@@ -472,7 +586,16 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_step = float(t.item())
     terms = w.n_terms
-    value = terms * world / (ms_step * 1e-3)
+    # weak scaling: every rank the same amount of work; split: the one table
+    job_terms = table_terms if split else terms * world
+    value = job_terms / (ms_step * 1e-3)
+
+    # the metric's error bound on the table just timed (outside the timed
+    # region; the FP64 oracle is the checker): sampled rows of every patch
+    accuracy = None
+    if rank == 0 and not args.no_accuracy:
+        accuracy = timed_table_accuracy(w, hm, pos, nrm)
+    link = measure_link(dev) if rank == 0 else None
 
     # end to end through the C ABI from pinned host buffers, outputs in the
     # layout the reference's vertex array consumes (world positions and normals
@@ -486,13 +609,14 @@ def run_ours(args):
     hnrm = torch.empty(enrm.shape, dtype=enrm.dtype, pin_memory=True)
     htex = hm.texels.cpu().pin_memory() if hm is not None else None
     hw = torch.from_numpy(np.ascontiguousarray(w.waves).view(np.uint8).reshape(-1)).pin_memory()
+    n_groups = max(1, args.e2e_groups)
     cum = np.cumsum(w.patches["cols"].astype(np.int64) * w.patches["rows"] * w.patches["wave_count"])
-    cuts = [0] + [int(np.searchsorted(cum, cum[-1] * (g + 1) / E2E_GROUPS)) + 1 for g in range(E2E_GROUPS - 1)] + \
+    cuts = [0] + [int(np.searchsorted(cum, cum[-1] * (g + 1) / n_groups)) + 1 for g in range(n_groups - 1)] + \
         [len(w.patches)]
     groups = []
-    for g in range(E2E_GROUPS):
+    for g in range(n_groups):
         sub = w.patches[cuts[g]:cuts[g + 1]]
-        if len(sub) == 0:
+        if len(sub) == 0 or cuts[g] >= cuts[g + 1]:
             continue
         o0 = int(sub["out_offset"][0])
         o1 = int(sub["out_offset"][-1]) + int(sub["cols"][-1]) * int(sub["rows"][-1])
@@ -533,7 +657,7 @@ def run_ours(args):
         t = torch.tensor([e2e_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
-    e2e_value = terms * world / (e2e_ms * 1e-3)
+    e2e_value = job_terms / (e2e_ms * 1e-3)
 
     extras = {}
     if not args.no_extras and rank == 0:
@@ -590,19 +714,23 @@ def run_ours(args):
 
     cpu = None
     if rank == 0:
-        r, dt, rows, cterms = cpu_sample(w, args.cpu_seconds, os.cpu_count() or 1)
-        cpu = {"value": r, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": f"first {rows} rows of each of the {args.patches} patches ({cterms} terms, {dt:.1f} s); "
-                         "FP32 restatement of water-grid.vert, 5 evaluations/vertex"}
+        cw = CpuWorkload(w)
+        ncpu = os.cpu_count() or 1
+        r, dt, stride, cterms = cpu_sample(cw, args.cpu_seconds, ncpu)
+        cpu = {"value": r, "unit": UNIT, "cores": ncpu, "kind": "port",
+               "sample": f"{every_nth(stride)} of each of the {len(w.patches)} patches of the timed table "
+                         f"({cterms} terms, {dt:.1f} s); FP32 restatement of water-grid.vert, 5 evaluations/vertex",
+               "build": f"gcc {cw.flags}"}
         # beside it: the same restatement on one thread, and the analytic form
         # (one evaluation per vertex, Jacobian normals) on every core
         short = max(1.0, args.cpu_seconds / 4)
-        r1, _, rows1, _ = cpu_sample(w, short, 1)
-        ra, _, rowsa, _ = cpu_sample(w, short, os.cpu_count() or 1, analytic=True)
+        r1, _, stride1, _ = cpu_sample(cw, short, 1)
+        ra, _, stridea, _ = cpu_sample(cw, short, ncpu, analytic=True)
         cpu["single_thread_value"] = r1
         cpu["analytic_value"] = ra
-        cpu["analytic_note"] = (f"one evaluation per vertex, Jacobian normals, {os.cpu_count() or 1} threads, "
-                                f"first {rowsa} rows per patch; single thread: first {rows1} rows per patch")
+        cpu["analytic_note"] = (f"one evaluation per vertex, Jacobian normals, {ncpu} threads, {every_nth(stridea)} "
+                                f"per patch; single thread: {every_nth(stride1)} per patch")
+        del cw
 
     if rank == 0:
         clocks = clk.summary()
@@ -612,19 +740,20 @@ def run_ours(args):
         verts = int(np.sum(w.patches["cols"].astype(np.int64) * w.patches["rows"]))
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (SplitMix64 seed 2 + rank)",
-            "config": {"workload": w.name, "patches": args.patches, "vertices": verts, "terms_per_step": terms,
-                       "waves_per_patch": "8..64", "grid_side": "64..1024 log-uniform", "heightmap": "none" if args.no_heightmap else "512^2 noise",
-                       "outputs": "float4 displacement + float4 normal (e2e: packed vec3 world position + "
-                                  "normal, the reference's vertex-array layout)", "phase": "FP64-reduced",
-                       "l2": "256 MiB buffer zeroed between timed steps (outside the per-step events)",
-                       "parallelism": f"weak x{world} (each GPU its own 256 patches)",
-                       "tuning": tuning},
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "strong" if split else "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (SplitMix64 seed 2, shared by the ranks)" if split else
+                    "synthetic (SplitMix64 seed 2 + rank)",
+            "config": workload_config(args, full if split else w, world, split),
+            "tuning": tuning,
+            "outputs": "float4 displacement + float4 normal (e2e: packed vec3 world position + normal, the "
+                       "reference's vertex-array layout); phase FP64-reduced",
+            "l2": "256 MiB buffer zeroed between timed steps (outside the per-step events)",
             "roofline": {"bound": "fma+mufu", "achieved": achieved / 1e9,
                          "peak": min(peak_fma_terms, peak_mufu_terms) / 1e9,
                          "unit": "Gterms/s", "frac": achieved / min(peak_fma_terms, peak_mufu_terms),
-                         "traffic": traffic_from_profile(),
+                         "traffic": traffic_from_profile(tuning, verts),
                          "peak_source": "term roofline min(P_FMA/10, P_MUFU/2) (10 FMA + 2 sin/cos of algorithmic "
                                         "work per term), P_FMA and P_MUFU measured in this run by wt_measure_peaks",
                          "fma_leg_peak": peak_fma_terms / 1e9, "fma_leg_frac": achieved / peak_fma_terms,
@@ -635,7 +764,14 @@ def run_ours(args):
                                  "pipe is FMA issue: fma_leg_frac is its fraction of that leg"},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                    "ms_per_step": e2e_ms},
+                    "ms_per_step": e2e_ms, "stream_groups": len(groups),
+                    "link_d2h_gbs_measured": link["d2h_gbs"], "link_h2d_gbs_measured": link["h2d_gbs"],
+                    "link_bound_ms": 1e3 * (d2h / (link["d2h_gbs"] * 1e9) + h2d / (link["h2d_gbs"] * 1e9)),
+                    "copy_frac": d2h / (e2e_ms * 1e-3) / (link["d2h_gbs"] * 1e9),
+                    "note": "copy_frac: the copy-back bytes over the whole end-to-end step time, as a fraction of "
+                            "the host link's D2H bandwidth measured in this run (1 GiB device -> pinned host "
+                            "cudaMemcpyAsync, best of 5); link_bound_ms: the step's copies alone at those rates"},
+            "accuracy": accuracy,
             "gpu_launches": 3 * args.steps,
             "clocks": clocks,
             "wall_s_timed_region": t_wall,

@@ -165,12 +165,13 @@ void wto_displace_f64(const wt_patch* p, const wt_wave* waves, const wto_heightm
 }
 
 void wto_displace_f64_rows(const wt_patch* p, const wt_wave* waves, const wto_heightmap* hm,
-                           const uint32_t* rows, uint32_t n_rows, double* pos, double* disp, double* nrm) {
+                           const uint32_t* rows, uint32_t n_rows, double* pos, double* disp, double* nrm,
+                           double* edge) {
     for (uint32_t k = 0; k < n_rows; ++k)
         for (uint32_t col = 0; col < p->cols; ++col) {
             size_t v = (size_t)k * p->cols + col;
             vertex_f64(p, waves, hm, rows[k], col, pos ? pos + 3 * v : NULL, disp ? disp + 3 * v : NULL,
-                       nrm ? nrm + 3 * v : NULL, NULL);
+                       nrm ? nrm + 3 * v : NULL, edge ? edge + v : NULL);
         }
 }
 

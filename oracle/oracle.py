@@ -82,7 +82,7 @@ def lib():
         vp = C.c_void_p
         _lib.wto_displace_f64.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp, vp, vp, vp]
         _lib.wto_adjoint_f64.argtypes = [vp, vp, vp, vp, vp, vp]
-        _lib.wto_displace_f64_rows.argtypes = [vp, vp, vp, vp, C.c_uint32, vp, vp, vp]
+        _lib.wto_displace_f64_rows.argtypes = [vp, vp, vp, vp, C.c_uint32, vp, vp, vp, vp]
         _lib.wto_reference_vertex.argtypes = [C.POINTER(RefUniforms), C.c_uint32, C.c_uint32,
                                               C.POINTER(RefOutputs)]
         for f in (_lib.wto_cpu_reference, _lib.wto_cpu_analytic):
@@ -151,17 +151,64 @@ def displace_f64(patches, waves, texels=None, hm_params=None, rows=None):
     return pos, disp, nrm, edge
 
 
-def displace_f64_rows(patch, waves, rows, texels=None, hm_params=None):
-    """FP64 truth on selected rows of one patch: (disp, nrm), row k at k*cols."""
+def displace_f64_rows(patch, waves, rows, texels=None, hm_params=None, with_edge=False):
+    """FP64 truth on selected rows of one patch: (disp, nrm[, edge]), row k at
+    k*cols."""
     L = lib()
     rows = np.ascontiguousarray(rows, dtype=np.uint32)
     cols = int(patch["cols"])
     disp = np.zeros((len(rows) * cols, 3)); nrm = np.zeros((len(rows) * cols, 3))
+    edge = np.full(len(rows) * cols, np.inf)
     hm = make_hm(texels, hm_params.sample_scale, hm_params.disp_scale, hm_params.wrap) if texels is not None else None
     pp = np.array(patch).copy()
     L.wto_displace_f64_rows(_ptr(pp), _ptr(waves), C.byref(hm) if hm else None, _ptr(rows), len(rows), None,
-                            _ptr(disp), _ptr(nrm))
-    return disp, nrm
+                            _ptr(disp), _ptr(nrm), _ptr(edge))
+    return (disp, nrm, edge) if with_edge else (disp, nrm)
+
+
+def sampled_rows(n_rows: int, per_patch: int = 8) -> np.ndarray:
+    """The rows of a patch the sampled accuracy check visits: the first, the
+    last and per_patch - 2 spread evenly between them."""
+    return np.unique(np.round(np.linspace(0, n_rows - 1, min(per_patch, n_rows))).astype(np.uint32))
+
+
+def accuracy_sampled_rows(patches, waves, disp32, nrm32, texels=None, hm_params=None, per_patch=8,
+                          edge_texels=1e-3, threads=None):
+    """The path's error metric on sampled rows of EVERY patch of a table,
+    against the FP64 truth: displacement error max|d32 - d64| / max|d64| over
+    all checked vertices (and the worst single patch), RMS of |d32 - d64| over
+    max|d64|, and the largest normal angle (vertices whose heightmap sample
+    lies within edge_texels of a texel-cell boundary excluded: the bilinear
+    gradient jumps there).  disp32 / nrm32: (n_out, >=3) arrays of the GPU's
+    displacement and normal, patch p's vertex (row, col) at out_offset + row *
+    cols + col."""
+    from concurrent.futures import ThreadPoolExecutor
+    threads = threads or os.cpu_count() or 1
+
+    def one(p):
+        rows = sampled_rows(int(p["rows"]), per_patch)
+        d64, n64, edge = displace_f64_rows(p, waves, rows, texels, hm_params, with_edge=True)
+        cols = int(p["cols"])
+        idx = (int(p["out_offset"]) + rows.astype(np.int64)[:, None] * cols + np.arange(cols)[None, :]).ravel()
+        d = disp32[idx, :3].astype(np.float64)
+        n = nrm32[idx, :3].astype(np.float64)
+        err = np.abs(d - d64)
+        ok = edge > edge_texels
+        ang = np.degrees(np.arctan2(np.linalg.norm(np.cross(n[ok], n64[ok]), axis=1),
+                                    np.sum(n[ok] * n64[ok], axis=1)))
+        return (float(err.max()), float(np.abs(d64).max()), float(np.sum(err ** 2)), len(idx),
+                float(ang.max()) if ang.size else 0.0, len(rows), len(idx))
+
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        res = list(ex.map(one, list(patches)))
+    emax = max(r[0] for r in res)
+    dmax = max(r[1] for r in res)
+    return {"max_rel_err": emax / dmax,
+            "rms_rel_err": float(np.sqrt(sum(r[2] for r in res) / sum(r[3] for r in res))) / dmax,
+            "per_patch_max_rel_err": max(r[0] / r[1] for r in res if r[1] > 0),
+            "max_normal_deg": max(r[4] for r in res),
+            "patches_checked": len(res), "rows_checked": sum(r[5] for r in res),
+            "vertices_checked": sum(r[6] for r in res)}
 
 
 def adjoint_f64(patches, waves, gpos, gnrm=None, texels=None, hm_params=None):
@@ -373,6 +420,45 @@ def wave_to_reference(wave):
     w = np.array(wave).copy()
     lib().wto_wave_to_reference(_ptr(w), C.byref(r))
     return (r.amplitude_A, r.frequency_w, r.phaseConstant_phi, r.steepness_Q_i, r.dir_x, r.dir_z)
+
+
+_timed = None
+
+
+def timed_lib():
+    """The timed CPU baseline: reference_mode.c built for speed
+    (build.TIMED_CFLAGS), separate from the bit-exact oracle build."""
+    global _timed
+    if _timed is None:
+        path = _build.build_timed()
+        _timed = C.CDLL(str(path))
+        vp = C.c_void_p
+        _timed.wto_cpu_reference_rows.argtypes = [vp, C.c_uint32, vp, vp, C.c_uint32, C.c_uint32, C.c_int, vp, vp,
+                                                  C.c_int]
+        _timed.wto_cpu_reference_rows.restype = C.c_uint64
+    return _timed
+
+
+def cpu_baseline_rows(patches, waves, texels=None, hm_params=None, row_stride=1, row_phase=0, threads=None,
+                      analytic=False, out=None):
+    """The timed CPU restatement over rows row_phase + k * row_stride of every
+    patch; returns (vertices, terms).  out: optional (pos4, nrm4) float32
+    arrays to write into (allocated when None)."""
+    threads = threads or os.cpu_count() or 1
+    if out is None:
+        n_out = int(max(int(p["out_offset"]) + int(p["cols"]) * int(p["rows"]) for p in patches))
+        out = (np.zeros((n_out, 4), np.float32), np.zeros((n_out, 4), np.float32))
+    hm = make_hm(texels, hm_params.sample_scale, hm_params.disp_scale, hm_params.wrap) if texels is not None else None
+    pp = np.ascontiguousarray(patches)
+    nv = timed_lib().wto_cpu_reference_rows(_ptr(pp), len(pp), _ptr(waves), C.byref(hm) if hm else None,
+                                            row_stride, row_phase, threads, _ptr(out[0]), _ptr(out[1]),
+                                            1 if analytic else 0)
+    terms = 0
+    for p in patches:
+        r = int(p["rows"])
+        n_rows = (r - row_phase + row_stride - 1) // row_stride if r > row_phase else 0
+        terms += n_rows * int(p["cols"]) * int(p["wave_count"])
+    return int(nv), terms
 
 
 def cpu_baseline(patches, waves, texels=None, hm_params=None, row_limit=1 << 30, threads=None,

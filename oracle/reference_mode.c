@@ -184,6 +184,7 @@ typedef struct job {
     const wt_wave* waves;
     const wto_heightmap* hm;
     uint32_t row_limit;
+    uint32_t row_stride, row_phase;  /* rows r = row_phase + k * row_stride, r < row_limit */
     float* pos4;
     float* nrm4;
     int analytic;
@@ -303,7 +304,7 @@ static void* worker(void* arg) {
             uint32_t mid = (lo + hi) / 2;
             if (J->row_start[mid] <= r) lo = mid; else hi = mid;
         }
-        uint32_t row = (uint32_t)(r - J->row_start[lo]);
+        uint32_t row = J->row_phase + (uint32_t)(r - J->row_start[lo]) * J->row_stride;
         if (J->analytic) run_row_analytic(J, lo, row, rw, phase);
         else run_row_reference(J, lo, row, rw, phase);
         atomic_fetch_add(&J->verts, J->patches[lo].cols);
@@ -314,19 +315,20 @@ static void* worker(void* arg) {
 }
 
 static uint64_t run_jobs(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
-                         const wto_heightmap* hm, uint32_t row_limit, int threads,
-                         float* pos4, float* nrm4, int analytic) {
-    if (n_patches == 0) return 0;
+                         const wto_heightmap* hm, uint32_t row_limit, uint32_t row_stride, uint32_t row_phase,
+                         int threads, float* pos4, float* nrm4, int analytic) {
+    if (n_patches == 0 || row_stride == 0) return 0;
     job J;
     memset(&J, 0, sizeof(J));
     J.patches = patches; J.n_patches = n_patches; J.waves = waves; J.hm = hm;
     J.row_limit = row_limit; J.pos4 = pos4; J.nrm4 = nrm4; J.analytic = analytic;
+    J.row_stride = row_stride; J.row_phase = row_phase;
     J.row_start = (uint64_t*)malloc(sizeof(uint64_t) * (n_patches + 1));
     uint64_t acc = 0;
     for (uint32_t i = 0; i < n_patches; ++i) {
         J.row_start[i] = acc;
-        uint32_t r = patches[i].rows < row_limit ? patches[i].rows : row_limit;
-        acc += r;
+        uint32_t lim = patches[i].rows < row_limit ? patches[i].rows : row_limit;
+        acc += lim > row_phase ? (lim - row_phase + row_stride - 1) / row_stride : 0;
     }
     J.row_start[n_patches] = acc;
     J.total_rows = acc;
@@ -344,11 +346,18 @@ static uint64_t run_jobs(const wt_patch* patches, uint32_t n_patches, const wt_w
 uint64_t wto_cpu_reference(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
                            const wto_heightmap* hm, uint32_t row_limit, int threads,
                            float* pos4, float* nrm4) {
-    return run_jobs(patches, n_patches, waves, hm, row_limit, threads, pos4, nrm4, 0);
+    return run_jobs(patches, n_patches, waves, hm, row_limit, 1, 0, threads, pos4, nrm4, 0);
 }
 
 uint64_t wto_cpu_analytic(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
                           const wto_heightmap* hm, uint32_t row_limit, int threads,
                           float* pos4, float* nrm4) {
-    return run_jobs(patches, n_patches, waves, hm, row_limit, threads, pos4, nrm4, 1);
+    return run_jobs(patches, n_patches, waves, hm, row_limit, 1, 0, threads, pos4, nrm4, 1);
+}
+
+uint64_t wto_cpu_reference_rows(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
+                                const wto_heightmap* hm, uint32_t row_stride, uint32_t row_phase, int threads,
+                                float* pos4, float* nrm4, int analytic) {
+    return run_jobs(patches, n_patches, waves, hm, 0xffffffffu, row_stride, row_phase, threads, pos4, nrm4,
+                    analytic != 0);
 }

@@ -55,9 +55,10 @@ void wto_displace_f64(const wt_patch* p, const wt_wave* waves, const wto_heightm
                       double* pos, double* disp, double* nrm, double* edge);
 
 /* The same for an explicit list of rows, written compactly (row k of the
- * list at k*cols). */
+ * list at k*cols); any output may be NULL. */
 void wto_displace_f64_rows(const wt_patch* p, const wt_wave* waves, const wto_heightmap* hm,
-                           const uint32_t* rows, uint32_t n_rows, double* pos, double* disp, double* nrm);
+                           const uint32_t* rows, uint32_t n_rows, double* pos, double* disp, double* nrm,
+                           double* edge);
 
 /* Undisplaced grid position (x, z) of vertex (row, col), water-grid.vert:87-91
  * and :123-125 in FP64. */
@@ -118,7 +119,7 @@ void wto_reference_vertex(const wto_ref_uniforms* u, uint32_t id0, uint32_t id1,
 /* ---- CPU baseline (timed, multi-threaded) -------------------------------- */
 
 /* Runs the FP32 reference-mode vertex stage (5 surface evaluations per vertex,
- * finite-difference normals) over rows [row0, row1) of every patch, with
+ * finite-difference normals) over rows [0, row_limit) of every patch, with
  * `threads` POSIX threads, writing float4 positions and normals at the
  * patches' out_offset.  Returns the number of vertices processed. */
 uint64_t wto_cpu_reference(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
@@ -129,6 +130,13 @@ uint64_t wto_cpu_reference(const wt_patch* patches, uint32_t n_patches, const wt
 uint64_t wto_cpu_analytic(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
                           const wto_heightmap* hm, uint32_t row_limit, int threads,
                           float* pos4, float* nrm4);
+
+/* Either form over the rows r = row_phase + k * row_stride of every patch (a
+ * sample spread evenly over each patch; the row_stride phases together cover
+ * the whole table). */
+uint64_t wto_cpu_reference_rows(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
+                                const wto_heightmap* hm, uint32_t row_stride, uint32_t row_phase, int threads,
+                                float* pos4, float* nrm4, int analytic);
 
 /* Maps one wt_wave of a patch to the shader's uniforms: frequency_w =
  * 2*pi/lambda, phaseConstant_phi = speed * frequency_w (FP32). */

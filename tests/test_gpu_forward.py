@@ -219,3 +219,38 @@ def test_precision_stress_2048sq_128waves(wt, oracle, gpu, t):
     assert out["fp64_phase"][0] <= DISP_TOL
     if t >= 1e4:
         assert out["fp32_naive"][0] > 10 * out["fp64_phase"][0]
+
+
+@pytest.fixture
+def restore_tuning(wt):
+    yield
+    wt.check(wt.lib().wt_set_tuning(None))
+
+
+@pytest.mark.parametrize("shape", ["autotuned", (8, 16, 0), (4, 8, 0)])
+def test_benchmarked_table_every_patch_against_f64(wt, oracle, gpu, restore_tuning, shape):
+    """The exact table the benchmark times (256 uneven patches, seed 2, the
+    512^2 noise layer) through the GPU, and sampled rows of EVERY patch (the
+    first, the last and six between) against FP64: the metric's <= 1e-5
+    bound measured on the timed inputs, with the shape the autotuner picks
+    and with 8 and 4 vertices per lane (the recurrence's length)."""
+    import torch
+    from wave_tool_gb300 import workloads
+    w = workloads.config3(n_patches=256, seed=2)
+    hm = wt.heightmap_from(w.heightmap)
+    surf = wt.Surface(w.patches, w.waves, hm)
+    pos, nrm = surf.alloc_outputs(wt.WT_OUT_DISPLACEMENT)
+    if shape == "autotuned":
+        surf.autotune(pos, nrm, flags=wt.WT_OUT_DISPLACEMENT, reps=2)
+    else:
+        vpl, warps, epi = shape
+        wt.set_tuning(warps, 0, 32, vpl, epi)
+    surf.displace(pos, nrm, flags=wt.WT_OUT_DISPLACEMENT)
+    torch.cuda.synchronize()
+    assert surf.status()[0] == 0
+    acc = oracle.accuracy_sampled_rows(w.patches, w.waves, pos.cpu().numpy(), nrm.cpu().numpy(),
+                                       hm.texels.cpu().numpy(), w.heightmap)
+    assert acc["patches_checked"] == 256 and acc["rows_checked"] == 256 * 8
+    assert acc["max_rel_err"] <= DISP_TOL, acc
+    assert acc["per_patch_max_rel_err"] <= DISP_TOL, acc
+    assert acc["max_normal_deg"] < ANGLE_TOL_DEG, acc

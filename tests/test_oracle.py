@@ -312,3 +312,32 @@ def test_noise_animation_restatement(oracle):
     c = oracle.noise_f64(terms, 20, 12, rates=whole, time_s=1.0)
     d = oracle.noise_f64(terms, 20, 12)
     assert np.abs(c - d).max() < 1e-5
+
+
+def test_timed_cpu_baseline_matches_the_reference_mode_oracle(oracle):
+    """The timed CPU baseline (reference_mode.c built for speed, with
+    -ffast-math) computes what the bit-exact restatement computes: world
+    positions to 1e-5 of the coordinates' scale, FD normals to 0.5 degree
+    (central differences over 0.2 m amplify the FP32 rounding of kilometre
+    coordinates), on every third row of eight batched patches."""
+    import numpy as np
+    import types
+    from helpers import angle_deg
+    from wave_tool_gb300 import workloads
+    w = workloads.config3(n_patches=8, seed=2)
+    tex = oracle.noise_f64(w.heightmap.terms, w.heightmap.width, w.heightmap.height).astype(np.float32)
+    hmp = types.SimpleNamespace(sample_scale=w.heightmap.sample_scale, disp_scale=w.heightmap.disp_scale,
+                                wrap=w.heightmap.wrap)
+    nv, terms = oracle.cpu_baseline_rows(w.patches, w.waves, tex, hmp, row_stride=3, row_phase=1, threads=2)
+    n_out = w.n_vertices
+    out = (np.zeros((n_out, 4), np.float32), np.zeros((n_out, 4), np.float32))
+    oracle.cpu_baseline_rows(w.patches, w.waves, tex, hmp, row_stride=3, row_phase=1, threads=2, out=out)
+    _, pos_ref, nrm_ref = oracle.cpu_baseline(w.patches, w.waves, tex, hmp, threads=2)
+    rows = np.concatenate([int(p["out_offset"]) + (np.arange(1, int(p["rows"]), 3)[:, None] * int(p["cols"])
+                                                   + np.arange(int(p["cols"]))[None, :]).ravel()
+                           for p in w.patches])
+    assert nv == len(rows)
+    assert terms == sum(len(range(1, int(p["rows"]), 3)) * int(p["cols"]) * int(p["wave_count"]) for p in w.patches)
+    scale = float(np.abs(pos_ref[rows, :3]).max())
+    assert np.abs(out[0][rows, :3] - pos_ref[rows, :3]).max() <= 1e-5 * scale
+    assert angle_deg(out[1][rows, :3].astype(np.float64), nrm_ref[rows, :3].astype(np.float64)).max() < 0.5

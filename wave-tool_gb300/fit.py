@@ -36,24 +36,41 @@ def _torch():
 _GRAD_TO_WAVE = (0, 1, 6, 7, 3, 5, 4)
 
 
+def rank_sum(t, group=None):
+    """Sum of a tensor over the ranks of `group` in rank order (bitwise the
+    same on every rank); the tensor itself without a group.  Gloo groups
+    exchange through host memory."""
+    if group is None:
+        return t
+    import torch.distributed as dist
+    from .sharding import allreduce_grads_fixed_order
+    if dist.get_backend(group) == "gloo" and t.is_cuda:
+        return allreduce_grads_fixed_order(t.cpu(), group).to(t.device)
+    return allreduce_grads_fixed_order(t, group)
+
+
 class GerstnerFunction:
-    """apply(wave_fields, surface, flags) -> (pos, nrm); wave_fields is an
-    [n_waves, 8] float32 CUDA tensor in wt_wave field order."""
+    """apply(wave_fields, surface, flags, group=None) -> (pos, nrm);
+    wave_fields is an [n_waves, 8] float32 CUDA tensor in wt_wave field
+    order.  With a process group, each rank's surface holds its shard of the
+    patches and the backward sums the wave gradients (wt_wave_grad) over the
+    ranks in rank order, so every rank steps its optimiser with the same
+    gradient."""
 
     _fn = None
 
     @classmethod
-    def apply(cls, wave_fields, surface: Surface, flags: int = WT_OUT_DISPLACEMENT):
+    def apply(cls, wave_fields, surface: Surface, flags: int = WT_OUT_DISPLACEMENT, group=None):
         if cls._fn is None:
             torch = _torch()
 
             class _F(torch.autograd.Function):
                 @staticmethod
-                def forward(ctx, w, surf, fl):
+                def forward(ctx, w, surf, fl, grp):
                     surf.waves.copy_(w.detach().contiguous().view(torch.uint8).reshape(-1))
                     sums = torch.empty((surf.n_vertices, 8), dtype=torch.float32, device=w.device)
                     pos, nrm = surf.displace(flags=fl, sums=sums)
-                    ctx.surf, ctx.flags = surf, fl
+                    ctx.surf, ctx.flags, ctx.group = surf, fl, grp
                     ctx.save_for_backward(sums)
                     return pos, nrm
 
@@ -65,13 +82,14 @@ class GerstnerFunction:
                     (sums,) = ctx.saved_tensors
                     g = surf.adjoint(gpos, None if gnrm is None else gnrm.contiguous(),
                                      flags=ctx.flags & WT_LAYOUT_VEC3, sums=sums)
+                    g = rank_sum(g, ctx.group)
                     out = torch.zeros((surf.n_waves, 8), dtype=torch.float32, device=g.device)
                     for dst, src in enumerate(_GRAD_TO_WAVE):
                         out[:, dst] = g[:, src]
-                    return out, None, None
+                    return out, None, None, None
 
             cls._fn = _F
-        return cls._fn.apply(wave_fields, surface, flags)
+        return cls._fn.apply(wave_fields, surface, flags, group)
 
 
 def waves_to_fields(waves: np.ndarray, device="cuda"):
@@ -101,7 +119,7 @@ def window_r2(patches: np.ndarray, n_vertices: int) -> np.ndarray:
 
 def fit_waves(patches: np.ndarray, target_waves: np.ndarray, start_waves: np.ndarray, steps: int = 500,
               lr: float = 1e-2, normal_weight: float = 1.0, log_every: int = 0, phase_lr: float | None = None,
-              window_start: float | None = 2.5, window_steps: int | None = None):
+              window_start: float | None = 2.5, window_steps: int | None = None, group=None):
     """Adam on (log A, log lambda, angle, log Q, phase) of start_waves to match
     the heights (y displacement) and normals of target_waves.  Speed is kept.
 
@@ -113,15 +131,36 @@ def fit_waves(patches: np.ndarray, target_waves: np.ndarray, start_waves: np.nda
     half-diagonals over window_steps steps (default 70 % of the steps); the
     remaining steps use the plain loss.  None: the plain loss throughout.
 
+    With a torch.distributed process group (data parallel over patches; no
+    reference counterpart), each rank fits on its LPT shard of the patches
+    (sharding.shard_patches): the loss is the mean over every rank's vertices,
+    its normalisers and the wave gradients are summed over the ranks in rank
+    order, and the ranks step identical parameters.
+
     Returns a dict: loss_first / loss_last (the plain loss of the starting and
     the fitted waves), the training-loss history, timings and the fitted waves."""
     torch = _torch()
     dev = torch.device("cuda")
+    all_patches = patches
+    if group is not None:
+        import torch.distributed as dist
+        from .sharding import shard_patches
+        patches, _ = shard_patches(patches, dist.get_world_size(group), dist.get_rank(group))
     tgt = Surface(patches, target_waves)
     pos_t, nrm_t = tgt.displace(flags=WT_OUT_DISPLACEMENT)
     y_t = pos_t[:, 1].clone()
     n_t = nrm_t[:, :3].clone()
-    y_scale = float(y_t.var())
+    if group is None:
+        n_all = float(y_t.numel())
+        y_scale = float(y_t.var())
+    else:
+        # vertex count and (unbiased) variance of the target heights over
+        # every rank's vertices
+        yd = y_t.double()
+        mom = rank_sum(torch.stack([torch.tensor(float(y_t.numel()), dtype=torch.float64, device=dev), yd.sum(),
+                                    (yd * yd).sum()]), group)
+        n_all = float(mom[0])
+        y_scale = float((mom[2] - mom[1] * mom[1] / n_all) / max(n_all - 1.0, 1.0))
     surf = Surface(patches, start_waves)
     f0 = waves_to_fields(start_waves, dev)
     logA = torch.log(f0[:, 0].clamp_min(1e-12)).clone().requires_grad_(True)
@@ -135,7 +174,7 @@ def fit_waves(patches: np.ndarray, target_waves: np.ndarray, start_waves: np.nda
     if window_start is not None:
         r2 = torch.from_numpy(window_r2(patches, surf.n_vertices)).to(dev)
         half_diag = max(0.5 * math.hypot(float(p["tr"][0] - p["bl"][0]), float(p["tr"][1] - p["bl"][1]))
-                        for p in patches)
+                        for p in all_patches)
         sigma_end = max(2.8 * half_diag, window_start)
         wsteps = max(1, int(round(0.7 * steps)) if window_steps is None else window_steps)
 
@@ -146,8 +185,12 @@ def fit_waves(patches: np.ndarray, target_waves: np.ndarray, start_waves: np.nda
     def plain_loss():
         with torch.no_grad():
             pos, nrm = GerstnerFunction.apply(fields_now(), surf, WT_OUT_DISPLACEMENT)
-            ey = ((pos[:, 1] - y_t) ** 2).mean() / y_scale
-            return float(ey + normal_weight * ((nrm[:, :3] - n_t) ** 2).sum(1).mean())
+            if group is None:
+                ey = ((pos[:, 1] - y_t) ** 2).mean() / y_scale
+                return float(ey + normal_weight * ((nrm[:, :3] - n_t) ** 2).sum(1).mean())
+            e = ((pos[:, 1] - y_t) ** 2).double().sum() / y_scale + \
+                normal_weight * ((nrm[:, :3] - n_t) ** 2).double().sum()
+            return float(rank_sum(e.reshape(1), group)[0]) / n_all
 
     loss_first = plain_loss()
     hist = []
@@ -155,16 +198,24 @@ def fit_waves(patches: np.ndarray, target_waves: np.ndarray, start_waves: np.nda
     t0 = time.perf_counter()
     for it in range(steps):
         opt.zero_grad(set_to_none=True)
-        pos, nrm = GerstnerFunction.apply(fields_now(), surf, WT_OUT_DISPLACEMENT)
+        pos, nrm = GerstnerFunction.apply(fields_now(), surf, WT_OUT_DISPLACEMENT, group)
         ey = (pos[:, 1] - y_t) ** 2 / y_scale
         en = ((nrm[:, :3] - n_t) ** 2).sum(1)
         if window_start is not None and it < wsteps:
             sigma = window_start * (sigma_end / window_start) ** (it / wsteps)
             wgt = torch.exp(r2 * (-0.5 / (sigma * sigma)))
-            wgt = wgt / wgt.mean()
-            loss = (wgt * (ey + normal_weight * en)).mean()
-        else:
+            if group is None:
+                wgt = wgt / wgt.mean()
+                loss = (wgt * (ey + normal_weight * en)).mean()
+            else:
+                wsum = rank_sum(wgt.sum().detach().reshape(1), group)[0]
+                loss = (wgt * (ey + normal_weight * en)).sum() / wsum
+        elif group is None:
             loss = (ey + normal_weight * en).mean()
+        else:
+            # this rank's share of the mean over every rank's vertices; the
+            # backward sums the shares' wave gradients
+            loss = (ey + normal_weight * en).sum() / n_all
         loss.backward()
         opt.step()
         if log_every and it % log_every == 0:
@@ -197,4 +248,4 @@ def parameter_errors(fitted: np.ndarray, target: np.ndarray) -> dict:
     }
 
 
-__all__ = ["GerstnerFunction", "fit_waves", "waves_to_fields", "parameter_errors", "window_r2"]
+__all__ = ["GerstnerFunction", "fit_waves", "waves_to_fields", "parameter_errors", "window_r2", "rank_sum"]
