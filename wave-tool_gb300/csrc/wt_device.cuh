@@ -116,7 +116,17 @@ __device__ __forceinline__ int mirror_index(int m, int n) {
     return n - 1 - (a >= 0 ? a : -(1 + a));
 }
 
+// FAST: REPEAT with a power-of-two size, known at compile time (the wrap is
+// one mask, no mirror selects).
+template <bool FAST = false>
 __device__ __forceinline__ Footprint footprint(float x, int n, uint32_t mode, bool pow2) {
+    if (FAST) {
+        Footprint f;
+        f.w = x - floorf(x);
+        f.i0 = __float2int_rd(x) & (n - 1);
+        f.i1 = (f.i0 + 1) & (n - 1);
+        return f;
+    }
     const bool mir = mode == WT_WRAP_MIRRORED_REPEAT;
     const int P = mir ? 2 * n : n;
     Footprint f;
@@ -149,11 +159,12 @@ struct HmSample {
     float h, hx, hz, hxz;
 };
 
+template <bool FAST = false>
 __device__ __forceinline__ HmSample hm_sample(const HmDev& hm, const PatchAux& a, float xd, float zd, bool pow2) {
     const float ut = fmaf(a.su, xd, a.hu0);
     const float vt = fmaf(a.sv, zd, a.hv0);
     const int W = (int)hm.width, H = (int)hm.height;
-    const Footprint fu = footprint(ut, W, hm.wrap, pow2), fv = footprint(vt, H, hm.wrap, pow2);
+    const Footprint fu = footprint<FAST>(ut, W, hm.wrap, pow2), fv = footprint<FAST>(vt, H, hm.wrap, pow2);
     const float al = fu.w, be = fv.w;
     const float t00 = __ldg(hm.texels + fv.i0 * W + fu.i0), t10 = __ldg(hm.texels + fv.i0 * W + fu.i1);
     const float t01 = __ldg(hm.texels + fv.i1 * W + fu.i0), t11 = __ldg(hm.texels + fv.i1 * W + fu.i1);
@@ -182,8 +193,9 @@ enum FwdMode : int {
 };
 
 // Heightmap, bounce, normal, stores for one vertex.  su: the 36 floats of
-// wt_view in shared memory (kModeStage only).
-template <int MODE>
+// wt_view in shared memory (kModeStage only).  FAST: the heightmap wraps by
+// REPEAT and has power-of-two sides.
+template <int MODE, bool FAST = false>
 __device__ __forceinline__ void finish_vertex(const VertexSums& s, float xl, float zl, const PatchAux& a,
                                               const HmDev& hm, bool pow2, uint64_t vidx,
                                               float* __restrict__ pos, float* __restrict__ nrm,
@@ -197,7 +209,7 @@ __device__ __forceinline__ void finish_vertex(const VertexSums& s, float xl, flo
     float pz0 = -s.sxz, pz1 = s.jz, pz2 = 1.0f - s.szz;
     float dy = s.dy;
     if (hm.present) {
-        const HmSample g = hm_sample(hm, a, xl + s.dx, zl + s.dz, pow2);
+        const HmSample g = hm_sample<FAST>(hm, a, xl + s.dx, zl + s.dz, pow2);
         dy += g.h;
         px1 = fmaf(g.hx, px0, fmaf(g.hz, px2, px1));
         pz1 = fmaf(g.hx, pz0, fmaf(g.hz, pz2, pz1));

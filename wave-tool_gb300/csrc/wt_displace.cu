@@ -401,6 +401,9 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
     const uint32_t n = hdr->n_patches;
     const uint32_t total = hdr->total_tiles;
     const bool pow2 = hm.present && (hm.width & (hm.width - 1)) == 0 && (hm.height & (hm.height - 1)) == 0;
+    // the plain epilogue's mask-only texel wrap (the other modes keep one
+    // general copy of the epilogue: two would spill their extra outputs)
+    const bool fast = pow2 && hm.wrap == WT_WRAP_REPEAT;
 
     // The queue index of the next tile is fetched while the current one runs;
     // the tile's patch is searched forward from the previous tile's (tiles
@@ -426,7 +429,13 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
         const uint32_t cols = patches[p].cols;
         const uint32_t nwaves = patches[p].wave_count;
         const uint64_t out0 = patches[p].out_offset;
-        const PatchAux a = aux[p];
+        // the rest of the patch's constants are loaded after the wave loop
+        // (held across it they would take 15 registers), except for the
+        // saving forward, which spills less with them loaded here
+        constexpr bool kLateAux = MODE != kModeSave;
+        PatchAux a;
+        if (!kLateAux) a = aux[p];
+        const uint32_t pair_offset = kLateAux ? aux[p].pair_offset : a.pair_offset;
         const uint32_t tpr = tiles_per_row(cols, SMAX);
         const uint32_t row = lt / tpr;
         const uint32_t c0 = (lt - row * tpr) * 32u * SMAX;
@@ -442,11 +451,12 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
             const uint32_t nw = min(chunk, nwaves - w0);
             __syncwarp();
             if ((uint32_t)lane < nw) {
-                stage_wave(coef[a.pair_offset + w0 + lane], c0, row, wst + kStage * lane);
+                stage_wave(coef[pair_offset + w0 + lane], c0, row, wst + kStage * lane);
             }
             __syncwarp();
             wave_loop_dispatch<SMAX>(S, acc, wst, nw, lane);
         }
+        if (kLateAux) a = aux[p];
 
         // grid position along the row: x(col) = col * du * (e1 + v e3) + v e2
         const float v = (float)row * a.inv_rm1;
@@ -473,8 +483,12 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
                     const float zl = fmaf(32.0f * (float)j, gz, zb);
                     const float2 pr[4] = {make_float2(s0.x, s0.y), make_float2(s0.z, s0.w), make_float2(s1.x, s1.y),
                                           make_float2(s1.z, s1.w)};
-                    finish_vertex<MODE>(sums_of(pr), xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums, su,
-                                        so);
+                    if (MODE == kModePlain && fast)
+                        finish_vertex<MODE, true>(sums_of(pr), xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags,
+                                                  sums, su, so);
+                    else
+                        finish_vertex<MODE>(sums_of(pr), xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums,
+                                            su, so);
                 }
             }
         } else {
@@ -484,8 +498,12 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
                 if ((uint32_t)j < S && col < cols) {
                     const float xl = fmaf(32.0f * j, gx, xb);
                     const float zl = fmaf(32.0f * j, gz, zb);
-                    finish_vertex<MODE>(sums_of(acc[j]), xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums,
-                                        su, so);
+                    if (MODE == kModePlain && fast)
+                        finish_vertex<MODE, true>(sums_of(acc[j]), xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags,
+                                                  sums, su, so);
+                    else
+                        finish_vertex<MODE>(sums_of(acc[j]), xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums,
+                                            su, so);
                 }
             }
         }
