@@ -159,15 +159,30 @@ struct HmSample {
     float h, hx, hz, hxz;
 };
 
+// The four texels of a sample's footprint and its weights (the loads), and
+// the layer value and derivatives formed from them (hm_combine).
+struct HmTexels {
+    float t00, t10, t01, t11, al, be;
+};
+
 template <bool FAST = false>
-__device__ __forceinline__ HmSample hm_sample(const HmDev& hm, const PatchAux& a, float xd, float zd, bool pow2) {
+__device__ __forceinline__ HmTexels hm_fetch(const HmDev& hm, const PatchAux& a, float xd, float zd, bool pow2) {
     const float ut = fmaf(a.su, xd, a.hu0);
     const float vt = fmaf(a.sv, zd, a.hv0);
     const int W = (int)hm.width, H = (int)hm.height;
     const Footprint fu = footprint<FAST>(ut, W, hm.wrap, pow2), fv = footprint<FAST>(vt, H, hm.wrap, pow2);
-    const float al = fu.w, be = fv.w;
-    const float t00 = __ldg(hm.texels + fv.i0 * W + fu.i0), t10 = __ldg(hm.texels + fv.i0 * W + fu.i1);
-    const float t01 = __ldg(hm.texels + fv.i1 * W + fu.i0), t11 = __ldg(hm.texels + fv.i1 * W + fu.i1);
+    HmTexels T;
+    T.al = fu.w;
+    T.be = fv.w;
+    T.t00 = __ldg(hm.texels + fv.i0 * W + fu.i0);
+    T.t10 = __ldg(hm.texels + fv.i0 * W + fu.i1);
+    T.t01 = __ldg(hm.texels + fv.i1 * W + fu.i0);
+    T.t11 = __ldg(hm.texels + fv.i1 * W + fu.i1);
+    return T;
+}
+
+__device__ __forceinline__ HmSample hm_combine(const HmDev& hm, const PatchAux& a, const HmTexels& T) {
+    const float al = T.al, be = T.be, t00 = T.t00, t10 = T.t10, t01 = T.t01, t11 = T.t11;
     const float r0 = fmaf(al, t10 - t00, t00), r1 = fmaf(al, t11 - t01, t01);
     const float r = fmaf(be, r1 - r0, r0);
     const float dru = fmaf(be, (t11 - t01) - (t10 - t00), t10 - t00);
@@ -181,6 +196,11 @@ __device__ __forceinline__ HmSample hm_sample(const HmDev& hm, const PatchAux& a
     return o;
 }
 
+template <bool FAST = false>
+__device__ __forceinline__ HmSample hm_sample(const HmDev& hm, const PatchAux& a, float xd, float zd, bool pow2) {
+    return hm_combine(hm, a, hm_fetch<FAST>(hm, a, xd, zd, pow2));
+}
+
 struct VertexSums {
     float dx, dy, dz, jx, jz, sxx, sxz, szz;
 };
@@ -192,15 +212,15 @@ enum FwdMode : int {
     kModeStage = 2,  // also the vertex-stage outputs (pos and nrm optional; world positions)
 };
 
-// Heightmap, bounce, normal, stores for one vertex.  su: the 36 floats of
-// wt_view in shared memory (kModeStage only).  FAST: the heightmap wraps by
-// REPEAT and has power-of-two sides.
-template <int MODE, bool FAST = false>
-__device__ __forceinline__ void finish_vertex(const VertexSums& s, float xl, float zl, const PatchAux& a,
-                                              const HmDev& hm, bool pow2, uint64_t vidx,
-                                              float* __restrict__ pos, float* __restrict__ nrm,
-                                              uint32_t flags, float4* __restrict__ sums,
-                                              const float* __restrict__ su, const StageOut& so) {
+// Bounce, normal, stores for one vertex, its heightmap texels fetched
+// already (T; used when hm.present).  su: the 36 floats of wt_view in shared
+// memory (kModeStage only).
+template <int MODE>
+__device__ __forceinline__ void finish_vertex_t(const VertexSums& s, float xl, float zl, const PatchAux& a,
+                                                const HmDev& hm, const HmTexels& T, uint64_t vidx,
+                                                float* __restrict__ pos, float* __restrict__ nrm,
+                                                uint32_t flags, float4* __restrict__ sums,
+                                                const float* __restrict__ su, const StageOut& so) {
     if (MODE == kModeSave) {
         __stcs(sums + 2 * vidx, make_float4(s.dx, s.dy, s.dz, s.jx));
         __stcs(sums + 2 * vidx + 1, make_float4(s.jz, s.sxx, s.sxz, s.szz));
@@ -209,7 +229,7 @@ __device__ __forceinline__ void finish_vertex(const VertexSums& s, float xl, flo
     float pz0 = -s.sxz, pz1 = s.jz, pz2 = 1.0f - s.szz;
     float dy = s.dy;
     if (hm.present) {
-        const HmSample g = hm_sample<FAST>(hm, a, xl + s.dx, zl + s.dz, pow2);
+        const HmSample g = hm_combine(hm, a, T);
         dy += g.h;
         px1 = fmaf(g.hx, px0, fmaf(g.hz, px2, px1));
         pz1 = fmaf(g.hx, pz0, fmaf(g.hz, pz2, pz1));
@@ -245,6 +265,19 @@ __device__ __forceinline__ void finish_vertex(const VertexSums& s, float xl, flo
     }
     if (MODE == kModeStage)
         stage_vertex<false>(su, make_float3(ox, dy, oz), make_float3(n0 * inv, n1 * inv, n2 * inv), vidx, so);
+}
+
+// Heightmap, bounce, normal, stores for one vertex.  FAST: the heightmap
+// wraps by REPEAT and has power-of-two sides.
+template <int MODE, bool FAST = false>
+__device__ __forceinline__ void finish_vertex(const VertexSums& s, float xl, float zl, const PatchAux& a,
+                                              const HmDev& hm, bool pow2, uint64_t vidx,
+                                              float* __restrict__ pos, float* __restrict__ nrm,
+                                              uint32_t flags, float4* __restrict__ sums,
+                                              const float* __restrict__ su, const StageOut& so) {
+    HmTexels T{};
+    if (hm.present) T = hm_fetch<FAST>(hm, a, xl + s.dx, zl + s.dz, pow2);
+    finish_vertex_t<MODE>(s, xl, zl, a, hm, T, vidx, pos, nrm, flags, sums, su, so);
 }
 
 __device__ __forceinline__ uint32_t hi32_round(unsigned long long x) {

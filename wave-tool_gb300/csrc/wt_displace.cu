@@ -41,6 +41,7 @@ constexpr int kSortBins = 1024;         // wave counts >= 1023 share the last bi
 constexpr uint32_t kWaveMaskWords = 512;  // waves validated into a shared bitmask up to 16384
 constexpr uint32_t kRankSortMax = 64;
 
+
 __device__ __forceinline__ void flag_error(WsHeader* h, uint32_t code, uint32_t patch) {
     atomicCAS(&h->status, 0u, code);
     atomicMin(&h->bad_patch, patch);
@@ -492,18 +493,37 @@ k_forward(const wt_patch* __restrict__ patches, HmDev hm, float* __restrict__ po
                 }
             }
         } else {
+            // kB vertices at a time: their texel loads are all issued before
+            // the first of them is used (half the lane's vertices: 1.079 ->
+            // 1.059 ms on 256 uneven patches at 8 per lane, 4 and 1 measured
+            // the same; the saving and staging epilogues, with more outputs
+            // live, take one at a time: more would spill)
+            constexpr int kB = MODE == kModePlain ? SMAX / 2 : 1;
 #pragma unroll
-            for (int j = 0; j < SMAX; ++j) {
-                const uint32_t col = c0 + lane + 32 * j;
-                if ((uint32_t)j < S && col < cols) {
-                    const float xl = fmaf(32.0f * j, gx, xb);
-                    const float zl = fmaf(32.0f * j, gz, zb);
-                    if (MODE == kModePlain && fast)
-                        finish_vertex<MODE, true>(sums_of(acc[j]), xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags,
-                                                  sums, su, so);
-                    else
-                        finish_vertex<MODE>(sums_of(acc[j]), xl, zl, a, hm, pow2, rowbase + col, pos, nrm, flags, sums,
-                                            su, so);
+            for (int jb = 0; jb < SMAX; jb += kB) {
+                HmTexels T[kB];
+#pragma unroll
+                for (int u = 0; u < kB; ++u) {
+                    const int j = jb + u;
+                    const uint32_t col = c0 + lane + 32 * j;
+                    T[u] = HmTexels{};
+                    if ((uint32_t)j < S && col < cols && hm.present) {
+                        const float xd = fmaf(32.0f * j, gx, xb) + acc[j][0].x;
+                        const float zd = fmaf(32.0f * j, gz, zb) + acc[j][1].x;
+                        if (MODE == kModePlain && fast) T[u] = hm_fetch<true>(hm, a, xd, zd, pow2);
+                        else T[u] = hm_fetch<false>(hm, a, xd, zd, pow2);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kB; ++u) {
+                    const int j = jb + u;
+                    const uint32_t col = c0 + lane + 32 * j;
+                    if ((uint32_t)j < S && col < cols) {
+                        const float xl = fmaf(32.0f * j, gx, xb);
+                        const float zl = fmaf(32.0f * j, gz, zb);
+                        finish_vertex_t<MODE>(sums_of(acc[j]), xl, zl, a, hm, T[u], rowbase + col, pos, nrm, flags,
+                                              sums, su, so);
+                    }
                 }
             }
         }
