@@ -454,6 +454,17 @@ wt_status wt_water_raster(const float* clip, uint64_t n_vertices, const uint32_t
                           uint32_t width, uint32_t height, const float* scene_depth, uint64_t* fragments,
                           void* workspace, size_t workspace_bytes, wt_stream stream);
 
+/* wt_water_raster for the projected grid's own triangle list (the one
+ * wt_grid_indices writes for cols x rows vertices from base_vertex), without
+ * the index buffer: the same fragments bit for bit, the same triangle
+ * numbering.  One thread per grid cell reads the cell's four vertices once.
+ * n_vertices >= base_vertex + cols * rows; workspace as wt_water_raster.
+ * Replaces the same glDrawElements (src/render-engine.cpp:1120) for the
+ * grid mesh of src/program.cpp:686-717. */
+wt_status wt_water_raster_grid(const float* clip, uint64_t n_vertices, uint32_t cols, uint32_t rows,
+                               uint32_t base_vertex, uint32_t width, uint32_t height, const float* scene_depth,
+                               uint64_t* fragments, void* workspace, size_t workspace_bytes, wt_stream stream);
+
 /* Workspace of wt_water_raster: 16 bytes per vertex (each vertex's snapped
  * window coordinates, computed once for the triangles that share it). */
 wt_status wt_water_raster_workspace_size(uint64_t n_vertices, size_t* bytes);

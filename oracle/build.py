@@ -26,14 +26,16 @@ REF_FRAG_LIB = REF_OUT / "libwgfrag_ref.so"
 CFLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-std=c11", "-Wall"]
 # The timed CPU baseline: the same FP32 restatement of the shader
 # (reference_mode.c) built for speed, in a library of its own so that the
-# bit-exact oracle build above is untouched.  -ffast-math lets the compiler
-# contract, reorder and pick faster libm paths, as a GPU driver may for GLSL
-# (on 16 Neoverse-V2 cores: 388 M terms/s against 343 M with -O2
-# -ffp-contract=off and 328 M with plain -O3).  No -march=native: host code
-# must build on the x86_64 and the aarch64 machines alike (the default aarch64
-# target already has the NEON vector unit).
+# bit-exact oracle build above is untouched: -O3, multiply-adds fused, no
+# errno or trap handling in libm calls.  -ffast-math is not used: its
+# reassociation and reciprocal rules break the shader's float arithmetic on
+# vertex ids (mod(id, L) through floor(id / L) lands on the wrong column at
+# row starts; tests/test_oracle.py checks the build against the bit-exact
+# one).  No -march=native: host code must build on the x86_64 and the
+# aarch64 machines alike (the default aarch64 target already has the NEON
+# vector unit and fused multiply-add).
 TIMED_LIB = BUILD / "libcpu_timed.so"
-TIMED_CFLAGS = ["-O3", "-ffast-math", "-fPIC", "-std=c11", "-Wall"]
+TIMED_CFLAGS = ["-O3", "-ffp-contract=fast", "-fno-math-errno", "-fno-trapping-math", "-fPIC", "-std=c11", "-Wall"]
 
 
 def reference_dir() -> Path:

@@ -315,8 +315,8 @@ def test_noise_animation_restatement(oracle):
 
 
 def test_timed_cpu_baseline_matches_the_reference_mode_oracle(oracle):
-    """The timed CPU baseline (reference_mode.c built for speed, with
-    -ffast-math) computes what the bit-exact restatement computes: world
+    """The timed CPU baseline (reference_mode.c built for speed: -O3, fused
+    multiply-adds) computes what the bit-exact restatement computes: world
     positions to 1e-5 of the coordinates' scale, FD normals to 0.5 degree
     (central differences over 0.2 m amplify the FP32 rounding of kilometre
     coordinates), on every third row of eight batched patches."""
