@@ -285,12 +285,7 @@ def build_frame(wt, workloads):
     colour = torch.empty((VH, VW, 4), dtype=torch.float32, device="cuda")
     shading = wt.water_shading(sun_position=(0.6, 0.8, 0.0))
 
-    G = int(patch["cols"][0]), int(patch["rows"][0])
-
-    def raster():   # the grid's own triangle list, no index buffer read
-        wt.water_raster_grid(outs["clip"], G[0], G[1], VW, VH, fragments=frags, workspace=rws)
-
-    def raster_indexed():
+    def raster():
         wt.water_raster(outs["clip"], idx, VW, VH, fragments=frags, workspace=rws)
 
     def shade():
@@ -304,12 +299,11 @@ def build_frame(wt, workloads):
         else:
             surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD, stream=s)
             wt.vertex_stage(view_dev, pos, nrm, out=outs, stream=s)
-        wt.water_raster_grid(outs["clip"], G[0], G[1], VW, VH, fragments=frags, workspace=rws, stream=s)
+        wt.water_raster(outs["clip"], idx, VW, VH, fragments=frags, workspace=rws, stream=s)
         wt.water_shade(frags, outs["clip"], idx, outs, VW, VH, shading, sky, local_reflections=lrefl,
                        local_refractions=lrefr, colour=colour, stream=s)
 
-    return dict(frame=frame, raster=raster, raster_indexed=raster_indexed, shade=shade, n=n, waves=len(w.waves),
-                VW=VW, VH=VH, frags=frags,
+    return dict(frame=frame, raster=raster, shade=shade, n=n, waves=len(w.waves), VW=VW, VH=VH, frags=frags,
                 tuning=tuning,
                 projected_grid=lambda: wt.projected_grid_async(cam_dev, surf.patches, view_dev),
                 displace=lambda: surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD),
@@ -346,7 +340,6 @@ def frame_pipeline(wt, workloads, stream, flush):
     vms = _event_ms(F["vertex_stage"], 20, stream, flush)
     fsms = _event_ms(F["displace_stage"], 20, stream, flush)
     rms = _event_ms(raster, 20, stream, flush)
-    rims = _event_ms(F["raster_indexed"], 20, stream, flush)
     sms = _event_ms(shade, 20, stream, flush)
     # the noise layer animated per frame (64 terms over 512^2 texels): what a
     # frame adds when it resynthesises the heightmap at the frame time
@@ -372,8 +365,7 @@ def frame_pipeline(wt, workloads, stream, flush):
         hbm_peak, peak_src = 6800.0, "fallback 6.8 TB/s"
     return {"vertices": n, "terms": n * F["waves"], "viewport": [VW, VH], "water_pixels_frac": covered,
             "displace_tuning": F["tuning"],
-            "frame_graph_ms": fms, "frame_graph_unfused_ms": graph_ms[False], "raster_ms": rms,
-            "raster_indexed_ms": rims, "shade_ms": sms,
+            "frame_graph_ms": fms, "frame_graph_unfused_ms": graph_ms[False], "raster_ms": rms, "shade_ms": sms,
             "noise_512sq_64terms_animated_ms": nms,
             "displace_with_fused_stage_ms": fsms,
             "frames_per_s": 1e3 / fms, "projected_grid_kernel_ms": gms, "displace_ms": dms,

@@ -195,13 +195,22 @@ wt_status wt_gerstner_displace(const wt_patch* patches, uint32_t n_patches,
  *   - n_patches <= WT_NOALLOC_MAX_PATCHES and total_wave_slots (the sum of the
  *     patches' wave_count) <= WT_NOALLOC_MAX_WAVE_SLOTS, else
  *     WT_ERR_INVALID_ARG;
- *   - the first call on a device looks up the array's device address; make
- *     that first call before any stream capture;
+ *   - the first call on a device looks up the array's device address and
+ *     keeps it for the life of the process; make that first call before any
+ *     stream capture.  A cudaDeviceReset (or anything else that destroys the
+ *     device's primary context) reloads the library's device code and may
+ *     move the array: do not call this entry point on a device after
+ *     resetting it;
  *   - every call on a device shares the one array, so calls that overlap on
  *     the GPU (e.g. on two streams at once) race: order them on one stream;
  *   - the first kernel of each call resets the array's queue and status words,
- *     so no clearing is needed between calls; device-side validation results
- *     are not reported (use wt_gerstner_displace to see them). */
+ *     so no clearing is needed between calls;
+ *   - total_wave_slots is checked on the host; when the patches' real sum of
+ *     wave_count is larger than the array holds (about 17,000 slots), or a
+ *     patch fails the device-side validation, the call still returns WT_OK
+ *     and leaves the outputs of the whole table (or of the failing patch)
+ *     unwritten: this entry point cannot report device-side results (use
+ *     wt_gerstner_displace and wt_workspace_status to see them). */
 wt_status wt_gerstner_displace_noalloc(const wt_patch* patches, uint32_t n_patches,
                                        uint64_t total_wave_slots,
                                        const wt_wave* waves, uint32_t n_waves,
@@ -453,17 +462,6 @@ typedef struct wt_water_textures {
 wt_status wt_water_raster(const float* clip, uint64_t n_vertices, const uint32_t* indices, uint64_t n_triangles,
                           uint32_t width, uint32_t height, const float* scene_depth, uint64_t* fragments,
                           void* workspace, size_t workspace_bytes, wt_stream stream);
-
-/* wt_water_raster for the projected grid's own triangle list (the one
- * wt_grid_indices writes for cols x rows vertices from base_vertex), without
- * the index buffer: the same fragments bit for bit, the same triangle
- * numbering.  One thread per grid cell reads the cell's four vertices once.
- * n_vertices >= base_vertex + cols * rows; workspace as wt_water_raster.
- * Replaces the same glDrawElements (src/render-engine.cpp:1120) for the
- * grid mesh of src/program.cpp:686-717. */
-wt_status wt_water_raster_grid(const float* clip, uint64_t n_vertices, uint32_t cols, uint32_t rows,
-                               uint32_t base_vertex, uint32_t width, uint32_t height, const float* scene_depth,
-                               uint64_t* fragments, void* workspace, size_t workspace_bytes, wt_stream stream);
 
 /* Workspace of wt_water_raster: 16 bytes per vertex (each vertex's snapped
  * window coordinates, computed once for the triangles that share it). */

@@ -72,45 +72,6 @@ def test_raster_bit_exact(wt, oracle, gpu, cam_kw):
     print(f"vertices behind the near plane: {(c[:, 2] < -c[:, 3]).sum()} of {len(c)}")
 
 
-@pytest.mark.parametrize("cam_kw", CAMERAS)
-def test_grid_raster_equals_index_raster(wt, oracle, gpu, cam_kw):
-    """wt_water_raster_grid (the grid's triangles without the index buffer)
-    gives the index-buffer path's fragments bit for bit, and the oracle's,
-    with and without a scene depth; an odd, non-square grid placed after
-    other vertices (base_vertex) as well."""
-    import torch
-    cam = wt.camera(displaceable_amplitude=1.5, **cam_kw)
-    stage, idx = frame(wt, cam)
-    clip = stage["clip"]
-    rng = np.random.default_rng(6)
-    depth = torch.from_numpy(rng.uniform(0.99, 1.0, (H, W)).astype(np.float32)).cuda()
-    for sd in (None, depth):
-        a = wt.water_raster(clip, idx, W, H, scene_depth=sd)
-        b = wt.water_raster_grid(clip, 129, 129, W, H, scene_depth=sd)
-        torch.cuda.synchronize()
-        assert torch.equal(a, b)
-        want = oracle.water_raster(np_(clip), np_(idx).view(np.uint32), W, H, np_(sd))
-        assert np.array_equal(b.cpu().numpy().view(np.uint64).ravel(), want)
-    # a 37 x 53 grid starting at vertex 100 of the same clip array
-    cols, rows, base = 37, 53, 100
-    idx2 = wt.grid_indices(cols, rows, base)
-    a = wt.water_raster(clip, idx2, W, H)
-    b = wt.water_raster_grid(clip, cols, rows, W, H, base_vertex=base)
-    torch.cuda.synchronize()
-    assert torch.equal(a, b)
-
-
-def test_grid_raster_rejects_a_grid_beyond_the_vertices(wt, gpu):
-    import torch
-    clip = torch.zeros((100, 4), device="cuda")
-    with pytest.raises(wt.WtError):
-        wt.water_raster_grid(clip, 10, 11, W, H)          # 110 vertices > 100
-    with pytest.raises(wt.WtError):
-        wt.water_raster_grid(clip, 10, 10, W, H, base_vertex=1)
-    with pytest.raises(wt.WtError):
-        wt.water_raster_grid(clip, 1, 10, W, H)
-
-
 def test_raster_clipping_and_degenerate_triangles(wt, oracle, gpu):
     """A triangle soup with vertices behind the eye, far outside the guard
     band, degenerate and non-finite ones, and out-of-range indices."""

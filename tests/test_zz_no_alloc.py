@@ -37,17 +37,24 @@ def _noalloc(wt, surf, pos, nrm, flags, n_patches=None, slots=None):
 
 
 def _compare(ref_pos, ref_nrm, pos, nrm):
+    """The same launches on the same inputs: the same bits (the tolerances
+    of the other parity tests hold a fortiori)."""
+    import torch
     a = pos.cpu().numpy().astype(np.float64)
     b = ref_pos.cpu().numpy().astype(np.float64)
     assert rel_err(a[:, :3], b[:, :3]) <= DISP_TOL
     assert angle_deg(nrm.cpu().numpy()[:, :3].astype(np.float64),
                      ref_nrm.cpu().numpy()[:, :3].astype(np.float64)).max() < ANGLE_TOL_DEG
+    assert torch.equal(pos, ref_pos) and torch.equal(nrm, ref_nrm)
 
 
-def test_noalloc_matches_workspace_entry_point_on_consecutive_calls(wt, gpu):
+@pytest.mark.parametrize("flag_name", ["WT_OUT_DISPLACEMENT", "WT_LAYOUT_VEC3", "WT_PHASE_FP32_NAIVE"])
+def test_noalloc_matches_workspace_entry_point_on_consecutive_calls(wt, gpu, flag_name):
+    """Displacement in float4, world positions in the reference's packed
+    vec3 layout, and the FP32-naive phase (its own forward kernel)."""
     import torch
     from wave_tool_gb300 import workloads
-    flags = wt.WT_OUT_DISPLACEMENT
+    flags = getattr(wt, flag_name)
     cases = [workloads.config3(n_patches=16, seed=2), workloads.small_random(5, n_patches=7, side_range=(2, 200))]
     surfs = [wt.Surface(w.patches, w.waves, wt.heightmap_from(w.heightmap)) for w in cases]
     refs = []
@@ -74,3 +81,34 @@ def test_noalloc_rejects_sizes_beyond_its_limits(wt, gpu):
     assert b"1024" in wt.lib().wt_last_error()
     assert _noalloc(wt, s, pos, nrm, 0, slots=16385) == wt.abi.WT_ERR_INVALID_ARG
     assert b"16384" in wt.lib().wt_last_error()
+
+
+def test_noalloc_leaves_outputs_unwritten_when_the_wave_slots_overflow_its_scratch(wt, gpu):
+    """The host checks the wave-slot count the caller states; when the
+    patches' real count is larger than the scratch holds, the first kernel
+    refuses the whole table: the call returns WT_OK and writes nothing (as
+    documented in wt.h), and the next call with a fitting table runs."""
+    import torch
+    from wave_tool_gb300 import workloads
+    from wave_tool_gb300.abi import PATCH_DTYPE
+    base = workloads.small_random(8, n_patches=1, side_range=(2, 4), n_waves_range=(64, 64), heightmap=False)
+    waves = base.waves
+    n = 300   # 300 patches x 64 waves = 19200 slots > the scratch's 17k
+    p0 = base.patches[0]
+    pt = np.array([p0] * n, dtype=PATCH_DTYPE)
+    verts = int(p0["cols"]) * int(p0["rows"])
+    pt["out_offset"] = np.arange(n, dtype=np.uint64) * verts
+    pt["wave_offset"] = 0
+    pt["wave_count"] = 64
+    s = wt.Surface(pt, waves)
+    pos, nrm = s.alloc_outputs(0)
+    pos.fill_(float("nan"))
+    nrm.fill_(float("nan"))
+    assert _noalloc(wt, s, pos, nrm, 0, slots=16384) == 0  # understated: passes the host check
+    assert torch.isnan(pos).all() and torch.isnan(nrm).all()
+    small = wt.Surface(pt[:8], waves)
+    p2, n2 = small.alloc_outputs(0)
+    assert _noalloc(wt, small, p2, n2, 0) == 0
+    ref_p, ref_n = small.displace()
+    torch.cuda.synchronize()
+    assert torch.equal(p2, ref_p) and torch.equal(n2, ref_n)

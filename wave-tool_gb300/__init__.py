@@ -34,7 +34,7 @@ EXPORTED = [
     "wt_gerstner_adjoint", "wt_grid_indices", "wt_noise_synth", "wt_wave_from_reference",
     "wt_measure_peaks", "wt_set_tuning", "wt_get_tuning", "wt_autotune_displace",
     "wt_projected_grid", "wt_projected_grid_async", "wt_vertex_stage", "wt_heightmap_from_unorm8",
-    "wt_water_raster", "wt_water_raster_grid", "wt_water_raster_workspace_size", "wt_water_shade",
+    "wt_water_raster", "wt_water_raster_workspace_size", "wt_water_shade",
     "wt_gerstner_displace_saving", "wt_gerstner_adjoint_saved", "wt_gerstner_displace_stage",
     "wt_noise_workspace_size", "wt_noise_synth_animated",
 ]
@@ -134,7 +134,6 @@ def lib():
         L.wt_heightmap_from_unorm8.argtypes = [vp, u32, u32, u32, u64, u32, vp, vp]
         L.wt_water_raster.argtypes = [vp, u64, vp, u64, u32, u32, vp, vp, vp, sz, vp]
         L.wt_water_raster_workspace_size.argtypes = [u64, C.POINTER(sz)]
-        L.wt_water_raster_grid.argtypes = [vp, u64, u32, u32, u32, u32, u32, vp, vp, vp, sz, vp]
         L.wt_water_shade.argtypes = [vp, vp, u64, vp, u64, vp, vp, vp, vp, u32, u32, C.POINTER(CWaterShading),
                                      C.POINTER(CWaterTextures), vp, vp, vp]
         for name in EXPORTED:
@@ -499,21 +498,6 @@ def water_raster(clip, indices, width: int, height: int, scene_depth=None, fragm
     return fragments
 
 
-def water_raster_grid(clip, cols: int, rows: int, width: int, height: int, base_vertex: int = 0, scene_depth=None,
-                      fragments=None, workspace=None, stream=None):
-    """water_raster for the grid triangle list of grid_indices(cols, rows,
-    base_vertex), without reading an index buffer (same fragments)."""
-    torch = _torch()
-    if fragments is None:
-        fragments = torch.empty((height, width), dtype=torch.int64, device=clip.device)
-    if workspace is None:
-        workspace = empty_bytes(water_raster_workspace_bytes(clip.shape[0]), clip.device)
-    check(lib().wt_water_raster_grid(clip.data_ptr(), clip.shape[0], cols, rows, base_vertex, width, height,
-                                     _ptr(scene_depth), fragments.data_ptr(), workspace.data_ptr(), workspace.numel(),
-                                     stream_handle(stream)))
-    return fragments
-
-
 def water_shade(fragments, clip, indices, stage: dict, width: int, height: int, shading: CWaterShading, skybox,
                 scene_depth=None, local_reflections=None, local_refractions=None, colour=None, composite=None,
                 stream=None):
@@ -554,7 +538,7 @@ __all__ = [
     "NOISE_TERM_DTYPE", "WAVE_GRAD_DTYPE", "WT_OUT_WORLD", "WT_OUT_DISPLACEMENT", "WT_LAYOUT_FLOAT4",
     "WT_LAYOUT_VEC3", "WT_PHASE_FP64", "WT_PHASE_FP32_NAIVE", "WT_WRAP_REPEAT", "WT_WRAP_MIRRORED_REPEAT",
     "EXPORTED", "math", "CAMERA_DTYPE", "VIEW_DTYPE", "camera", "displaceable_amplitude", "projected_grid",
-    "projected_grid_async", "vertex_stage", "water_shading", "water_raster", "water_raster_grid",
+    "projected_grid_async", "vertex_stage", "water_shading", "water_raster",
     "water_raster_workspace_bytes", "water_shade",
     "WATER_SHADING_DEFAULTS",
 ]

@@ -14,6 +14,7 @@
 #include <mutex>
 #include <string>
 
+#include "wt_nvtx.h"
 #include "wt_internal.h"
 
 namespace {
@@ -223,6 +224,7 @@ wt_status wt_gerstner_displace(const wt_patch* patches, uint32_t n_patches, cons
                                uint32_t n_waves, const wt_heightmap* hm, float* pos_out, float* nrm_out,
                                uint64_t out_capacity, uint32_t flags, void* workspace, size_t workspace_bytes,
                                wt_stream stream) {
+    WT_NVTX_RANGE("wt_gerstner_displace");
     return run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags,
                         workspace, workspace_bytes, (cudaStream_t)stream, cfg_for(n_patches, n_waves));
 }
@@ -231,6 +233,7 @@ wt_status wt_gerstner_displace_saving(const wt_patch* patches, uint32_t n_patche
                                       uint32_t n_waves, const wt_heightmap* hm, float* pos_out, float* nrm_out,
                                       uint64_t out_capacity, uint32_t flags, float* sums_out, void* workspace,
                                       size_t workspace_bytes, wt_stream stream) {
+    WT_NVTX_RANGE("wt_gerstner_displace_saving");
     if (!sums_out || !aligned(sums_out, 16)) return fail(WT_ERR_INVALID_ARG, "sums_out NULL or not 16-byte aligned");
     if (flags & WT_PHASE_FP32_NAIVE)
         return fail(WT_ERR_UNSUPPORTED, "saving forward: the FP32-naive phase has no adjoint to save for");
@@ -245,6 +248,7 @@ wt_status wt_gerstner_displace_stage(const wt_patch* patches, uint32_t n_patches
                                      float* pos_out, float* nrm_out, uint64_t out_capacity, uint32_t flags,
                                      const wt_stage_outputs* outputs, void* workspace, size_t workspace_bytes,
                                      wt_stream stream) {
+    WT_NVTX_RANGE("wt_gerstner_displace_stage");
     if (!view || !aligned(view, 4)) return fail(WT_ERR_INVALID_ARG, "view NULL or not 4-byte aligned");
     if (!outputs) return fail(WT_ERR_INVALID_ARG, "outputs is NULL");
     if (flags & (WT_OUT_DISPLACEMENT | WT_PHASE_FP32_NAIVE))
@@ -266,6 +270,7 @@ wt_status wt_gerstner_displace_unbatched(const wt_patch* host_patches, const wt_
                                          const wt_heightmap* hm, float* pos_out, float* nrm_out,
                                          uint64_t out_capacity, uint32_t flags, void* workspace,
                                          size_t workspace_bytes, wt_stream stream) {
+    WT_NVTX_RANGE("wt_gerstner_displace_unbatched");
     if (n_patches > 0 && !host_patches) return fail(WT_ERR_INVALID_ARG, "host_patches is NULL");
     const wt::FwdConfig cfg = cfg_for(1, n_waves);
     for (uint32_t i = 0; i < n_patches; ++i) {
@@ -319,6 +324,7 @@ wt_status wt_gerstner_adjoint(const wt_patch* host_patches, const wt_patch* patc
                               const wt_wave* waves, uint32_t n_waves, const wt_heightmap* hm, const float* d_pos,
                               const float* d_nrm, uint64_t out_capacity, uint32_t flags, wt_wave_grad* grad_out,
                               void* workspace, size_t workspace_bytes, wt_stream stream) {
+    WT_NVTX_RANGE("wt_gerstner_adjoint");
     return run_adjoint(host_patches, patches, n_patches, waves, n_waves, hm, d_pos, d_nrm, out_capacity, flags,
                        nullptr, grad_out, workspace, workspace_bytes, stream);
 }
@@ -328,12 +334,14 @@ wt_status wt_gerstner_adjoint_saved(const wt_patch* host_patches, const wt_patch
                                     const float* d_pos, const float* d_nrm, uint64_t out_capacity, uint32_t flags,
                                     const float* sums, wt_wave_grad* grad_out, void* workspace,
                                     size_t workspace_bytes, wt_stream stream) {
+    WT_NVTX_RANGE("wt_gerstner_adjoint_saved");
     if (!sums || !aligned(sums, 16)) return fail(WT_ERR_INVALID_ARG, "sums NULL or not 16-byte aligned");
     return run_adjoint(host_patches, patches, n_patches, waves, n_waves, hm, d_pos, d_nrm, out_capacity, flags,
                        sums, grad_out, workspace, workspace_bytes, stream);
 }
 
 wt_status wt_grid_indices(uint32_t cols, uint32_t rows, uint32_t base_vertex, uint32_t* idx_out, wt_stream stream) {
+    WT_NVTX_RANGE("wt_grid_indices");
     if (cols < 2 || rows < 2) return fail(WT_ERR_INVALID_ARG, "grid %ux%u: need at least 2x2", cols, rows);
     if (!idx_out) return fail(WT_ERR_INVALID_ARG, "idx_out is NULL");
     if (!aligned(idx_out, 4)) return fail(WT_ERR_INVALID_ARG, "idx_out not 4-byte aligned");
@@ -355,6 +363,7 @@ wt_status wt_noise_workspace_size(uint32_t n_terms, uint32_t width, uint32_t hei
 wt_status wt_noise_synth_animated(const wt_noise_term* terms, uint32_t n_terms, const float* rates, double time_s,
                                   uint32_t width, uint32_t height, float* texels_out, void* workspace,
                                   size_t workspace_bytes, wt_stream stream) {
+    WT_NVTX_RANGE("wt_noise_synth_animated");
     if (width < 1 || height < 1 || width > 32768 || height > 32768)
         return fail(WT_ERR_INVALID_ARG, "noise size %ux%u outside [1, 32768]", width, height);
     if (n_terms > 0 && !terms) return fail(WT_ERR_INVALID_ARG, "terms is NULL");
@@ -374,6 +383,7 @@ wt_status wt_noise_synth_animated(const wt_noise_term* terms, uint32_t n_terms, 
 
 wt_status wt_noise_synth(const wt_noise_term* terms, uint32_t n_terms, uint32_t width, uint32_t height,
                          float* texels_out, void* workspace, size_t workspace_bytes, wt_stream stream) {
+    WT_NVTX_RANGE("wt_noise_synth");
     return wt_noise_synth_animated(terms, n_terms, nullptr, 0.0, width, height, texels_out, workspace,
                                    workspace_bytes, stream);
 }
@@ -381,6 +391,7 @@ wt_status wt_noise_synth(const wt_noise_term* terms, uint32_t n_terms, uint32_t 
 wt_status wt_heightmap_from_unorm8(const uint8_t* pixels, uint32_t width, uint32_t height, uint32_t channels,
                                    uint64_t row_stride_bytes, uint32_t flip_vertically, float* texels_out,
                                    wt_stream stream) {
+    WT_NVTX_RANGE("wt_heightmap_from_unorm8");
     if (width < 1 || height < 1 || width > 32768 || height > 32768)
         return fail(WT_ERR_INVALID_ARG, "image size %ux%u outside [1, 32768]", width, height);
     if (channels < 1 || channels > 4) return fail(WT_ERR_INVALID_ARG, "channels %u outside [1, 4]", channels);
@@ -461,6 +472,7 @@ wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches, cons
                                const wt_heightmap* hm, float* pos_out, float* nrm_out, uint64_t out_capacity,
                                uint32_t flags, void* workspace, size_t workspace_bytes, uint32_t reps,
                                wt_tuning* best, wt_stream stream) {
+    WT_NVTX_RANGE("wt_autotune_displace");
     if (reps == 0 || reps > 1000) return fail(WT_ERR_INVALID_ARG, "reps must be in [1, 1000]");
     cudaStream_t s = (cudaStream_t)stream;
     cudaEvent_t e0, e1;
@@ -521,6 +533,7 @@ wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches, cons
 
 wt_status wt_measure_peaks(void* scratch, size_t scratch_bytes, double* fma_per_s, double* sin_per_s,
                            wt_stream stream) {
+    WT_NVTX_RANGE("wt_measure_peaks");
     if (!scratch || !fma_per_s || !sin_per_s) return fail(WT_ERR_INVALID_ARG, "NULL argument");
     if (scratch_bytes < (4u << 20)) return fail(WT_ERR_NOMEM, "peak probes need 4 MiB of scratch");
     cudaError_t e = wt::measure_peaks(scratch, scratch_bytes, fma_per_s, sin_per_s, (cudaStream_t)stream);

@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 
+#include "wt_nvtx.h"
 #include "wt_internal.h"
 #include "wt_stage.cuh"
 
@@ -429,6 +430,7 @@ extern "C" wt_status wt_projected_grid(const wt_camera* camera, wt_patch* patch,
 
 extern "C" wt_status wt_projected_grid_async(const wt_camera* camera, wt_patch* patch, wt_view* view,
                                              wt_stream stream) {
+    WT_NVTX_RANGE("wt_projected_grid_async");
     if (!camera || !aligned(camera, 8)) return fail(WT_ERR_INVALID_ARG, "wt_projected_grid_async: camera NULL or misaligned");
     if (!patch || !aligned(patch, 8)) return fail(WT_ERR_INVALID_ARG, "wt_projected_grid_async: patch NULL or misaligned");
     if (!view || !aligned(view, 4)) return fail(WT_ERR_INVALID_ARG, "wt_projected_grid_async: view NULL or misaligned");
@@ -440,6 +442,7 @@ extern "C" wt_status wt_projected_grid_async(const wt_camera* camera, wt_patch* 
 extern "C" wt_status wt_vertex_stage(const wt_view* view, const float* pos, const float* nrm, uint64_t n_vertices,
                                      uint32_t flags, float* clip_out, float* ndc0_out, float* view_out,
                                      float* facing_out, float* nrm_yaw_out, wt_stream stream) {
+    WT_NVTX_RANGE("wt_vertex_stage");
     if (flags & ~(uint32_t)WT_LAYOUT_VEC3) return fail(WT_ERR_INVALID_ARG, "wt_vertex_stage: flags other than WT_LAYOUT_VEC3");
     const bool vec3 = (flags & WT_LAYOUT_VEC3) != 0;
     const size_t la = vec3 ? 4 : 16;

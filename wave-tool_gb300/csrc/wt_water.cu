@@ -28,13 +28,20 @@
 #include <cmath>
 #include <cstdio>
 
+#include "wt_nvtx.h"
 #include "wt_internal.h"
 
 namespace {
 
 constexpr float kSub = 256.0f;   // sub-pixel steps per pixel
 constexpr float kGuard = 64.0f;  // guard band, in NDC units
-constexpr int kSmallPixels = 16;
+#ifndef WT_SMALL_PIXELS
+#define WT_SMALL_PIXELS 16
+#endif
+constexpr int kSmallPixels = WT_SMALL_PIXELS;
+#ifndef WT_RASTER_MINB
+#define WT_RASTER_MINB 3
+#endif
 constexpr int64_t kSmallExtent = 1 << 13;  // sub-pixel steps (32 pixels)
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -283,68 +290,12 @@ __global__ void __launch_bounds__(256) k_water_clear(const float* __restrict__ s
     }
 }
 
-// One lane's triangle (window coordinates a, b, c of its vertices): covered
-// by the lane itself when its box is small; otherwise marked for the whole
-// warp (2: window triangle in w, 3: to be clipped first).
-__device__ __forceinline__ int raster_lane(const int4& a, const int4& b, const int4& c, uint64_t t, uint32_t W,
-                                           uint32_t H, unsigned long long* frag, WinTri& w) {
-    if (!(a.w & b.w & c.w)) return 3;
-    w.X[0] = a.x; w.Y[0] = a.y; w.Z[0] = __int_as_float(a.z);
-    w.X[1] = b.x; w.Y[1] = b.y; w.Z[1] = __int_as_float(b.z);
-    w.X[2] = c.x; w.Y[2] = c.y; w.Z[2] = __int_as_float(c.z);
-    Setup s;
-    if (!setup_tri(w, W, H, s)) return 0;
-    // box <= 16384^2 pixels: 32 bits hold its size
-    const int32_t npix = (s.px1 - s.px0 + 1) * (s.py1 - s.py0 + 1);
-    if (npix > kSmallPixels) return 2;
-    if (s.small) raster_small(s, (uint32_t)t, W, frag);
-    else raster_own(s, (uint32_t)t, W, frag);
-    return 0;
-}
-
-// The warp rasterises, one after another, the triangles its lanes marked.
-__device__ __forceinline__ void raster_marked(int kind, const WinTri& w, const uint32_t (&vi)[3], uint64_t t,
-                                              const float4* __restrict__ clip, uint32_t W, uint32_t H,
-                                              unsigned long long* frag, int lane) {
-    const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
-    unsigned coop = __ballot_sync(kFull, kind >= 2);
-    while (coop) {
-        const int src = __ffs(coop) - 1;
-        coop &= coop - 1;
-        const int k = __shfl_sync(kFull, kind, src);
-        const uint32_t tri = (uint32_t)__shfl_sync(kFull, (unsigned long long)t, src);
-        if (k == 2) {
-            const WinTri sw = shfl_tri(w, src);
-            Setup s;
-            if (setup_tri(sw, W, H, s)) raster_warp(s, tri, W, frag, lane);
-            continue;
-        }
-        CV4 poly[8];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            const float4 c = clip[__shfl_sync(kFull, vi[j], src)];
-            poly[j] = CV4{c.x, c.y, c.z, c.w};
-        }
-        const int n = clip_polygon(poly, 3);
-        bool bad = n < 3;
-        for (int j = 0; j < n; ++j) bad |= !(poly[j].w > 0.0f);
-        if (bad) continue;
-        for (int j = 1; j + 1 < n; ++j) {
-            WinTri sw;
-            to_window(poly[0], hw, hh, sw.X[0], sw.Y[0], sw.Z[0]);
-            to_window(poly[j], hw, hh, sw.X[1], sw.Y[1], sw.Z[1]);
-            to_window(poly[j + 1], hw, hh, sw.X[2], sw.Y[2], sw.Z[2]);
-            Setup s;
-            if (setup_tri(sw, W, H, s)) raster_warp(s, tri, W, frag, lane);
-        }
-    }
-}
-
-__global__ void __launch_bounds__(256, 3) k_water_raster(const float4* __restrict__ clip,
+__global__ void __launch_bounds__(256, WT_RASTER_MINB) k_water_raster(const float4* __restrict__ clip,
                                                          const int4* __restrict__ win, uint64_t n_vertices,
                                                          const uint32_t* __restrict__ idx, uint64_t n_tri,
                                                          uint32_t W, uint32_t H, unsigned long long* frag) {
     const int lane = threadIdx.x & 31;
+    const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); base < n_tri; base += stride) {
         const uint64_t t = base + lane;
@@ -355,49 +306,58 @@ __global__ void __launch_bounds__(256, 3) k_water_raster(const float4* __restric
             vi[0] = idx[3 * t];
             vi[1] = idx[3 * t + 1];
             vi[2] = idx[3 * t + 2];
-            if (vi[0] < n_vertices && vi[1] < n_vertices && vi[2] < n_vertices)
-                kind = raster_lane(win[vi[0]], win[vi[1]], win[vi[2]], t, W, H, frag, w);
+            if (vi[0] < n_vertices && vi[1] < n_vertices && vi[2] < n_vertices) {
+                const int4 a = win[vi[0]], b = win[vi[1]], c = win[vi[2]];
+                if (a.w & b.w & c.w) {
+                    w.X[0] = a.x; w.Y[0] = a.y; w.Z[0] = __int_as_float(a.z);
+                    w.X[1] = b.x; w.Y[1] = b.y; w.Z[1] = __int_as_float(b.z);
+                    w.X[2] = c.x; w.Y[2] = c.y; w.Z[2] = __int_as_float(c.z);
+                    Setup s;
+                    if (setup_tri(w, W, H, s)) {
+                        // box <= 16384^2 pixels: 32 bits hold its size
+                        const int32_t npix = (s.px1 - s.px0 + 1) * (s.py1 - s.py0 + 1);
+                        if (npix <= kSmallPixels) {
+                            if (s.small) raster_small(s, (uint32_t)t, W, frag);
+                            else raster_own(s, (uint32_t)t, W, frag);
+                        } else {
+                            kind = 2;
+                        }
+                    }
+                } else {
+                    kind = 3;
+                }
+            }
         }
-        raster_marked(kind, w, vi, t, clip, W, H, frag, lane);
-    }
-}
-
-// The same for the projected grid's own triangle list (wt_grid_indices),
-// without reading it: one lane per grid cell, whose four vertices are loaded
-// once (neighbouring lanes read neighbouring vertices of two rows) and whose
-// two triangles, 2 cell and 2 cell + 1, are those of the index buffer.
-__global__ void __launch_bounds__(256, 3) k_water_raster_grid(const float4* __restrict__ clip,
-                                                              const int4* __restrict__ win, uint32_t cols,
-                                                              uint32_t rows, uint32_t base_vertex, uint32_t W,
-                                                              uint32_t H, unsigned long long* frag) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t cm1 = cols - 1;
-    const uint64_t n_cells = (uint64_t)cm1 * (rows - 1);
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); base < n_cells; base += stride) {
-        const uint64_t cell = base + lane;
-        const bool valid = cell < n_cells;
-        uint32_t v00 = 0, v01 = 0, v10 = 0, v11 = 0;
-        int4 a00 = make_int4(0, 0, 0, 0), a01 = a00, a10 = a00, a11 = a00;
-        if (valid) {
-            const uint32_t r = (uint32_t)(cell / cm1), c = (uint32_t)(cell - (uint64_t)r * cm1);
-            v00 = base_vertex + r * cols + c;
-            v01 = v00 + 1;
-            v10 = v00 + cols;
-            v11 = v10 + 1;
-            a00 = win[v00];
-            a01 = win[v01];
-            a10 = win[v10];
-            a11 = win[v11];
-        }
-#pragma unroll 1
-        for (int k = 0; k < 2; ++k) {
-            // (r,c), (r+1,c+1), (r+1,c) then (r,c), (r,c+1), (r+1,c+1)
-            const uint64_t t = 2 * cell + k;
-            uint32_t vi[3] = {v00, k == 0 ? v11 : v01, k == 0 ? v10 : v11};
-            WinTri w;
-            const int kind = valid ? raster_lane(a00, k == 0 ? a11 : a01, k == 0 ? a10 : a11, t, W, H, frag, w) : 0;
-            raster_marked(kind, w, vi, t, clip, W, H, frag, lane);
+        unsigned coop = __ballot_sync(kFull, kind >= 2);
+        while (coop) {
+            const int src = __ffs(coop) - 1;
+            coop &= coop - 1;
+            const int k = __shfl_sync(kFull, kind, src);
+            const uint32_t tri = (uint32_t)__shfl_sync(kFull, (unsigned long long)t, src);
+            if (k == 2) {
+                const WinTri sw = shfl_tri(w, src);
+                Setup s;
+                if (setup_tri(sw, W, H, s)) raster_warp(s, tri, W, frag, lane);
+                continue;
+            }
+            CV4 poly[8];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const float4 c = clip[__shfl_sync(kFull, vi[j], src)];
+                poly[j] = CV4{c.x, c.y, c.z, c.w};
+            }
+            const int n = clip_polygon(poly, 3);
+            bool bad = n < 3;
+            for (int j = 0; j < n; ++j) bad |= !(poly[j].w > 0.0f);
+            if (bad) continue;
+            for (int j = 1; j + 1 < n; ++j) {
+                WinTri sw;
+                to_window(poly[0], hw, hh, sw.X[0], sw.Y[0], sw.Z[0]);
+                to_window(poly[j], hw, hh, sw.X[1], sw.Y[1], sw.Z[1]);
+                to_window(poly[j + 1], hw, hh, sw.X[2], sw.Y[2], sw.Z[2]);
+                Setup s;
+                if (setup_tri(sw, W, H, s)) raster_warp(s, tri, W, frag, lane);
+            }
         }
     }
 }
@@ -658,6 +618,7 @@ extern "C" wt_status wt_water_raster(const float* clip, uint64_t n_vertices, con
                                      uint64_t n_triangles, uint32_t width, uint32_t height, const float* scene_depth,
                                      uint64_t* fragments, void* workspace, size_t workspace_bytes,
                                      wt_stream stream) {
+    WT_NVTX_RANGE("wt_water_raster");
     if (!viewport_ok(width, height)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: viewport outside [1, 16384]^2");
     if (!fragments || !aligned(fragments, 8)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: fragments NULL or misaligned");
     if (scene_depth && !aligned(scene_depth, 4)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: scene_depth misaligned");
@@ -694,53 +655,12 @@ extern "C" wt_status wt_water_raster(const float* clip, uint64_t n_vertices, con
     return e == cudaSuccess ? WT_OK : cuda_fail(e, "wt_water_raster launch");
 }
 
-extern "C" wt_status wt_water_raster_grid(const float* clip, uint64_t n_vertices, uint32_t cols, uint32_t rows,
-                                          uint32_t base_vertex, uint32_t width, uint32_t height,
-                                          const float* scene_depth, uint64_t* fragments, void* workspace,
-                                          size_t workspace_bytes, wt_stream stream) {
-    if (!viewport_ok(width, height))
-        return fail(WT_ERR_INVALID_ARG, "wt_water_raster_grid: viewport outside [1, 16384]^2");
-    if (!fragments || !aligned(fragments, 8))
-        return fail(WT_ERR_INVALID_ARG, "wt_water_raster_grid: fragments NULL or misaligned");
-    if (scene_depth && !aligned(scene_depth, 4))
-        return fail(WT_ERR_INVALID_ARG, "wt_water_raster_grid: scene_depth misaligned");
-    if (cols < 2 || rows < 2) return fail(WT_ERR_INVALID_ARG, "wt_water_raster_grid: the grid needs 2 x 2 vertices");
-    if ((uint64_t)base_vertex + (uint64_t)cols * rows > n_vertices)
-        return fail(WT_ERR_INVALID_ARG, "wt_water_raster_grid: base_vertex + cols * rows > n_vertices");
-    const uint64_t n_tri = 2ull * (cols - 1) * (rows - 1);
-    if (n_tri > (1ull << 32) - 2) return fail(WT_ERR_INVALID_ARG, "wt_water_raster_grid: more than 2^32 - 2 triangles");
-    if (!clip || !aligned(clip, 16))
-        return fail(WT_ERR_INVALID_ARG, "wt_water_raster_grid: clip NULL or not 16-byte aligned");
-    if (!workspace || !aligned(workspace, 16))
-        return fail(WT_ERR_INVALID_ARG, "wt_water_raster_grid: workspace NULL or not 16-byte aligned");
-    if (workspace_bytes < 16 * (size_t)n_vertices)
-        return fail(WT_ERR_NOMEM, "wt_water_raster_grid: workspace below 16 bytes per vertex");
-    int sms = 0;
-    wt_status st = sms_of_device(&sms);
-    if (st != WT_OK) return st;
-    cudaStream_t s = (cudaStream_t)stream;
-    const uint64_t npx = (uint64_t)width * height;
-    k_water_clear<<<resident_grid(k_water_clear, g_occ_clear, sms, npx), 256, 0, s>>>(
-        scene_depth, npx, reinterpret_cast<unsigned long long*>(fragments));
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "wt_water_raster_grid clear launch");
-    k_water_vertices<<<resident_grid(k_water_vertices, g_occ_vertices, sms, n_vertices), 256, 0, s>>>(
-        reinterpret_cast<const float4*>(clip), n_vertices, width, height, static_cast<int4*>(workspace));
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "wt_water_raster_grid vertex launch");
-    const uint64_t cb = ((n_tri / 2) + 255) / 256;  // one cell per thread, as one triangle per thread above
-    k_water_raster_grid<<<(unsigned)cb, 256, 0, s>>>(reinterpret_cast<const float4*>(clip),
-                                                      static_cast<const int4*>(workspace), cols, rows, base_vertex,
-                                                      width, height, reinterpret_cast<unsigned long long*>(fragments));
-    e = cudaGetLastError();
-    return e == cudaSuccess ? WT_OK : cuda_fail(e, "wt_water_raster_grid launch");
-}
-
 extern "C" wt_status wt_water_shade(const uint64_t* fragments, const float* clip, uint64_t n_vertices,
                                     const uint32_t* indices, uint64_t n_triangles, const float* facing, const float* nrm_yaw, const float* view, const float* ndc0,
                                     uint32_t width, uint32_t height, const wt_water_shading* shading,
                                     const wt_water_textures* textures, float* colour_out, float* composite,
                                     wt_stream stream) {
+    WT_NVTX_RANGE("wt_water_shade");
     if (!viewport_ok(width, height)) return fail(WT_ERR_INVALID_ARG, "wt_water_shade: viewport outside [1, 16384]^2");
     if (!fragments || !aligned(fragments, 8)) return fail(WT_ERR_INVALID_ARG, "wt_water_shade: fragments NULL or misaligned");
     const float* v16[4] = {clip, facing, nrm_yaw, view};
