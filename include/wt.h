@@ -540,7 +540,10 @@ wt_status wt_get_tuning(wt_tuning* tuning);
 /* Times every candidate launch shape on the given (device-resident) workload
  * (CUDA events on `stream`, synchronising it; after 4 * reps warm-up
  * launches, each candidate's best of three batches of `reps` launches, over
- * two passes) and caches the fastest for the workload's shape bucket (the bit lengths of
+ * two passes; each timed launch follows a clear of pos_out and nrm_out, which
+ * evicts the previous launch's lines from L2 when the outputs outsize it,
+ * so the shapes are ranked as a launch with cold inputs finds them) and
+ * caches the fastest for the workload's shape bucket (the bit lengths of
  * n_patches and n_waves): later wt_gerstner_displace calls in that bucket use
  * it.  Returns it in *best (may be NULL).  Arguments as wt_gerstner_displace;
  * the outputs are overwritten. */
