@@ -83,3 +83,22 @@ def test_cuda_graph_replay_equals_eager(wt, gpu):
     ep, en = s2.displace()
     torch.cuda.synchronize()
     assert torch.equal(pos, ep) and torch.equal(nrm, en)
+
+
+def test_fit_resumes_from_a_checkpoint_bit_for_bit(wt, gpu, tmp_path):
+    """A fit stopped after 25 of 50 steps and resumed from its checkpoint
+    ends with the parameters and loss history of the same fit run straight
+    through (every kernel and the optimiser are deterministic)."""
+    from wave_tool_gb300 import fit, workloads
+    target, start = workloads.config4()
+    straight = fit.fit_waves(target.patches, target.waves, start, steps=50, lr=1e-2)
+    ck = str(tmp_path / "fit.ckpt")
+    first = fit.fit_waves(target.patches, target.waves, start, steps=50, lr=1e-2, checkpoint=ck,
+                          checkpoint_every=10, stop_after=25)
+    assert first["steps_done"] == 25 and first["resumed_from"] == 0
+    resumed = fit.fit_waves(target.patches, target.waves, start, steps=50, lr=1e-2, checkpoint=ck,
+                            checkpoint_every=10)
+    assert resumed["resumed_from"] == 25 and resumed["steps_done"] == 50
+    assert np.array_equal(resumed["fitted"].view(np.uint32), straight["fitted"].view(np.uint32))
+    assert resumed["history"] == straight["history"]
+    assert resumed["loss_last"] == straight["loss_last"]

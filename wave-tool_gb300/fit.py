@@ -119,7 +119,8 @@ def window_r2(patches: np.ndarray, n_vertices: int) -> np.ndarray:
 
 def fit_waves(patches: np.ndarray, target_waves: np.ndarray, start_waves: np.ndarray, steps: int = 500,
               lr: float = 1e-2, normal_weight: float = 1.0, log_every: int = 0, phase_lr: float | None = None,
-              window_start: float | None = 2.5, window_steps: int | None = None, group=None):
+              window_start: float | None = 2.5, window_steps: int | None = None, group=None,
+              checkpoint: str | None = None, checkpoint_every: int = 100, stop_after: int | None = None):
     """Adam on (log A, log lambda, angle, log Q, phase) of start_waves to match
     the heights (y displacement) and normals of target_waves.  Speed is kept.
 
@@ -136,6 +137,15 @@ def fit_waves(patches: np.ndarray, target_waves: np.ndarray, start_waves: np.nda
     (sharding.shard_patches): the loss is the mean over every rank's vertices,
     its normalisers and the wave gradients are summed over the ranks in rank
     order, and the ranks step identical parameters.
+
+    With `checkpoint` (a file path), the fit's state (step, parameters, Adam
+    state, loss history) is written there every `checkpoint_every` steps and
+    at the end (rank 0 writes; through a temporary file, so a crash leaves the
+    previous checkpoint whole), and a fit started with an existing checkpoint
+    resumes from it: the steps it had done are skipped and the rest follow
+    the same schedule, so a resumed fit ends with the same parameters, bit for
+    bit, as one run straight through.  No reference counterpart (the
+    reference saves only screenshots, src/program.cpp:505-511).
 
     Returns a dict: loss_first / loss_last (the plain loss of the starting and
     the fitted waves), the training-loss history, timings and the fitted waves."""
@@ -194,9 +204,41 @@ def fit_waves(patches: np.ndarray, target_waves: np.ndarray, start_waves: np.nda
 
     loss_first = plain_loss()
     hist = []
+    it0 = 0
+    params = [logA, logL, ang, logQ, ph]
+    if checkpoint is not None:
+        import os
+        if os.path.exists(checkpoint):
+            ck = torch.load(checkpoint, map_location=dev, weights_only=False)
+            if ck["steps"] != steps or ck["n_waves"] != len(start_waves):
+                raise ValueError(f"checkpoint {checkpoint} is of another fit ({ck['steps']} steps, "
+                                 f"{ck['n_waves']} waves)")
+            with torch.no_grad():
+                for t_, v in zip(params, ck["params"]):
+                    t_.copy_(v)
+            opt.load_state_dict(ck["opt"])
+            it0 = ck["step"]
+            hist = list(ck["history"])
+            loss_first = ck["loss_first"]
+
+    def save(step):
+        if checkpoint is None:
+            return
+        if group is not None:
+            import torch.distributed as dist
+            if dist.get_rank(group) != 0:
+                return
+        import os
+        tmp = checkpoint + ".tmp"
+        torch.save({"step": step, "steps": steps, "n_waves": len(start_waves),
+                    "params": [t_.detach().clone() for t_ in params], "opt": opt.state_dict(),
+                    "history": [(i, float(l)) for i, l in hist], "loss_first": loss_first}, tmp)
+        os.replace(tmp, checkpoint)
+
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for it in range(steps):
+    it_end = steps if stop_after is None else min(steps, it0 + stop_after)
+    for it in range(it0, it_end):
         opt.zero_grad(set_to_none=True)
         pos, nrm = GerstnerFunction.apply(fields_now(), surf, WT_OUT_DISPLACEMENT, group)
         ey = (pos[:, 1] - y_t) ** 2 / y_scale
@@ -222,6 +264,10 @@ def fit_waves(patches: np.ndarray, target_waves: np.ndarray, start_waves: np.nda
             hist.append((it, float(loss)))
         elif not log_every:
             hist.append((it, loss.detach()))
+        if checkpoint is not None and (it + 1) % checkpoint_every == 0:
+            save(it + 1)
+    if it_end == steps or it_end % checkpoint_every != 0:
+        save(it_end)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     hist = [(i, float(l)) for i, l in hist]
@@ -231,7 +277,8 @@ def fit_waves(patches: np.ndarray, target_waves: np.ndarray, start_waves: np.nda
         fields = fields_now().cpu().numpy()
     fitted.view(np.float32).reshape(-1, 8)[:] = fields
     return {"loss_first": loss_first, "loss_last": loss_last, "history": hist, "seconds": dt,
-            "ms_per_step": 1e3 * dt / steps, "fitted": fitted}
+            "ms_per_step": 1e3 * dt / max(it_end - it0, 1), "fitted": fitted, "resumed_from": it0,
+            "steps_done": it_end}
 
 
 def parameter_errors(fitted: np.ndarray, target: np.ndarray) -> dict:
