@@ -51,9 +51,13 @@ def parse_args():
     ap.add_argument("--patches", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
     ap.add_argument("--no-extras", action="store_true", help="skip the unbatched / single-patch side runs")
-    ap.add_argument("--mode", choices=["forward", "adjoint", "frame"], default="forward",
+    ap.add_argument("--mode", choices=["forward", "adjoint", "frame", "displace"], default="forward",
                     help="'adjoint' times only wt_gerstner_adjoint on 64 uneven patches, 'frame' only the "
-                         "camera-to-pixels water frame (for profiling)")
+                         "camera-to-pixels water frame, 'displace' only wt_gerstner_displace on --workload "
+                         "(for profiling)")
+    ap.add_argument("--workload", choices=["config2", "config3", "config5"], default="config3",
+                    help="with --mode displace: the 1024^2 patch, the batched table (--patches) or 2048^2 x 128 "
+                         "waves")
     ap.add_argument("--no-heightmap", action="store_true",
                     help="the batched workload without its noise layer (for instruction-mix comparisons)")
     ap.add_argument("--saved-sums", action="store_true",
@@ -807,6 +811,32 @@ def run_adjoint_only(args):
                       "terms_per_s": w.n_terms / (ms * 1e-3)}), flush=True)
 
 
+def run_displace_only(args):
+    """wt_gerstner_displace alone on one workload (warmup, then `steps`
+    timed calls, L2 flushed between them); prints one JSON line (not the
+    headline)."""
+    import torch
+    wt = __graft_entry__.load_package()
+    from wave_tool_gb300 import workloads
+    w = {"config2": workloads.config2, "config3": lambda: workloads.config3(n_patches=args.patches, seed=2),
+         "config5": lambda: workloads.config5(time_s=100.0)}[args.workload]()
+    surf = wt.Surface(w.patches, w.waves, wt.heightmap_from(w.heightmap))
+    pos, nrm = surf.alloc_outputs(wt.WT_OUT_DISPLACEMENT)
+    if args.tuning == "auto":
+        tuning = surf.autotune(pos, nrm, flags=wt.WT_OUT_DISPLACEMENT, reps=5)
+    else:
+        vals = [int(x) for x in args.tuning.split(",")] + [8, 1]
+        wt.set_tuning(vals[0], 0, vals[1], vals[2], vals[3])
+        tuning = wt.get_tuning()
+    for _ in range(args.warmup):
+        surf.displace(pos, nrm, flags=wt.WT_OUT_DISPLACEMENT)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ms = _event_ms(lambda: surf.displace(pos, nrm, flags=wt.WT_OUT_DISPLACEMENT), args.steps,
+                   torch.cuda.current_stream(), flush)
+    print(json.dumps({"mode": "displace", "workload": w.name, "terms": w.n_terms, "ms_per_step": ms,
+                      "terms_per_s": w.n_terms / (ms * 1e-3), "tuning": tuning}), flush=True)
+
+
 def run_frame_only(args):
     """The water frame (camera -> pixels at 1920 x 1080 over a 1024^2 grid,
     eager launches): warmup, then `steps` timed frames; prints one JSON line
@@ -829,6 +859,9 @@ def main():
         return
     if args.mode == "frame":
         run_frame_only(args)
+        return
+    if args.mode == "displace":
+        run_displace_only(args)
         return
     if args.impl == "reference":
         run_reference(args)
