@@ -285,7 +285,7 @@ def build_frame(wt, workloads):
     lrefr = torch.randint(0, 256, (VH, VW, 4), dtype=torch.uint8, device="cuda", generator=gen)
     idx = wt.grid_indices(int(patch["cols"][0]), int(patch["rows"][0]))
     frags = torch.empty((VH, VW), dtype=torch.int64, device="cuda")
-    rws = wt.empty_bytes(wt.water_raster_workspace_bytes(n))
+    rws = wt.empty_bytes(wt.water_raster_workspace_bytes(n, idx.numel() // 3))
     colour = torch.empty((VH, VW, 4), dtype=torch.float32, device="cuda")
     shading = wt.water_shading(sun_position=(0.6, 0.8, 0.0))
 

@@ -464,8 +464,11 @@ wt_status wt_water_raster(const float* clip, uint64_t n_vertices, const uint32_t
                           void* workspace, size_t workspace_bytes, wt_stream stream);
 
 /* Workspace of wt_water_raster: 16 bytes per vertex (each vertex's snapped
- * window coordinates, computed once for the triangles that share it). */
-wt_status wt_water_raster_workspace_size(uint64_t n_vertices, size_t* bytes);
+ * window coordinates, computed once for the triangles that share it), 16
+ * bytes, and 16 bytes per triangle (the queue of triangles with more than 128
+ * pixels in their box, or that need clipping, which a second pass rasterises
+ * with whole warps).  At most 2^40 vertices and 2^32 - 2 triangles. */
+wt_status wt_water_raster_workspace_size(uint64_t n_vertices, uint64_t n_triangles, size_t* bytes);
 
 /* Shades every water pixel of a visibility buffer with the arithmetic of
  * water-grid.frag:65-151: perspective-correct varyings (facing normal, yaw-only

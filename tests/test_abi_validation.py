@@ -29,7 +29,7 @@ def test_vertex_stage_rejects_bad_arguments(wt, L):
 
 def test_water_raster_rejects_bad_arguments(wt, L):
     E, N = wt.abi.WT_ERR_INVALID_ARG, wt.abi.WT_ERR_NOMEM
-    ok = (FAKE, 4, FAKE, 2, 64, 32, None, FAKE, FAKE, 64, None)
+    ok = (FAKE, 4, FAKE, 2, 64, 32, None, FAKE, FAKE, 16 * 4 + 16 + 16 * 2, None)
 
     def call(**kw):
         a = list(ok)
@@ -41,9 +41,10 @@ def test_water_raster_rejects_bad_arguments(wt, L):
     assert call(w=0) == E and call(h=16385) == E
     assert call(frags=None) == E and call(frags=ODD) == E
     assert call(clip=ODD) == E and call(idx=None) == E
-    assert call(ws=None) == E and call(wsb=63) == N
+    assert call(ws=None) == E and call(wsb=16 * 4 + 16 + 16 * 2 - 1) == N
     sz = C.c_size_t()
-    assert L.wt_water_raster_workspace_size(1000, C.byref(sz)) == 0 and sz.value == 16000
+    assert L.wt_water_raster_workspace_size(1000, 1800, C.byref(sz)) == 0 and sz.value == 16000 + 16 + 16 * 1800
+    assert L.wt_water_raster_workspace_size(1000, 1 << 32, C.byref(sz)) == E
 
 
 def test_water_shade_rejects_bad_arguments(wt, L):

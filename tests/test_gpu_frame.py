@@ -318,7 +318,7 @@ def test_camera_to_pixels_frame_graph(wt, gpu, fused):
             for k in ("clip", "ndc0", "view", "facing", "nrm_yaw")}
     idx = wt.grid_indices(97, 97)
     frags = torch.empty((VH, VW), dtype=torch.int64, device="cuda")
-    rws = wt.empty_bytes(wt.water_raster_workspace_bytes(n))
+    rws = wt.empty_bytes(wt.water_raster_workspace_bytes(n, idx.numel() // 3))
     colour = torch.empty((VH, VW, 4), dtype=torch.float32, device="cuda")
     gen = torch.Generator(device="cuda").manual_seed(5)
     sky = torch.randint(0, 256, (6, 8, 8, 4), dtype=torch.uint8, device="cuda", generator=gen)

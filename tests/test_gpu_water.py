@@ -98,6 +98,22 @@ def test_raster_clipping_and_degenerate_triangles(wt, oracle, gpu):
     assert np.mean((want & 0xffffffff) != 0) > 0.5
 
 
+def test_raster_reuses_its_workspace(wt, oracle, gpu):
+    """One workspace for consecutive frames of different meshes (A, B, A):
+    the queue of large and clipped triangles starts empty every call."""
+    import torch
+    meshes = []
+    for cam_kw, side in ((CAMERAS[1], 129), (CAMERAS[0], 65)):
+        stage, idx = frame(wt, wt.camera(displaceable_amplitude=1.5, **cam_kw), side=side)
+        meshes.append((stage["clip"], idx, oracle.water_raster(np_(stage["clip"]), np_(idx).view(np.uint32), W, H)))
+    ws = wt.empty_bytes(max(wt.water_raster_workspace_bytes(c.shape[0], i.numel() // 3) for c, i, _ in meshes))
+    for k in (0, 1, 0):
+        clip, idx, want = meshes[k]
+        got = wt.water_raster(clip, idx, W, H, workspace=ws)
+        torch.cuda.synchronize()
+        assert np.array_equal(got.cpu().numpy().view(np.uint64).ravel(), want)
+
+
 @pytest.mark.parametrize("cam_kw", CAMERAS[:2])
 def test_shade_against_oracle(wt, oracle, gpu, cam_kw):
     import torch

@@ -133,7 +133,7 @@ def lib():
         L.wt_vertex_stage.argtypes = [vp, vp, vp, u64, u32, vp, vp, vp, vp, vp, vp]
         L.wt_heightmap_from_unorm8.argtypes = [vp, u32, u32, u32, u64, u32, vp, vp]
         L.wt_water_raster.argtypes = [vp, u64, vp, u64, u32, u32, vp, vp, vp, sz, vp]
-        L.wt_water_raster_workspace_size.argtypes = [u64, C.POINTER(sz)]
+        L.wt_water_raster_workspace_size.argtypes = [u64, u64, C.POINTER(sz)]
         L.wt_water_shade.argtypes = [vp, vp, u64, vp, u64, vp, vp, vp, vp, u32, u32, C.POINTER(CWaterShading),
                                      C.POINTER(CWaterTextures), vp, vp, vp]
         for name in EXPORTED:
@@ -477,9 +477,9 @@ def water_shading(**kw) -> CWaterShading:
     return s
 
 
-def water_raster_workspace_bytes(n_vertices: int) -> int:
+def water_raster_workspace_bytes(n_vertices: int, n_triangles: int) -> int:
     out = C.c_size_t()
-    check(lib().wt_water_raster_workspace_size(n_vertices, C.byref(out)))
+    check(lib().wt_water_raster_workspace_size(n_vertices, n_triangles, C.byref(out)))
     return out.value
 
 
@@ -491,7 +491,7 @@ def water_raster(clip, indices, width: int, height: int, scene_depth=None, fragm
     if fragments is None:
         fragments = torch.empty((height, width), dtype=torch.int64, device=clip.device)
     if workspace is None:
-        workspace = empty_bytes(water_raster_workspace_bytes(clip.shape[0]), clip.device)
+        workspace = empty_bytes(water_raster_workspace_bytes(clip.shape[0], indices.numel() // 3), clip.device)
     check(lib().wt_water_raster(clip.data_ptr(), clip.shape[0], indices.data_ptr(), indices.numel() // 3, width,
                                 height, _ptr(scene_depth), fragments.data_ptr(), workspace.data_ptr(),
                                 workspace.numel(), stream_handle(stream)))

@@ -14,10 +14,11 @@
 // a 64-bit atomic minimum (no return value, so no round trip per fragment):
 // nearest fragment wins, ties go to the lower index, and the
 // result does not depend on launch order.  Triangles with more than
-// kSmallPixels pixels in their box, and triangles that reach behind the near
+// kOwnPixels pixels in their box, and triangles that reach behind the near
 // plane or past a guard band of 64 viewports (clipped in clip space first),
-// are rasterised by their whole warp, one after another, lanes striding over
-// the pixels.
+// go to a queue; a second pass (k_water_raster_deferred) spreads the queue
+// over every warp of a resident grid, each triangle rasterised by a whole
+// warp, lanes striding over the pixels.
 //
 // Shading (k_water_shade): one thread per pixel; perspective-correct
 // barycentrics from the triangle's three clip-space vertices (2D homogeneous
@@ -35,12 +36,16 @@ namespace {
 
 constexpr float kSub = 256.0f;   // sub-pixel steps per pixel
 constexpr float kGuard = 64.0f;  // guard band, in NDC units
-#ifndef WT_SMALL_PIXELS
-#define WT_SMALL_PIXELS 16
+// Triangles with at most kOwnPixels pixels in their box are rasterised by
+// their own thread in the first pass; 6 blocks of 256 threads a multiprocessor
+// (40 registers) hide its gather latency.  1080p frame of a 1024^2 grid:
+// 16 / 64 / 128 / 256 pixels -> 94 / 62 / 57 / 64 us for the whole call.
+#ifndef WT_OWN_PIXELS
+#define WT_OWN_PIXELS 128
 #endif
-constexpr int kSmallPixels = WT_SMALL_PIXELS;
+constexpr int kOwnPixels = WT_OWN_PIXELS;
 #ifndef WT_RASTER_MINB
-#define WT_RASTER_MINB 3
+#define WT_RASTER_MINB 6
 #endif
 constexpr int64_t kSmallExtent = 1 << 13;  // sub-pixel steps (32 pixels)
 constexpr unsigned kFull = 0xffffffffu;
@@ -251,93 +256,171 @@ __device__ __forceinline__ void raster_warp(const Setup& s, uint32_t tri, uint32
     }
 }
 
-__device__ __forceinline__ WinTri shfl_tri(const WinTri& w, int src) {
-    WinTri o;
+// One pass before the triangles: the visibility buffer cleared to the scene
+// depth (or 1, the far plane) with no triangle, the queue emptied, and the
+// per-vertex window coordinates, computed once for the ~6 triangles sharing a
+// vertex: (X, Y, depth bits, 1) for vertices inside the guard band, w = 0
+// otherwise (their triangles take the clipping path).
+__global__ void __launch_bounds__(256) k_water_prepare(const float* __restrict__ scene_depth, uint64_t npx,
+                                                       unsigned long long* __restrict__ frag,
+                                                       const float4* __restrict__ clip, uint64_t nv, uint32_t W,
+                                                       uint32_t H, int4* __restrict__ win,
+                                                       uint32_t* __restrict__ queue_count) {
+    // the first raster pass may be scheduled now; it waits for this grid's
+    // results before it reads them
+    cudaTriggerProgrammaticLaunchCompletion();
+    const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
+    if (queue_count && blockIdx.x == 0 && threadIdx.x == 0) *queue_count = 0;
+    const uint64_t n = npx > nv ? npx : nv;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (i < nv) {
+            const float4 c4 = clip[i];
+            const CV4 c{c4.x, c4.y, c4.z, c4.w};
+            int4 o = make_int4(0, 0, 0, 0);
+            if (inside_guard(c)) {
+                float z;
+                to_window(c, hw, hh, o.x, o.y, z);
+                o.z = __float_as_int(z);
+                o.w = 1;
+            }
+            win[i] = o;
+        }
+        if (i < npx) {
+            const float d = scene_depth ? scene_depth[i] : 1.0f;
+            frag[i] = (unsigned long long)__float_as_uint(d) << 32;
+        }
+    }
+}
+
+__device__ __forceinline__ Setup shfl_setup(const Setup& s, int src) {
+    Setup o;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        o.X[k] = __shfl_sync(kFull, w.X[k], src);
-        o.Y[k] = __shfl_sync(kFull, w.Y[k], src);
-        o.Z[k] = __shfl_sync(kFull, w.Z[k], src);
+        o.x[k] = __shfl_sync(kFull, s.x[k], src);
+        o.y[k] = __shfl_sync(kFull, s.y[k], src);
+        o.z[k] = __shfl_sync(kFull, s.z[k], src);
     }
+    o.area_f = __shfl_sync(kFull, s.area_f, src);
+    o.px0 = __shfl_sync(kFull, s.px0, src);
+    o.px1 = __shfl_sync(kFull, s.px1, src);
+    o.py0 = __shfl_sync(kFull, s.py0, src);
+    o.py1 = __shfl_sync(kFull, s.py1, src);
+    const int flags = __shfl_sync(kFull, s.incl | (s.small ? 8 : 0), src);
+    o.incl = flags & 7;
+    o.small = (flags & 8) != 0;
     return o;
 }
 
-// Per-vertex window coordinates, computed once for the ~6 triangles sharing a
-// vertex: (X, Y, depth bits, 1) for vertices inside the guard band, w = 0
-// otherwise (their triangles take the clipping path).
-__global__ void __launch_bounds__(256) k_water_vertices(const float4* __restrict__ clip, uint64_t n, uint32_t W,
-                                                        uint32_t H, int4* __restrict__ win) {
-    const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const float4 c4 = clip[i];
-        const CV4 c{c4.x, c4.y, c4.z, c4.w};
-        int4 o = make_int4(0, 0, 0, 0);
-        if (inside_guard(c)) {
-            float z;
-            to_window(c, hw, hh, o.x, o.y, z);
-            o.z = __float_as_int(z);
-            o.w = 1;
-        }
-        win[i] = o;
-    }
-}
-
-__global__ void __launch_bounds__(256) k_water_clear(const float* __restrict__ scene_depth, uint64_t n,
-                                                     unsigned long long* __restrict__ frag) {
-    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n; p += (uint64_t)gridDim.x * blockDim.x) {
-        const float d = scene_depth ? scene_depth[p] : 1.0f;
-        frag[p] = (unsigned long long)__float_as_uint(d) << 32;
-    }
-}
-
-__global__ void __launch_bounds__(256, WT_RASTER_MINB) k_water_raster(const float4* __restrict__ clip,
-                                                         const int4* __restrict__ win, uint64_t n_vertices,
-                                                         const uint32_t* __restrict__ idx, uint64_t n_tri,
-                                                         uint32_t W, uint32_t H, unsigned long long* frag) {
+// First pass: one thread per triangle (the grid covers them all).  Triangles
+// whose pixel box holds at most kOwnPixels pixels are rasterised by their
+// own thread; the others (larger boxes, and triangles that need clipping) are
+// appended to a queue for the second pass (the triangle and its three vertex
+// indices), with one atomic per warp.  Launched dependent on the preparing
+// pass: the index loads are issued before it waits for that pass's results.
+__global__ void __launch_bounds__(256, WT_RASTER_MINB) k_water_raster(const int4* __restrict__ win,
+                                                         uint64_t n_vertices, const uint32_t* __restrict__ idx,
+                                                         uint64_t n_tri, uint32_t W, uint32_t H,
+                                                         unsigned long long* frag, uint32_t* __restrict__ queue_count,
+                                                         uint4* __restrict__ queue) {
     const int lane = threadIdx.x & 31;
-    const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); base < n_tri; base += stride) {
-        const uint64_t t = base + lane;
-        int kind = 0;  // 0 nothing, 2 warp-rasterised window triangle, 3 clip first
-        uint32_t vi[3] = {0u, 0u, 0u};
-        WinTri w;
-        if (t < n_tri) {
-            vi[0] = idx[3 * t];
-            vi[1] = idx[3 * t + 1];
-            vi[2] = idx[3 * t + 2];
-            if (vi[0] < n_vertices && vi[1] < n_vertices && vi[2] < n_vertices) {
-                const int4 a = win[vi[0]], b = win[vi[1]], c = win[vi[2]];
-                if (a.w & b.w & c.w) {
-                    w.X[0] = a.x; w.Y[0] = a.y; w.Z[0] = __int_as_float(a.z);
-                    w.X[1] = b.x; w.Y[1] = b.y; w.Z[1] = __int_as_float(b.z);
-                    w.X[2] = c.x; w.Y[2] = c.y; w.Z[2] = __int_as_float(c.z);
-                    Setup s;
-                    if (setup_tri(w, W, H, s)) {
-                        // box <= 16384^2 pixels: 32 bits hold its size
-                        const int32_t npix = (s.px1 - s.px0 + 1) * (s.py1 - s.py0 + 1);
-                        if (npix <= kSmallPixels) {
-                            if (s.small) raster_small(s, (uint32_t)t, W, frag);
-                            else raster_own(s, (uint32_t)t, W, frag);
-                        } else {
-                            kind = 2;
-                        }
-                    }
-                } else {
-                    kind = 3;
+    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    bool defer = false, own = false;
+    Setup s;
+    uint32_t v0 = 0, v1 = 0, v2 = 0;
+    if (t < n_tri) {
+        v0 = idx[3 * t];
+        v1 = idx[3 * t + 1];
+        v2 = idx[3 * t + 2];
+    }
+    cudaGridDependencySynchronize();                // window coordinates, cleared buffer, empty queue
+    cudaTriggerProgrammaticLaunchCompletion();      // the second pass may be scheduled
+    if (t < n_tri) {
+        if (v0 < n_vertices && v1 < n_vertices && v2 < n_vertices) {
+            const int4 a = win[v0], b = win[v1], c = win[v2];
+            if (a.w & b.w & c.w) {
+                WinTri w;
+                w.X[0] = a.x; w.Y[0] = a.y; w.Z[0] = __int_as_float(a.z);
+                w.X[1] = b.x; w.Y[1] = b.y; w.Z[1] = __int_as_float(b.z);
+                w.X[2] = c.x; w.Y[2] = c.y; w.Z[2] = __int_as_float(c.z);
+                if (setup_tri(w, W, H, s)) {
+                    // box <= 16384^2 pixels: 32 bits hold its size
+                    const int32_t npix = (s.px1 - s.px0 + 1) * (s.py1 - s.py0 + 1);
+                    own = npix <= kOwnPixels;
+                    defer = !own;
                 }
+            } else {
+                defer = true;
             }
         }
-        unsigned coop = __ballot_sync(kFull, kind >= 2);
-        while (coop) {
-            const int src = __ffs(coop) - 1;
-            coop &= coop - 1;
+    }
+    const unsigned m = __ballot_sync(kFull, defer);
+    if (m) {
+        const int leader = __ffs(m) - 1;
+        uint32_t q0 = 0;
+        if (lane == leader) q0 = atomicAdd(queue_count, (uint32_t)__popc(m));
+        q0 = __shfl_sync(kFull, q0, leader);
+        // at most n_tri <= 2^32 - 2 entries: the queue holds them all
+        if (defer) queue[q0 + (uint32_t)__popc(m & ((1u << lane) - 1u))] = make_uint4((uint32_t)t, v0, v1, v2);
+    }
+    if (own) {
+        if (s.small) raster_small(s, (uint32_t)t, W, frag);
+        else raster_own(s, (uint32_t)t, W, frag);
+    }
+}
+
+// Second pass over the queue (launched dependent on the first, whose
+// completion it waits for): every warp of a resident grid takes `per`
+// consecutive entries a round (loads and triangle set-up in parallel, one
+// lane each), then rasterises them one after another with all 32 lanes
+// striding over the pixels; clipped triangles are cut into a fan first.
+// Spreading the queue over every warp keeps the near-camera rows, whose
+// triangles are the large ones and lie next to one another in the index
+// buffer, off a few warps.
+__global__ void __launch_bounds__(256) k_water_raster_deferred(const float4* __restrict__ clip,
+                                                               const int4* __restrict__ win,
+                                                               uint32_t W, uint32_t H, unsigned long long* frag,
+                                                               const uint32_t* __restrict__ queue_count,
+                                                               const uint4* __restrict__ queue) {
+    cudaGridDependencySynchronize();  // the first pass is complete: the queue and its count
+    const uint64_t n = *queue_count;
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    const uint64_t warp = blockIdx.x * (uint64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+    const uint64_t want = (n + warps - 1) / warps;
+    const uint32_t per = want < 1 ? 1u : (want > 32 ? 32u : (uint32_t)want);
+    const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
+    for (uint64_t e0 = warp * per; e0 < n; e0 += warps * per) {
+        const uint64_t e = e0 + lane;
+        int kind = 0;  // 0 nothing, 2 window triangle set up, 3 clip first
+        uint32_t t = 0;
+        uint32_t vi[3] = {0u, 0u, 0u};
+        Setup s;
+        if ((uint32_t)lane < per && e < n) {
+            // the first pass queued only triangles whose three indices are in range
+            const uint4 q = queue[e];
+            t = q.x;
+            vi[0] = q.y;
+            vi[1] = q.z;
+            vi[2] = q.w;
+            const int4 a = win[vi[0]], b = win[vi[1]], c = win[vi[2]];
+            if (a.w & b.w & c.w) {
+                WinTri w;
+                w.X[0] = a.x; w.Y[0] = a.y; w.Z[0] = __int_as_float(a.z);
+                w.X[1] = b.x; w.Y[1] = b.y; w.Z[1] = __int_as_float(b.z);
+                w.X[2] = c.x; w.Y[2] = c.y; w.Z[2] = __int_as_float(c.z);
+                if (setup_tri(w, W, H, s)) kind = 2;
+            } else {
+                kind = 3;
+            }
+        }
+        unsigned todo = __ballot_sync(kFull, kind != 0);
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
             const int k = __shfl_sync(kFull, kind, src);
-            const uint32_t tri = (uint32_t)__shfl_sync(kFull, (unsigned long long)t, src);
+            const uint32_t tri = __shfl_sync(kFull, t, src);
             if (k == 2) {
-                const WinTri sw = shfl_tri(w, src);
-                Setup s;
-                if (setup_tri(sw, W, H, s)) raster_warp(s, tri, W, frag, lane);
+                raster_warp(shfl_setup(s, src), tri, W, frag, lane);
                 continue;
             }
             CV4 poly[8];
@@ -346,17 +429,17 @@ __global__ void __launch_bounds__(256, WT_RASTER_MINB) k_water_raster(const floa
                 const float4 c = clip[__shfl_sync(kFull, vi[j], src)];
                 poly[j] = CV4{c.x, c.y, c.z, c.w};
             }
-            const int n = clip_polygon(poly, 3);
-            bool bad = n < 3;
-            for (int j = 0; j < n; ++j) bad |= !(poly[j].w > 0.0f);
+            const int nv = clip_polygon(poly, 3);
+            bool bad = nv < 3;
+            for (int j = 0; j < nv; ++j) bad |= !(poly[j].w > 0.0f);
             if (bad) continue;
-            for (int j = 1; j + 1 < n; ++j) {
+            for (int j = 1; j + 1 < nv; ++j) {
                 WinTri sw;
                 to_window(poly[0], hw, hh, sw.X[0], sw.Y[0], sw.Z[0]);
                 to_window(poly[j], hw, hh, sw.X[1], sw.Y[1], sw.Z[1]);
                 to_window(poly[j + 1], hw, hh, sw.X[2], sw.Y[2], sw.Z[2]);
-                Setup s;
-                if (setup_tri(sw, W, H, s)) raster_warp(s, tri, W, frag, lane);
+                Setup cs;
+                if (setup_tri(sw, W, H, cs)) raster_warp(cs, tri, W, frag, lane);
             }
         }
     }
@@ -596,7 +679,24 @@ unsigned resident_grid(K kernel, std::atomic<int> (&cache)[64], int sms, uint64_
     return (unsigned)(need < cap ? need : cap);
 }
 
-std::atomic<int> g_occ_clear[64], g_occ_vertices[64], g_occ_shade[64];
+std::atomic<int> g_occ_prepare[64], g_occ_deferred[64], g_occ_shade[64];
+
+// 256-thread launch that may begin before the previous kernel on the stream
+// has finished (programmatic dependent launch); the kernel waits for that
+// kernel's results (cudaGridDependencySynchronize) before it reads them.
+template <typename K, typename... Args>
+cudaError_t launch_dependent(K kernel, dim3 grid, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = grid;
+    lc.blockDim = dim3(256);
+    lc.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    return cudaLaunchKernelEx(&lc, kernel, args...);
+}
 
 wt_status sms_of_device(int* sms) {
     *sms = wt::sm_count();
@@ -608,9 +708,22 @@ bool viewport_ok(uint32_t w, uint32_t h) { return w >= 1 && h >= 1 && w <= 16384
 
 }  // namespace
 
-extern "C" wt_status wt_water_raster_workspace_size(uint64_t n_vertices, size_t* bytes) {
+// Workspace: the vertices' window coordinates (int4 each), the queue's
+// entry count (16 bytes, for alignment), then the queue (uint4 per triangle:
+// the triangle and its vertex indices).
+namespace {
+constexpr uint64_t kMaxRasterVertices = 1ull << 40;
+size_t raster_queue_offset(uint64_t n_vertices) { return 16 * (size_t)n_vertices; }
+size_t raster_workspace_bytes(uint64_t n_vertices, uint64_t n_triangles) {
+    return raster_queue_offset(n_vertices) + 16 + 16 * (size_t)n_triangles;
+}
+}  // namespace
+
+extern "C" wt_status wt_water_raster_workspace_size(uint64_t n_vertices, uint64_t n_triangles, size_t* bytes) {
     if (!bytes) return fail(WT_ERR_INVALID_ARG, "wt_water_raster_workspace_size: bytes is NULL");
-    *bytes = 16 * (size_t)(n_vertices > 0 ? n_vertices : 1);
+    if (n_vertices > kMaxRasterVertices || n_triangles > (1ull << 32) - 2)
+        return fail(WT_ERR_INVALID_ARG, "wt_water_raster_workspace_size: more than 2^40 vertices or 2^32 - 2 triangles");
+    *bytes = raster_workspace_bytes(n_vertices, n_triangles);
     return WT_OK;
 }
 
@@ -627,32 +740,38 @@ extern "C" wt_status wt_water_raster(const float* clip, uint64_t n_vertices, con
         if (!indices || !aligned(indices, 4)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: indices NULL or misaligned");
         if (n_triangles > (1ull << 32) - 2) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: more than 2^32 - 2 triangles");
         if (!workspace || !aligned(workspace, 16)) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: workspace NULL or not 16-byte aligned");
-        if (workspace_bytes < 16 * (size_t)n_vertices) return fail(WT_ERR_NOMEM, "wt_water_raster: workspace below 16 bytes per vertex");
+        if (n_vertices > kMaxRasterVertices) return fail(WT_ERR_INVALID_ARG, "wt_water_raster: more than 2^40 vertices");
+        if (workspace_bytes < raster_workspace_bytes(n_vertices, n_triangles))
+            return fail(WT_ERR_NOMEM, "wt_water_raster: workspace below wt_water_raster_workspace_size");
     }
     int sms = 0;
     wt_status st = sms_of_device(&sms);
     if (st != WT_OK) return st;
     cudaStream_t s = (cudaStream_t)stream;
     const uint64_t npx = (uint64_t)width * height;
-    k_water_clear<<<resident_grid(k_water_clear, g_occ_clear, sms, npx), 256, 0, s>>>(
-        scene_depth, npx, reinterpret_cast<unsigned long long*>(fragments));
+    const bool tris = n_triangles > 0 && n_vertices > 0;
+    const uint64_t nv = tris ? n_vertices : 0;
+    int4* win = static_cast<int4*>(workspace);
+    uint32_t* queue_count =
+        tris ? reinterpret_cast<uint32_t*>(static_cast<char*>(workspace) + raster_queue_offset(n_vertices)) : nullptr;
+    uint4* queue = tris ? reinterpret_cast<uint4*>(queue_count + 4) : nullptr;
+    unsigned long long* frag = reinterpret_cast<unsigned long long*>(fragments);
+    k_water_prepare<<<resident_grid(k_water_prepare, g_occ_prepare, sms, npx > nv ? npx : nv), 256, 0, s>>>(
+        scene_depth, npx, frag, reinterpret_cast<const float4*>(clip), nv, width, height, win, queue_count);
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "wt_water_raster clear launch");
-    if (n_triangles == 0 || n_vertices == 0) return WT_OK;
-    k_water_vertices<<<resident_grid(k_water_vertices, g_occ_vertices, sms, n_vertices), 256, 0, s>>>(
-        reinterpret_cast<const float4*>(clip), n_vertices, width, height, static_cast<int4*>(workspace));
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "wt_water_raster vertex launch");
-    // triangles cost from nothing to a warp's worth of pixels each: one
-    // triangle per thread (at most 2^24 blocks) lets the block scheduler even
-    // that out (1080p frame: 88 us, against 97 us at 8 blocks per SM and 124
-    // us at the resident count)
+    if (e != cudaSuccess) return cuda_fail(e, "wt_water_raster prepare launch");
+    if (!tris) return WT_OK;
+    // one thread per triangle (at most 2^24 blocks): most cost almost nothing
     const uint64_t rb = (n_triangles + 255) / 256;
-    k_water_raster<<<(unsigned)rb, 256, 0, s>>>(
-        reinterpret_cast<const float4*>(clip), static_cast<const int4*>(workspace), n_vertices, indices,
-        n_triangles, width, height, reinterpret_cast<unsigned long long*>(fragments));
-    e = cudaGetLastError();
-    return e == cudaSuccess ? WT_OK : cuda_fail(e, "wt_water_raster launch");
+    e = launch_dependent(k_water_raster, dim3((unsigned)rb), s, static_cast<const int4*>(win), n_vertices, indices,
+                         n_triangles, width, height, frag, queue_count, queue);
+    if (e != cudaSuccess) return cuda_fail(e, "wt_water_raster launch");
+    // the queue: a resident grid, at most one warp per triangle
+    e = launch_dependent(k_water_raster_deferred,
+                         dim3(resident_grid(k_water_raster_deferred, g_occ_deferred, sms, 32 * n_triangles)), s,
+                         reinterpret_cast<const float4*>(clip), static_cast<const int4*>(win), width, height, frag,
+                         static_cast<const uint32_t*>(queue_count), static_cast<const uint4*>(queue));
+    return e == cudaSuccess ? WT_OK : cuda_fail(e, "wt_water_raster deferred launch");
 }
 
 extern "C" wt_status wt_water_shade(const uint64_t* fragments, const float* clip, uint64_t n_vertices,
