@@ -186,14 +186,20 @@ __device__ __forceinline__ void raster_small(const Setup& s, uint32_t tri, uint3
         dx[k] = -ey * 256;
         dy[k] = ex * 256;
     }
+    // inside edge k: e_k > 0, or e_k == 0 where the edge owns its centres,
+    // i.e. e_k - 1 + incl_k >= 0: all three at once by the sign of an OR
+    int32_t b[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        b[k] = ((s.incl >> k) & 1) - 1;
+        e0[k] += b[k];
+    }
     for (int32_t py = s.py0; py <= s.py1; ++py) {
         int32_t e[3] = {e0[0], e0[1], e0[2]};
         for (int32_t px = s.px0; px <= s.px1; ++px) {
-            bool in = true;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) in &= e[k] > 0 || (e[k] == 0 && ((s.incl >> k) & 1));
-            if (in) {
-                float d = ((float)e[0] * s.z[0] + (float)e[1] * s.z[1] + (float)e[2] * s.z[2]) / s.area_f;
+            if ((e[0] | e[1] | e[2]) >= 0) {
+                float d = ((float)(e[0] - b[0]) * s.z[0] + (float)(e[1] - b[1]) * s.z[1] +
+                           (float)(e[2] - b[2]) * s.z[2]) / s.area_f;
                 if (d >= 0.0f && d <= 1.0f) {
                     d = d + 0.0f;  // -0 -> +0
                     const unsigned long long key =
@@ -218,13 +224,14 @@ __device__ __forceinline__ void raster_own(const Setup& s, uint32_t tri, uint32_
 __device__ __forceinline__ void raster_pixel32(const Setup& s, int32_t px, int32_t py, uint32_t tri, uint32_t W,
                                                unsigned long long* frag) {
     const int32_t cx = px * 256 + 128, cy = py * 256 + 128;
-    int32_t e[3];
+    int32_t e[3], out = 0;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const int i = k == 2 ? 0 : k + 1, j = k == 0 ? 2 : (k == 1 ? 0 : 1);
         e[k] = (s.x[j] - s.x[i]) * (cy - s.y[i]) - (s.y[j] - s.y[i]) * (cx - s.x[i]);
-        if (!(e[k] > 0 || (e[k] == 0 && ((s.incl >> k) & 1)))) return;
+        out |= e[k] + ((s.incl >> k) & 1) - 1;  // negative: outside edge k (as in raster_small)
     }
+    if (out < 0) return;
     float d = ((float)e[0] * s.z[0] + (float)e[1] * s.z[1] + (float)e[2] * s.z[2]) / s.area_f;
     if (!(d >= 0.0f && d <= 1.0f)) return;
     d = d + 0.0f;  // -0 -> +0
