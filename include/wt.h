@@ -209,14 +209,21 @@ wt_status wt_gerstner_displace(const wt_patch* patches, uint32_t n_patches,
  *     wave_count is larger than the array holds (about 17,000 slots), or a
  *     patch fails the device-side validation, the call still returns WT_OK
  *     and leaves the outputs of the whole table (or of the failing patch)
- *     unwritten: this entry point cannot report device-side results (use
- *     wt_gerstner_displace and wt_workspace_status to see them). */
+ *     unwritten; wt_noalloc_status reads that device-side result back. */
 wt_status wt_gerstner_displace_noalloc(const wt_patch* patches, uint32_t n_patches,
                                        uint64_t total_wave_slots,
                                        const wt_wave* waves, uint32_t n_waves,
                                        const wt_heightmap* hm,
                                        float* pos_out, float* nrm_out, uint64_t out_capacity,
                                        uint32_t flags, wt_stream stream);
+
+/* wt_workspace_status for the no-alloc entry point: reads back (synchronising
+ * `stream`) the validation word that the last wt_gerstner_displace_noalloc
+ * call on the current device wrote into the library's array: WT_OK,
+ * WT_ERR_NOMEM when the patches' wave slots did not fit it (nothing written),
+ * or WT_ERR_INVALID_ARG with the first offending patch in *bad_patch (may be
+ * NULL).  Allocates nothing; WT_OK before any call on the device. */
+wt_status wt_noalloc_status(wt_stream stream, uint32_t* bad_patch);
 
 /* The same work issued as one launch pair per patch (no batching).  Exists to
  * measure the batched launch against; results are identical. */

@@ -36,6 +36,14 @@ def _noalloc(wt, surf, pos, nrm, flags, n_patches=None, slots=None):
     return st
 
 
+def _status(wt):
+    """wt_noalloc_status: (status, first offending patch)."""
+    import ctypes as C
+    bad = C.c_uint32(0)
+    st = wt.lib().wt_noalloc_status(wt.stream_handle(), C.byref(bad))
+    return st, bad.value
+
+
 def _compare(ref_pos, ref_nrm, pos, nrm):
     """The same launches on the same inputs: the same bits (the tolerances
     of the other parity tests hold a fortiori)."""
@@ -69,6 +77,7 @@ def test_noalloc_matches_workspace_entry_point_on_consecutive_calls(wt, gpu, fla
         pos.fill_(float("nan"))
         nrm.fill_(float("nan"))
         assert _noalloc(wt, s, pos, nrm, flags) == 0, wt.lib().wt_last_error()
+        assert _status(wt)[0] == 0
         _compare(*refs[k], pos, nrm)
 
 
@@ -106,9 +115,35 @@ def test_noalloc_leaves_outputs_unwritten_when_the_wave_slots_overflow_its_scrat
     nrm.fill_(float("nan"))
     assert _noalloc(wt, s, pos, nrm, 0, slots=16384) == 0  # understated: passes the host check
     assert torch.isnan(pos).all() and torch.isnan(nrm).all()
+    assert _status(wt)[0] == wt.abi.WT_ERR_NOMEM
     small = wt.Surface(pt[:8], waves)
     p2, n2 = small.alloc_outputs(0)
     assert _noalloc(wt, small, p2, n2, 0) == 0
+    assert _status(wt)[0] == 0
     ref_p, ref_n = small.displace()
     torch.cuda.synchronize()
     assert torch.equal(p2, ref_p) and torch.equal(n2, ref_n)
+
+
+def test_noalloc_status_names_the_patch_that_fails_device_side_validation(wt, gpu):
+    """A patch whose wave range runs past the wave array passes the host's
+    checks (the table is device memory) and fails the first kernel's: the
+    call returns WT_OK, that patch's outputs stay unwritten, the others are
+    written, and wt_noalloc_status reports WT_ERR_INVALID_ARG at that patch."""
+    import torch
+    from wave_tool_gb300 import workloads
+    w = workloads.small_random(11, n_patches=3, side_range=(4, 40), heightmap=False)
+    pt = w.patches.copy()
+    pt[1]["wave_offset"] = len(w.waves)
+    pt[1]["wave_count"] = 1
+    s = wt.Surface(pt, w.waves)
+    pos, nrm = s.alloc_outputs(0)
+    pos.fill_(float("nan"))
+    nrm.fill_(float("nan"))
+    assert _noalloc(wt, s, pos, nrm, 0) == 0
+    assert _status(wt) == (wt.abi.WT_ERR_INVALID_ARG, 1)
+    assert b"patch 1" in wt.lib().wt_last_error()
+    for p in range(3):
+        o, n = int(pt[p]["out_offset"]), int(pt[p]["cols"]) * int(pt[p]["rows"])
+        assert bool(torch.isnan(pos[o:o + n]).all()) == (p == 1)
+

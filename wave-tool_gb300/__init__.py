@@ -29,7 +29,7 @@ LIB_PATH = HERE / "_build" / "libwt_gb300.so"
 # every symbol include/wt.h declares
 EXPORTED = [
     "wt_version", "wt_last_error", "wt_displace_workspace_size", "wt_adjoint_workspace_size",
-    "wt_workspace_status", "wt_gerstner_displace", "wt_gerstner_displace_noalloc",
+    "wt_workspace_status", "wt_gerstner_displace", "wt_gerstner_displace_noalloc", "wt_noalloc_status",
     "wt_gerstner_displace_unbatched",
     "wt_gerstner_adjoint", "wt_grid_indices", "wt_noise_synth", "wt_wave_from_reference",
     "wt_measure_peaks", "wt_set_tuning", "wt_get_tuning", "wt_autotune_displace",
@@ -105,6 +105,7 @@ def lib():
         L.wt_displace_workspace_size.argtypes = [u32, u64, C.POINTER(sz)]
         L.wt_adjoint_workspace_size.argtypes = [vp, u32, C.POINTER(sz)]
         L.wt_workspace_status.argtypes = [vp, vp, C.POINTER(u32)]
+        L.wt_noalloc_status.argtypes = [vp, C.POINTER(u32)]
         L.wt_gerstner_displace.argtypes = [vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, u64, u32, vp, sz, vp]
         L.wt_gerstner_displace_noalloc.argtypes = [vp, u32, u64, vp, u32, C.POINTER(CHeightmap), vp, vp, u64, u32,
                                                    vp]

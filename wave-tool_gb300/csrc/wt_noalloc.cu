@@ -108,3 +108,19 @@ extern "C" wt_status wt_gerstner_displace_noalloc(const wt_patch* patches, uint3
     if (e != cudaSuccess) return cuda_fail(e, "forward launch");
     return WT_OK;
 }
+
+extern "C" wt_status wt_noalloc_status(wt_stream stream, uint32_t* bad_patch) {
+    void* ws = nullptr;
+    const wt_status st = scratch_address(&ws);
+    if (st != WT_OK) return st;
+    uint32_t h[2] = {0, 0};  // the header's status word and first offending patch
+    cudaError_t e = cudaMemcpyAsync(h, ws, sizeof(h), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "reading the no-alloc status");
+    if (bad_patch) *bad_patch = h[1];
+    if (h[0] == WT_OK) return WT_OK;
+    if (h[0] == WT_ERR_NOMEM) return fail(WT_ERR_NOMEM, "no-alloc scratch too small for the patches' wave slots");
+    char buf[96];
+    snprintf(buf, sizeof(buf), "device-side validation failed at patch %u", h[1]);
+    return fail((wt_status)h[0], buf);
+}
