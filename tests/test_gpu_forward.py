@@ -101,6 +101,37 @@ def test_batched_equals_unbatched_and_is_deterministic(wt, gpu):
     assert np.array_equal(a, c) and np.array_equal(na, nc)
 
 
+def test_small_table_prep_matches_the_general_prep(wt, oracle, gpu):
+    """Tables of at most 32 patches with at most 1024 (patch, wave) pairs take
+    a shared-memory prep; 33 patches take the general one (two prep kernels).
+    The same 32 patches give the same bits either way, and the FP64 oracle
+    agrees; a structurally invalid and a bad-wave patch are reported alike."""
+    from wave_tool_gb300 import workloads
+    w = workloads.small_random(23, n_patches=33, side_range=(2, 60), n_waves_range=(0, 32))
+    pt = w.patches.copy()
+    waves = w.waves[:32].copy()
+    rng = np.random.default_rng(23)
+    for i in range(len(pt)):
+        off = int(rng.integers(0, 32))
+        pt[i]["wave_offset"] = off
+        pt[i]["wave_count"] = int(rng.integers(0, 33 - off))
+    small = workloads.Workload("small32", pt[:32].copy(), waves, w.heightmap)
+    a, na, tex = run(wt, small)
+    b, nb, _ = run(wt, workloads.Workload("general33", pt, waves, w.heightmap))
+    n32 = int(pt[31]["out_offset"] + pt[31]["cols"] * pt[31]["rows"])
+    assert np.array_equal(a, b[:n32]) and np.array_equal(na, nb[:n32])
+    check_against_f64(oracle, small, a, na, tex)
+    bad = pt[:32].copy()
+    bad[5]["cols"] = 1
+    bad_waves = waves.copy()
+    k = next(i for i in range(32) if i != 5 and bad[i]["wave_count"] > 0)
+    bad_waves[int(bad[k]["wave_offset"])]["wavelength"] = np.nan
+    for table in (bad, np.concatenate([bad, pt[32:]])):
+        surf = wt.Surface(table, bad_waves, wt.heightmap_from(w.heightmap))
+        surf.displace()
+        assert surf.status() == (wt.abi.WT_ERR_INVALID_ARG, min(5, k))
+
+
 def test_config3_subset_against_f64(wt, oracle, gpu):
     """Sixteen config-3 patches (uneven sides 64..1024, 8..64 waves, noise
     layer), all checked against FP64."""

@@ -146,6 +146,163 @@ __device__ __forceinline__ bool patch_ok(const wt_patch& P, uint32_t n_waves, ui
            isfinite(P.time_s) && finitef(P.y_offset);
 }
 
+// Tables of at most kSmallPrep patches whose constants are formed here too
+// (k_prep_scan with fuse_coef): the whole prep through shared memory, with
+// two dependent global loads (the patches, then each pair's wave) instead of
+// the general path's chain of global-memory scans.  Writes what the general
+// path writes: header, pair and tile prefixes, the order, tiles, the
+// constants and, for the adjoint, its queue (adj_scan_body's arrays).
+constexpr uint32_t kSmallPrep = 32;
+
+__device__ void prep_small(const wt_patch* __restrict__ patches, uint32_t n, const wt_wave* __restrict__ waves,
+                           uint32_t n_waves, uint64_t out_capacity, uint64_t coef_capacity, uint32_t tile_cols,
+                           char* ws, const WsLayout& L, const HmDev& hm, int do_adj, const AdjLayout& AL,
+                           uint32_t adj_chunk_max, uint32_t adj_min_tiles) {
+    __shared__ wt_patch sp[kSmallPrep];
+    __shared__ uint32_t s_sorted[kSmallPrep];      // patch at each sorted rank
+    __shared__ uint32_t s_off[kSmallPrep + 1];     // pair prefix over the structurally valid patches
+    __shared__ uint32_t s_rank_tiles[kSmallPrep];  // tiles of the patch at each sorted rank
+    __shared__ uint32_t s_struct_bad, s_wave_bad;  // bit p: patch p fails that check
+    WsHeader* hdr = reinterpret_cast<WsHeader*>(ws);
+    uint32_t* sorted = reinterpret_cast<uint32_t*>(ws + L.sorted);
+    uint32_t* tile_pre = reinterpret_cast<uint32_t*>(ws + L.tile_pre);
+    uint32_t* pair_off = reinterpret_cast<uint32_t*>(ws + L.pair_off);
+    uint32_t* tiles_g = reinterpret_cast<uint32_t*>(ws + L.tiles);
+    PatchAux* aux = reinterpret_cast<PatchAux*>(ws + L.aux);
+    PairCoef* coef = reinterpret_cast<PairCoef*>(ws + L.coef);
+    const uint32_t tid = threadIdx.x, lane = tid & 31u;
+    constexpr unsigned kAll = 0xffffffffu;
+
+    if (tid < n) sp[tid] = patches[tid];
+    if (tid == 0) s_wave_bad = 0;
+    __syncthreads();
+    uint32_t tiles_p = 0;  // warp 0: lane p's patch
+    if (tid < 32) {
+        bool ok = false;
+        uint32_t wc = 0;
+        if (tid < n) {
+            const wt_patch& P = sp[tid];
+            ok = patch_ok(P, n_waves, out_capacity);
+            wc = ok ? P.wave_count : 0u;
+            tiles_p = ok ? P.rows * tiles_per_row(P.cols, tile_cols / 32) : 0u;
+        }
+        uint32_t x = wc;  // inclusive prefix of the pair counts
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kAll, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (tid < n) s_off[tid + 1] = x;
+        if (tid == 0) s_off[0] = 0;
+        const unsigned bad = __ballot_sync(kAll, tid < n && !ok);
+        if (tid == 0) s_struct_bad = bad;
+    }
+    __syncthreads();
+    const uint32_t total_pairs = s_off[n];
+    const bool nomem = total_pairs > coef_capacity;
+    // one (patch, wave) pair per thread (at most 1024 with fuse_coef)
+    if (tid < total_pairs) {
+        uint32_t p = 0;
+        while (s_off[p + 1] <= tid) ++p;
+        const wt_patch& Pt = sp[p];
+        const wt_wave w = waves[Pt.wave_offset + (tid - s_off[p])];
+        if (!wave_ok(w)) atomicOr(&s_wave_bad, 1u << p);
+        if (!nomem) coef[tid] = make_pair_coef(Pt, w);
+    }
+    if (tid < n && !nomem) aux[tid] = make_patch_aux(sp[tid], hm, s_off[tid]);
+    __syncthreads();
+    if (tid >= 32) return;
+    const unsigned bad = s_struct_bad | s_wave_bad;
+    if (tid < n && ((s_wave_bad >> tid) & 1u)) tiles_p = 0;
+    if (tid < n) {
+        pair_off[tid] = s_off[tid];
+        tiles_g[tid] = tiles_p;
+    }
+    bool adj_nomem = false;  // lane 0
+    if (nomem) {
+        // workspace too small for the wave slots: run nothing
+        if (tid < n) tile_pre[tid] = 0;
+        if (tid == 0) {
+            tile_pre[n] = 0;
+            pair_off[n] = 0;
+            if (do_adj) hdr->total_chunks = 0;
+        }
+    } else {
+        // descending wave count, ties by index (as the general path's rank sort)
+        const uint32_t key = tid < n ? min(sp[tid].wave_count, (uint32_t)kSortBins - 1) : 0u;
+        uint32_t rank = 0;
+        for (uint32_t q = 0; q < n; ++q) {
+            const uint32_t kq = __shfl_sync(kAll, key, q);
+            rank += kq > key || (kq == key && q < tid);
+        }
+        if (tid < n) {
+            sorted[rank] = tid;
+            s_rank_tiles[rank] = tiles_p;
+        }
+        __syncwarp();
+        const uint32_t tq = tid < n ? s_rank_tiles[tid] : 0u;
+        uint32_t x = tq;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kAll, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        const uint32_t total_tiles = __shfl_sync(kAll, x, 31);
+        if (tid < n) tile_pre[tid] = x - tq;
+        if (tid == 0) {
+            tile_pre[n] = total_tiles;
+            pair_off[n] = total_pairs;
+        }
+        if (tid == 0) hdr->total_tiles = total_tiles;
+        if (do_adj) {
+            // the adjoint's queue: each patch's rank, its chunks of tiles and
+            // the prefixes of chunks and of records (chunks x waves) over the
+            // sorted order, summed in 32 bits as the general path does
+            uint32_t* rank_g = reinterpret_cast<uint32_t*>(ws + AL.rank);
+            uint32_t* part_off = reinterpret_cast<uint32_t*>(ws + AL.part_off);
+            uint32_t* chunk_pre = reinterpret_cast<uint32_t*>(ws + AL.chunk_pre);
+            if (tid < n) s_sorted[rank] = tid;
+            __syncwarp();
+            const uint32_t chunk = total_tiles >= adj_min_tiles ? adj_chunk_max : 1u;
+            uint32_t chunks = 0, rec = 0;
+            if (tid < n) {
+                const uint32_t pq = s_sorted[tid];
+                chunks = (tq + chunk - 1) / chunk;
+                const uint64_t r = (uint64_t)chunks * (s_off[pq + 1] - s_off[pq]);
+                rec = r > 0xffffffffull ? 0xffffffffu : (uint32_t)r;
+                rank_g[pq] = tid;
+            }
+            uint32_t xr = rec, xc = chunks;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t yr = __shfl_up_sync(kAll, xr, o), yc = __shfl_up_sync(kAll, xc, o);
+                if (lane >= (uint32_t)o) {
+                    xr += yr;
+                    xc += yc;
+                }
+            }
+            const uint32_t total_rec = __shfl_sync(kAll, xr, 31), total_chunks = __shfl_sync(kAll, xc, 31);
+            if (tid < n) {
+                part_off[tid] = xr - rec;
+                chunk_pre[tid] = xc - chunks;
+            }
+            if (tid == 0) {
+                part_off[n] = total_rec;
+                chunk_pre[n] = total_chunks;
+                hdr->adj_chunk = chunk;
+                const bool over = (uint64_t)total_rec > AL.cap_records || total_rec == 0xffffffffu || total_tiles == 0;
+                hdr->total_chunks = over ? 0u : total_chunks;
+                adj_nomem = over && total_tiles != 0;
+            }
+        }
+    }
+    if (tid == 0) {
+        hdr->status = bad ? (uint32_t)WT_ERR_INVALID_ARG : (nomem || adj_nomem ? (uint32_t)WT_ERR_NOMEM : 0u);
+        hdr->bad_patch = bad ? (uint32_t)(__ffs(bad) - 1) : kNoPatch;
+        hdr->tile_counter = 0;
+        hdr->n_patches = n;
+        hdr->tile_cols = tile_cols;
+        if (nomem) hdr->total_tiles = 0;
+    }
+}
+
 // fuse_coef: also form the per-(patch, wave) and per-patch constants here
 // (small tables: the host passes it when n_patches * n_waves <= 1024, one
 // pair per thread), so that no second prep kernel runs.
@@ -162,6 +319,11 @@ __global__ void __launch_bounds__(1024) k_prep_scan(const wt_patch* __restrict__
     // waits at its start anyway)
     if (!fuse_coef) cudaTriggerProgrammaticLaunchCompletion();
 #endif
+    if (n <= kSmallPrep && fuse_coef) {
+        prep_small(patches, n, waves, n_waves, out_capacity, coef_capacity, tile_cols, ws, L, hm, do_adj, AL,
+                   adj_chunk_max, adj_min_tiles);
+        return;
+    }
     WsHeader* hdr = reinterpret_cast<WsHeader*>(ws);
     uint32_t* sorted = reinterpret_cast<uint32_t*>(ws + L.sorted);
     uint32_t* tile_pre = reinterpret_cast<uint32_t*>(ws + L.tile_pre);
