@@ -275,6 +275,8 @@ def build_frame(wt, workloads):
     n = pos.shape[0]
     outs = {k: torch.empty((n, 2 if k == "ndc0" else 4), device="cuda")
             for k in ("clip", "ndc0", "view", "facing", "nrm_yaw")}
+    # and the fused displacement + vertex stage the frame runs
+    stage_tuning = surf.autotune_stage(view_dev, outs, reps=5)
 
     # the fragment stage at 1920 x 1080: seeded sky box and local reflection /
     # refraction targets, nothing drawn behind the water
@@ -308,7 +310,7 @@ def build_frame(wt, workloads):
                        local_refractions=lrefr, colour=colour, stream=s)
 
     return dict(frame=frame, raster=raster, shade=shade, n=n, waves=len(w.waves), VW=VW, VH=VH, frags=frags,
-                tuning=tuning,
+                tuning=tuning, stage_tuning=stage_tuning,
                 projected_grid=lambda: wt.projected_grid_async(cam_dev, surf.patches, view_dev),
                 displace=lambda: surf.displace(pos, nrm, flags=wt.WT_OUT_WORLD),
                 vertex_stage=lambda: wt.vertex_stage(view_dev, pos, nrm, out=outs),
@@ -368,7 +370,7 @@ def frame_pipeline(wt, workloads, stream, flush):
     except (OSError, KeyError, ValueError):
         hbm_peak, peak_src = 6800.0, "fallback 6.8 TB/s"
     return {"vertices": n, "terms": n * F["waves"], "viewport": [VW, VH], "water_pixels_frac": covered,
-            "displace_tuning": F["tuning"],
+            "displace_tuning": F["tuning"], "stage_tuning": F["stage_tuning"],
             "frame_graph_ms": fms, "frame_graph_unfused_ms": graph_ms[False], "raster_ms": rms, "shade_ms": sms,
             "noise_512sq_64terms_animated_ms": nms,
             "displace_with_fused_stage_ms": fsms,

@@ -564,6 +564,20 @@ wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches,
                                uint32_t flags, void* workspace, size_t workspace_bytes,
                                uint32_t reps, wt_tuning* best, wt_stream stream);
 
+/* The same for wt_gerstner_displace_stage (the vertex stage in the
+ * displacement's epilogue favours other shapes: on a 1024^2 frame grid 4
+ * vertices per lane ran 47 us against 52.5 us for the plain forward's 8).
+ * The winner is kept for later wt_gerstner_displace_stage calls in the bucket
+ * (which otherwise use the plain forward's shape); wt_set_tuning drops it.
+ * Arguments as wt_gerstner_displace_stage; the outputs are overwritten. */
+wt_status wt_autotune_displace_stage(const wt_patch* patches, uint32_t n_patches,
+                                     const wt_wave* waves, uint32_t n_waves,
+                                     const wt_heightmap* hm, const wt_view* view,
+                                     float* pos_out, float* nrm_out, uint64_t out_capacity,
+                                     uint32_t flags, const wt_stage_outputs* outputs,
+                                     void* workspace, size_t workspace_bytes,
+                                     uint32_t reps, wt_tuning* best, wt_stream stream);
+
 /* ---- measurement helpers ------------------------------------------------ */
 
 /* Measures this GPU's FP32 FMA rate (FMA/s) and MUFU sine rate (sin/s) with

@@ -203,6 +203,39 @@ def test_fused_vertex_stage_ragged_batches(wt, gpu, seed):
         assert torch.equal(fused[k][cov], ref[k][cov]), k
 
 
+def test_stage_autotuner_keeps_its_own_shape(wt, gpu):
+    """wt_autotune_displace_stage picks one of the candidate shapes and later
+    displace_stage calls in that bucket use it (the same bits as with the
+    shape set explicitly), while plain displace calls keep theirs; validation
+    as displace_stage's."""
+    import torch
+    cam = wt.camera(position=(3.0, 6.0, 20.0), yaw_deg=-80.0, pitch_deg=-20.0, aspect=1.6,
+                    displaceable_amplitude=2.0)
+    surf, view = frame_surface(wt, cam, side=257, n_waves=24)
+    vd = dev_view(wt, view)
+    old = wt.get_tuning()
+    try:
+        wt.set_tuning(warps_per_block=16, max_vertices_per_lane=8, wave_chunk=32, epilogue_in_shared=0)
+        plain_before = surf.displace(flags=wt.WT_OUT_WORLD)[0].clone()
+        out = surf.displace_stage(vd)
+        best = surf.autotune_stage(vd, out, reps=1)
+        assert (best["max_vertices_per_lane"], best["warps_per_block"]) in {(8, 8), (8, 16), (4, 8)}
+        assert best["wave_chunk"] in (16, 32)
+        tuned = {k: v.clone() for k, v in surf.displace_stage(vd).items()}
+        plain_after = surf.displace(flags=wt.WT_OUT_WORLD)[0]
+        wt.set_tuning(**best)
+        explicit = surf.displace_stage(vd)
+        torch.cuda.synchronize()
+        with pytest.raises(wt.WtError):
+            surf.autotune_stage(vd, out, flags=wt.WT_OUT_DISPLACEMENT, reps=1)
+    finally:
+        wt.set_tuning(**old)
+    assert surf.status()[0] == 0
+    assert torch.equal(plain_before, plain_after)
+    for k in ("clip", "ndc0", "view", "facing", "nrm_yaw"):
+        assert torch.equal(tuned[k], explicit[k]), k
+
+
 def test_fused_vertex_stage_validation(wt, gpu):
     surf, view = frame_surface(wt, wt.camera(position=(0.0, 4.0, 30.0), displaceable_amplitude=1.0), side=33)
     vd = dev_view(wt, view)

@@ -32,7 +32,7 @@ EXPORTED = [
     "wt_workspace_status", "wt_gerstner_displace", "wt_gerstner_displace_noalloc", "wt_noalloc_status",
     "wt_gerstner_displace_unbatched",
     "wt_gerstner_adjoint", "wt_grid_indices", "wt_noise_synth", "wt_wave_from_reference",
-    "wt_measure_peaks", "wt_set_tuning", "wt_get_tuning", "wt_autotune_displace",
+    "wt_measure_peaks", "wt_set_tuning", "wt_get_tuning", "wt_autotune_displace", "wt_autotune_displace_stage",
     "wt_projected_grid", "wt_projected_grid_async", "wt_vertex_stage", "wt_heightmap_from_unorm8",
     "wt_water_raster", "wt_water_raster_workspace_size", "wt_water_shade",
     "wt_gerstner_displace_saving", "wt_gerstner_adjoint_saved", "wt_gerstner_displace_stage",
@@ -129,6 +129,8 @@ def lib():
         L.wt_get_tuning.argtypes = [C.POINTER(CTuning)]
         L.wt_autotune_displace.argtypes = [vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, u64, u32, vp, sz, u32,
                                            C.POINTER(CTuning), vp]
+        L.wt_autotune_displace_stage.argtypes = [vp, u32, vp, u32, C.POINTER(CHeightmap), vp, vp, vp, u64, u32,
+                                                 C.POINTER(CStageOutputs), vp, sz, u32, C.POINTER(CTuning), vp]
         L.wt_projected_grid.argtypes = [vp, vp, vp, C.POINTER(u32)]
         L.wt_projected_grid_async.argtypes = [vp, vp, vp, vp]
         L.wt_vertex_stage.argtypes = [vp, vp, vp, u64, u32, vp, vp, vp, vp, vp, vp]
@@ -336,6 +338,20 @@ class Surface:
             self.patches.data_ptr(), self.n_patches, self.waves.data_ptr(), self.n_waves,
             C.byref(hm) if hm is not None else None, pos.data_ptr(), _ptr(nrm), pos.shape[0], flags,
             self.workspace.data_ptr(), self.workspace.numel(), reps, C.byref(best), stream_handle(stream)))
+        return {f: getattr(best, f) for f, _ in CTuning._fields_}
+
+    def autotune_stage(self, view_dev, out, pos=None, nrm=None, flags: int = 0, reps: int = 3, stream=None) -> dict:
+        """Times the candidate launch shapes of displace_stage on this surface
+        (out: the stage outputs, as displace_stage returns them) and keeps the
+        fastest for later displace_stage calls (process-wide)."""
+        hm = self.heightmap.cstruct() if self.heightmap is not None else None
+        so = CStageOutputs(*[_ptr(out.get(k)) for k in ("clip", "ndc0", "view", "facing", "nrm_yaw")])
+        best = CTuning()
+        check(lib().wt_autotune_displace_stage(
+            self.patches.data_ptr(), self.n_patches, self.waves.data_ptr(), self.n_waves,
+            C.byref(hm) if hm is not None else None, view_dev.data_ptr(), _ptr(pos), _ptr(nrm), self.n_vertices,
+            flags, C.byref(so), self.workspace.data_ptr(), self.workspace.numel(), reps, C.byref(best),
+            stream_handle(stream)))
         return {f: getattr(best, f) for f, _ in CTuning._fields_}
 
 

@@ -39,10 +39,12 @@ wt_status cuda_fail(cudaError_t e, const char* what) {
 bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
 
 // Forward launch tuning: a default (wt_set_tuning) and the autotuner's
-// winners cached per shape bucket (bit lengths of the patch and wave counts).
+// winners cached per shape bucket (bit lengths of the patch and wave counts),
+// one cache for the plain forward and one for the forward with the vertex
+// stage in its epilogue (its heavier epilogue favours other shapes).
 std::mutex g_tune_mu;
 wt::FwdConfig g_fwd_cfg = {8, 32, 16, 0, 1};
-std::map<uint32_t, wt::FwdConfig> g_tuned;
+std::map<uint32_t, wt::FwdConfig> g_tuned, g_tuned_stage;
 
 uint32_t bit_length(uint32_t x) {
     uint32_t b = 0;
@@ -122,10 +124,34 @@ wt::FwdConfig current_cfg() {
     return g_fwd_cfg;
 }
 
+// The arguments wt_gerstner_displace_stage adds to wt_gerstner_displace.
+wt_status check_stage(const wt_view* view, const wt_stage_outputs* outputs, uint32_t flags) {
+    if (!view || !aligned(view, 4)) return fail(WT_ERR_INVALID_ARG, "view NULL or not 4-byte aligned");
+    if (!outputs) return fail(WT_ERR_INVALID_ARG, "outputs is NULL");
+    if (flags & (WT_OUT_DISPLACEMENT | WT_PHASE_FP32_NAIVE))
+        return fail(WT_ERR_INVALID_ARG, "displace_stage: the vertex stage needs world positions and the FP64 phase");
+    if (outputs->clip && !aligned(outputs->clip, 16)) return fail(WT_ERR_INVALID_ARG, "clip not 16-byte aligned");
+    if (outputs->ndc0 && !aligned(outputs->ndc0, 8)) return fail(WT_ERR_INVALID_ARG, "ndc0 not 8-byte aligned");
+    const float* f4[3] = {outputs->view, outputs->facing, outputs->nrm_yaw};
+    for (const float* q : f4)
+        if (q && !aligned(q, 16)) return fail(WT_ERR_INVALID_ARG, "view / facing / nrm_yaw not 16-byte aligned");
+    return WT_OK;
+}
+
 wt::FwdConfig cfg_for(uint32_t n_patches, uint32_t n_waves) {
     std::lock_guard<std::mutex> g(g_tune_mu);
     auto it = g_tuned.find(shape_bucket(n_patches, n_waves));
     return it != g_tuned.end() ? it->second : g_fwd_cfg;
+}
+
+// the fused vertex stage: its own tuned shape, else the plain forward's
+wt::FwdConfig cfg_for_stage(uint32_t n_patches, uint32_t n_waves) {
+    {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        auto it = g_tuned_stage.find(shape_bucket(n_patches, n_waves));
+        if (it != g_tuned_stage.end()) return it->second;
+    }
+    return cfg_for(n_patches, n_waves);
 }
 
 wt_status run_displace(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
@@ -249,20 +275,13 @@ wt_status wt_gerstner_displace_stage(const wt_patch* patches, uint32_t n_patches
                                      const wt_stage_outputs* outputs, void* workspace, size_t workspace_bytes,
                                      wt_stream stream) {
     WT_NVTX_RANGE("wt_gerstner_displace_stage");
-    if (!view || !aligned(view, 4)) return fail(WT_ERR_INVALID_ARG, "view NULL or not 4-byte aligned");
-    if (!outputs) return fail(WT_ERR_INVALID_ARG, "outputs is NULL");
-    if (flags & (WT_OUT_DISPLACEMENT | WT_PHASE_FP32_NAIVE))
-        return fail(WT_ERR_INVALID_ARG, "displace_stage: the vertex stage needs world positions and the FP64 phase");
-    if (outputs->clip && !aligned(outputs->clip, 16)) return fail(WT_ERR_INVALID_ARG, "clip not 16-byte aligned");
-    if (outputs->ndc0 && !aligned(outputs->ndc0, 8)) return fail(WT_ERR_INVALID_ARG, "ndc0 not 8-byte aligned");
-    const float* f4[3] = {outputs->view, outputs->facing, outputs->nrm_yaw};
-    for (const float* q : f4)
-        if (q && !aligned(q, 16)) return fail(WT_ERR_INVALID_ARG, "view / facing / nrm_yaw not 16-byte aligned");
+    const wt_status st = check_stage(view, outputs, flags);
+    if (st != WT_OK) return st;
     wt::FwdExtra x{};
     x.view = view;
     x.stage = wt::StageOut{outputs->clip, outputs->ndc0, outputs->view, outputs->facing, outputs->nrm_yaw};
     return run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags, workspace,
-                        workspace_bytes, (cudaStream_t)stream, cfg_for(n_patches, n_waves), x);
+                        workspace_bytes, (cudaStream_t)stream, cfg_for_stage(n_patches, n_waves), x);
 }
 
 wt_status wt_gerstner_displace_unbatched(const wt_patch* host_patches, const wt_patch* patches,
@@ -454,6 +473,7 @@ wt_status wt_set_tuning(const wt_tuning* t) {
     std::lock_guard<std::mutex> g(g_tune_mu);
     g_fwd_cfg = c;
     g_tuned.clear();  // an explicit shape replaces the autotuned ones
+    g_tuned_stage.clear();
     return WT_OK;
 }
 
@@ -468,13 +488,20 @@ wt_status wt_get_tuning(wt_tuning* t) {
     return WT_OK;
 }
 
-wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
-                               const wt_heightmap* hm, float* pos_out, float* nrm_out, uint64_t out_capacity,
-                               uint32_t flags, void* workspace, size_t workspace_bytes, uint32_t reps,
-                               wt_tuning* best, wt_stream stream) {
-    WT_NVTX_RANGE("wt_autotune_displace");
+}  // extern "C"
+
+namespace {
+
+// The autotuner's loop: `run(c)` launches the call being tuned with shape c,
+// `clear()` writes its output buffers (outside the timed events, so that a
+// timed call finds its inputs as cold as in a frame or training step: timed
+// back to back with a warm L2 the shapes ranked differently, a 16-wave chunk
+// winning there and losing 4 % in the cold case).  The winner goes into
+// `cache` for the table's shape bucket.
+template <typename Run, typename Clear>
+wt_status autotune(Run run, Clear clear, uint32_t n_patches, uint32_t n_waves, uint32_t reps, cudaStream_t s,
+                   std::map<uint32_t, wt::FwdConfig>& cache, const wt::FwdConfig& start, wt_tuning* best) {
     if (reps == 0 || reps > 1000) return fail(WT_ERR_INVALID_ARG, "reps must be in [1, 1000]");
-    cudaStream_t s = (cudaStream_t)stream;
     cudaEvent_t e0, e1;
     cudaError_t e = cudaEventCreate(&e0);
     if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
@@ -483,22 +510,14 @@ wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches, cons
     const int shapes[][3] = {{8, 8, 0}, {8, 16, 0}, {8, 8, 1}, {8, 16, 1}, {4, 8, 0}};  // (vertices/lane, warps, epi)
     const int chunks[] = {16, 32};
     float best_ms = 1e30f;
-    wt::FwdConfig best_cfg = current_cfg();
+    wt::FwdConfig best_cfg = start;
     wt_status st = WT_OK;
-    // Each timed call is preceded (outside its events) by a clear of the
-    // output buffers, which evicts the last call's lines from L2 when the
-    // outputs outsize it: a call in a frame or training step finds its
-    // inputs cold, and timed back to back with a warm L2 the shapes ranked
-    // differently (a 16-wave chunk won there and lost 4 % in the cold case).
-    const size_t out_bytes = (size_t)out_capacity * ((flags & WT_LAYOUT_VEC3) ? 12 : 16);
     auto timed_batch = [&](const wt::FwdConfig& c, float* total_ms) -> wt_status {
         *total_ms = 0.0f;
         for (uint32_t r = 0; r < reps; ++r) {
-            cudaMemsetAsync(pos_out, 0, out_bytes, s);
-            if (nrm_out) cudaMemsetAsync(nrm_out, 0, out_bytes, s);
+            clear();
             cudaEventRecord(e0, s);
-            wt_status st2 = run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity,
-                                         flags, workspace, workspace_bytes, s, c);
+            wt_status st2 = run(c);
             cudaEventRecord(e1, s);
             if (st2 != WT_OK) return st2;
             cudaError_t e2 = cudaEventSynchronize(e1);
@@ -512,15 +531,12 @@ wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches, cons
     // bring the clocks up before anything is timed, then keep each
     // candidate's best of three batches over two passes: one batch per
     // candidate was enough for clock ramps and noise to reorder close shapes
-    for (uint32_t r = 0; r < 4 * reps && st == WT_OK; ++r)
-        st = run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags, workspace,
-                          workspace_bytes, s, best_cfg);
+    for (uint32_t r = 0; r < 4 * reps && st == WT_OK; ++r) st = run(best_cfg);
     for (int pass = 0; pass < 2 && st == WT_OK; ++pass)
     for (const auto& sh : shapes) {
         for (int ch : chunks) {
             wt::FwdConfig c = {sh[0], ch, sh[1], 0, sh[2]};
-            st = run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags,
-                              workspace, workspace_bytes, s, c);
+            st = run(c);
             for (int batch = 0; batch < 3 && st == WT_OK; ++batch) {
                 float ms = 0.0f;
                 st = timed_batch(c, &ms);
@@ -536,7 +552,7 @@ wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches, cons
     if (st != WT_OK) return st;
     {
         std::lock_guard<std::mutex> g(g_tune_mu);
-        g_tuned[shape_bucket(n_patches, n_waves)] = best_cfg;
+        cache[shape_bucket(n_patches, n_waves)] = best_cfg;
     }
     if (best) {
         best->warps_per_block = (uint32_t)best_cfg.warps;
@@ -546,6 +562,56 @@ wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches, cons
         best->epilogue_in_shared = (uint32_t)best_cfg.epi;
     }
     return WT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+wt_status wt_autotune_displace(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves, uint32_t n_waves,
+                               const wt_heightmap* hm, float* pos_out, float* nrm_out, uint64_t out_capacity,
+                               uint32_t flags, void* workspace, size_t workspace_bytes, uint32_t reps,
+                               wt_tuning* best, wt_stream stream) {
+    WT_NVTX_RANGE("wt_autotune_displace");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t out_bytes = (size_t)out_capacity * ((flags & WT_LAYOUT_VEC3) ? 12 : 16);
+    auto run = [&](const wt::FwdConfig& c) {
+        return run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags, workspace,
+                            workspace_bytes, s, c);
+    };
+    auto clear = [&]() {
+        cudaMemsetAsync(pos_out, 0, out_bytes, s);
+        if (nrm_out) cudaMemsetAsync(nrm_out, 0, out_bytes, s);
+    };
+    return autotune(run, clear, n_patches, n_waves, reps, s, g_tuned, current_cfg(), best);
+}
+
+wt_status wt_autotune_displace_stage(const wt_patch* patches, uint32_t n_patches, const wt_wave* waves,
+                                     uint32_t n_waves, const wt_heightmap* hm, const wt_view* view, float* pos_out,
+                                     float* nrm_out, uint64_t out_capacity, uint32_t flags,
+                                     const wt_stage_outputs* outputs, void* workspace, size_t workspace_bytes,
+                                     uint32_t reps, wt_tuning* best, wt_stream stream) {
+    WT_NVTX_RANGE("wt_autotune_displace_stage");
+    const wt_status st = check_stage(view, outputs, flags);
+    if (st != WT_OK) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t out_bytes = (size_t)out_capacity * ((flags & WT_LAYOUT_VEC3) ? 12 : 16);
+    wt::FwdExtra x{};
+    x.view = view;
+    x.stage = wt::StageOut{outputs->clip, outputs->ndc0, outputs->view, outputs->facing, outputs->nrm_yaw};
+    auto run = [&](const wt::FwdConfig& c) {
+        return run_displace(patches, n_patches, waves, n_waves, hm, pos_out, nrm_out, out_capacity, flags, workspace,
+                            workspace_bytes, s, c, x);
+    };
+    auto clear = [&]() {
+        if (pos_out) cudaMemsetAsync(pos_out, 0, out_bytes, s);
+        if (nrm_out) cudaMemsetAsync(nrm_out, 0, out_bytes, s);
+        float* f4[4] = {outputs->clip, outputs->view, outputs->facing, outputs->nrm_yaw};
+        for (float* q : f4)
+            if (q) cudaMemsetAsync(q, 0, 16 * (size_t)out_capacity, s);
+        if (outputs->ndc0) cudaMemsetAsync(outputs->ndc0, 0, 8 * (size_t)out_capacity, s);
+    };
+    return autotune(run, clear, n_patches, n_waves, reps, s, g_tuned_stage, cfg_for_stage(n_patches, n_waves), best);
 }
 
 wt_status wt_measure_peaks(void* scratch, size_t scratch_bytes, double* fma_per_s, double* sin_per_s,
