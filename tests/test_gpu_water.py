@@ -98,6 +98,40 @@ def test_raster_clipping_and_degenerate_triangles(wt, oracle, gpu):
     assert np.mean((want & 0xffffffff) != 0) > 0.5
 
 
+def test_raster_large_triangles_take_the_second_pass(wt, oracle, gpu):
+    """A full-viewport quad (two triangles of 64,000 box pixels), triangles
+    with boxes around and above the per-thread limit of 128 pixels (about
+    8 x 16 to 16 x 23) and one of exactly 128, over a field of one-pixel
+    triangles: the queue, its spread over the warps and the per-thread path
+    give the oracle's buffer bit for bit."""
+    import torch
+    rng = np.random.default_rng(31)
+    verts, tris = [], []
+
+    def add(pts):
+        base = len(verts)
+        verts.extend(pts)
+        tris.append((base, base + 1, base + 2))
+    add([(-1.0, -1.0, 0.5, 1.0), (1.0, -1.0, 0.5, 1.0), (1.0, 1.0, 0.5, 1.0)])
+    add([(-1.0, -1.0, 0.4, 1.0), (1.0, 1.0, 0.4, 1.0), (-1.0, 1.0, 0.6, 1.0)])
+    for k in range(40):                      # boxes of about 8 x 16 .. 16 x 23 pixels
+        x0, y0 = rng.uniform(-0.9, 0.8), rng.uniform(-0.9, 0.8)
+        dx, dy = (8 + k / 5) * 2 / W, (16 + k / 6) * 2 / H
+        add([(x0, y0, 0.3, 1.0), (x0 + dx, y0, 0.35, 1.0), (x0, y0 + dy, 0.25, 1.0)])
+    add([(0.0, 0.0, 0.2, 1.0), (16 * 2 / W, 0.0, 0.2, 1.0), (0.0, 8 * 2 / H, 0.2, 1.0)])  # 128-pixel box
+    for k in range(3000):                    # one-pixel triangles
+        x0, y0 = rng.uniform(-1, 1), rng.uniform(-1, 1)
+        add([(x0, y0, 0.1, 1.0), (x0 + 2.2 / W, y0, 0.1, 1.0), (x0, y0 + 2.2 / H, 0.1, 1.0)])
+    clip = np.asarray(verts, np.float32)
+    idx = np.asarray(tris, np.uint32)
+    ct, it = torch.from_numpy(clip).cuda(), torch.from_numpy(idx.view(np.int32).ravel()).cuda()
+    got = wt.water_raster(ct, it, W, H)
+    torch.cuda.synchronize()
+    want = oracle.water_raster(clip, idx.ravel(), W, H)
+    assert np.array_equal(got.cpu().numpy().view(np.uint64).ravel(), want)
+    assert np.all((want & 0xffffffff) != 0)  # the quad covers every pixel
+
+
 def test_raster_reuses_its_workspace(wt, oracle, gpu):
     """One workspace for consecutive frames of different meshes (A, B, A):
     the queue of large and clipped triangles starts empty every call."""
