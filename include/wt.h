@@ -527,12 +527,13 @@ wt_status wt_wave_from_reference(float amplitude_A, float frequency_w,
 /* ---- launch tuning ------------------------------------------------------- */
 
 /* Launch shape of the persistent forward kernel (supported: 8 vertices per
- * lane with 8 or 16 warps and either epilogue; 4 vertices per lane with 8 warps
- * and the register epilogue).  Process-wide; applies to
+ * lane with 8 or 16 warps and either epilogue, or 20 warps and the register
+ * epilogue (the saving and vertex-stage forwards run it as 16); 4 vertices per
+ * lane with 8 warps and the register epilogue).  Process-wide; applies to
  * launches issued after it is set.  No reference counterpart (the reference
  * has one fixed draw call). */
 typedef struct wt_tuning {
-    uint32_t warps_per_block; /* 8 or 16 (0 = 16) */
+    uint32_t warps_per_block; /* 8, 16 or 20 (0 = 16) */
     uint32_t blocks_per_sm;   /* 0 = as many as fit */
     uint32_t wave_chunk;      /* waves staged per warp at a time: 8, 16 or 32 (0 = 32) */
     uint32_t max_vertices_per_lane; /* widest tile = 32 * this; 4 or 8 (0 = 8).  4 halves

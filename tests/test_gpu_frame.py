@@ -219,7 +219,7 @@ def test_stage_autotuner_keeps_its_own_shape(wt, gpu):
         plain_before = surf.displace(flags=wt.WT_OUT_WORLD)[0].clone()
         out = surf.displace_stage(vd)
         best = surf.autotune_stage(vd, out, reps=1)
-        assert (best["max_vertices_per_lane"], best["warps_per_block"]) in {(8, 8), (8, 16), (4, 8)}
+        assert (best["max_vertices_per_lane"], best["warps_per_block"]) in {(8, 8), (8, 16), (8, 20), (4, 8)}
         assert best["wave_chunk"] in (16, 32)
         tuned = {k: v.clone() for k, v in surf.displace_stage(vd).items()}
         plain_after = surf.displace(flags=wt.WT_OUT_WORLD)[0]

@@ -1,7 +1,7 @@
 """Every launch shape the forward kernel supports (and the autotuner may
 pick) against the FP64 oracle, through the C ABI: vertices per lane 4 / 8,
-8 / 16 warps per block, register or shared-memory epilogue, wave chunks of 16
-and 32.  Shapes with the same vertices per lane tile every patch the same way
+8 / 16 / 20 warps per block, register or shared-memory epilogue, wave chunks of
+16 and 32.  Shapes with the same vertices per lane tile every patch the same way
 and give identical bits."""
 from __future__ import annotations
 
@@ -12,7 +12,7 @@ from helpers import angle_deg, rel_err
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(8, 8, 0), (8, 16, 0), (8, 8, 1), (8, 16, 1), (4, 8, 0)]  # (vpl, warps, epi)
+SHAPES = [(8, 8, 0), (8, 16, 0), (8, 20, 0), (8, 8, 1), (8, 16, 1), (4, 8, 0)]  # (vpl, warps, epi)
 
 
 @pytest.fixture
@@ -53,6 +53,8 @@ def test_unsupported_shape_is_rejected(wt, gpu, default_tuning):
         wt.set_tuning(16, 0, 32, 4, 1)   # 4 vertices per lane only with 8 warps and the register epilogue
     with pytest.raises(wt.WtError):
         wt.set_tuning(8, 0, 32, 8, 3)
+    with pytest.raises(wt.WtError):
+        wt.set_tuning(20, 0, 32, 8, 1)   # 20 warps only with the register epilogue
 
 
 def test_autotune_picks_a_supported_shape(wt, gpu, default_tuning):

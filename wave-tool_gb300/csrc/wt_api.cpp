@@ -507,7 +507,7 @@ wt_status autotune(Run run, Clear clear, uint32_t n_patches, uint32_t n_waves, u
     if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
     e = cudaEventCreate(&e1);
     if (e != cudaSuccess) { cudaEventDestroy(e0); return cuda_fail(e, "cudaEventCreate"); }
-    const int shapes[][3] = {{8, 8, 0}, {8, 16, 0}, {8, 8, 1}, {8, 16, 1}, {4, 8, 0}};  // (vertices/lane, warps, epi)
+    const int shapes[][3] = {{8, 8, 0}, {8, 16, 0}, {8, 20, 0}, {8, 8, 1}, {8, 16, 1}, {4, 8, 0}};  // (vertices/lane, warps, epi)
     const int chunks[] = {16, 32};
     float best_ms = 1e30f;
     wt::FwdConfig best_cfg = start;

@@ -867,14 +867,15 @@ cudaError_t launch_prep(const wt_patch* patches, uint32_t n_patches, const wt_wa
 
 bool forward_config_supported(const FwdConfig& c) {
     if (c.epi != 0 && c.epi != 1) return false;
-    if (c.s == 8) return c.warps == 8 || c.warps == 16;
+    if (c.s == 8) return c.warps == 8 || c.warps == 16 || (c.warps == 20 && c.epi == 0);
     if (c.s == 4) return c.warps == 8 && c.epi == 0;
     return false;
 }
 
 // The epilogue variants beyond the plain one exist with the register
 // epilogue only: a tuning with the shared-memory epilogue runs them through
-// the register one, same shape.
+// the register one, same shape; 20 warps (the plain forward's 96-register
+// shape) run as 16.
 template <int MODE>
 cudaError_t launch_forward_mode(const FwdConfig& cfg, const wt_patch* patches, uint32_t n_patches, const HmDev& hm,
                                 float* pos, float* nrm, uint32_t flags, void* ws, const WsLayout& L,
@@ -883,7 +884,7 @@ cudaError_t launch_forward_mode(const FwdConfig& cfg, const wt_patch* patches, u
         return launch_fwd_t<256, 3, 4, 0, MODE>(cfg, patches, n_patches, hm, pos, nrm, flags, ws, L, x, s);
     if (cfg.s == 8 && cfg.warps == 8)
         return launch_fwd_t<256, 2, 8, 0, MODE>(cfg, patches, n_patches, hm, pos, nrm, flags, ws, L, x, s);
-    if (cfg.s == 8 && cfg.warps == 16)
+    if (cfg.s == 8 && (cfg.warps == 16 || cfg.warps == 20))
         return launch_fwd_t<512, 1, 8, 0, MODE>(cfg, patches, n_patches, hm, pos, nrm, flags, ws, L, x, s);
     return cudaErrorInvalidValue;
 }
@@ -900,6 +901,10 @@ cudaError_t launch_forward(const FwdConfig& cfg, const wt_patch* patches, uint32
     if (cfg.s == 8 && cfg.epi == 0) {
         if (cfg.warps == 8) return launch_fwd_t<256, 2, 8, 0, kModePlain>(cfg, patches, n_patches, hm, pos, nrm, flags, ws, L, x, s);
         if (cfg.warps == 16) return launch_fwd_t<512, 1, 8, 0, kModePlain>(cfg, patches, n_patches, hm, pos, nrm, flags, ws, L, x, s);
+        // 20 warps at 96 registers (a few bytes spilled): more warps to hide
+        // the wave loop's latencies (256 uneven patches: 1.041 against 1.054
+        // ms for 16 warps; 18 and 24 warps were slower)
+        if (cfg.warps == 20) return launch_fwd_t<640, 1, 8, 0, kModePlain>(cfg, patches, n_patches, hm, pos, nrm, flags, ws, L, x, s);
     }
     if (cfg.s == 8 && cfg.epi == 1) {
         if (cfg.warps == 8) return launch_fwd_t<256, 2, 8, 1, kModePlain>(cfg, patches, n_patches, hm, pos, nrm, flags, ws, L, x, s);
