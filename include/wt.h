@@ -38,8 +38,8 @@ typedef enum wt_status {
     WT_OK = 0,
     WT_ERR_INVALID_ARG = 1,  /* bad pointer, size, alignment or parameter */
     WT_ERR_CUDA = 2,         /* a CUDA runtime call failed (see wt_last_error) */
-    WT_ERR_TIMEOUT = 3,      /* reserved: no kernel of this library waits on another, so
-                                no call returns it */
+    WT_ERR_TIMEOUT = 3,      /* reserved: no kernel of this library spins on a flag or on
+                                another kernel, so no call returns it */
     WT_ERR_NOMEM = 4,        /* workspace smaller than the size query asked for */
     WT_ERR_UNSUPPORTED = 5   /* a parameter combination this build does not handle */
 } wt_status;
