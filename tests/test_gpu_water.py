@@ -4,8 +4,10 @@ pinned bit for bit to water-grid.frag compiled as C++).
 
  - the visibility buffer (coverage, depth, winning triangle) is bit-exact;
  - colours agree to 2e-5 (1 + |c|): both sides round every FP32 operation
-   once in the same order; they differ only through powf (the CUDA and C
-   library implementations differ in the last bits)."""
+   once in the same order; they differ only through the powers: the sun's
+   powf (the CUDA and C library implementations differ in the last bits)
+   and the Fresnel term's fifth power, which the kernel forms as products
+   where the oracle calls powf."""
 from __future__ import annotations
 
 import numpy as np
@@ -176,6 +178,7 @@ def test_shade_against_oracle(wt, oracle, gpu, cam_kw):
     water = (frags.cpu().numpy().view(np.uint64).ravel() & 0xffffffff) != 0
     assert water.mean() > 0.05
     tol = 2e-5 * (1.0 + np.abs(want))
+    print(f"max colour difference against the oracle: {float(np.abs(got - want).max()):.2e}")
     assert np.all(np.abs(got - want) <= tol), float(np.abs(got - want).max())
     assert np.all(got[~water] == 0.0)
     gc = comp.cpu().numpy().reshape(-1, 4)

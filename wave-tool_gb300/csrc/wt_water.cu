@@ -607,7 +607,10 @@ __global__ void __launch_bounds__(256) k_water_shade(const unsigned long long* _
             sh.sun_shininess);
         const float sun = (sh.sun_strength * 1.0f) * sun_p;
         const float cos_t = N[0] * vv[0] + N[1] * vv[1] + N[2] * vv[2];
-        const float fres = 0.02f + (1.0f - 0.02f) * powf(1.0f - cos_t, 5.0f);
+        // pow(1 - cos, 5) as products, as shader compilers expand a constant
+        // integer exponent (within a few ulp of powf)
+        const float om = 1.0f - cos_t, om2 = om * om;
+        const float fres = 0.02f + (1.0f - 0.02f) * (om2 * om2 * om);
         const float ds = 0.1f * (1.0f - view_depth);  // both distortion strengths are 0.1
         const float ul0 = clampf(mixf(u0, h0, ds) + ds * NY[0], 0.0f, 1.0f);
         const float ul1 = clampf(mixf(u1, h1, ds) + ds * -NY[2], 0.0f, 1.0f);
