@@ -321,8 +321,17 @@ __global__ void __launch_bounds__(32) k_projected_grid(const wt_camera* __restri
         if (lane == 0) view->status = WT_VIEW_INVALID_CAMERA;
         return;
     }
+    // lanes 0-2: camera_trig(c, lane) with one shared instruction stream (a
+    // warp-wide FP64 operation costs ~64 cycles and a division ~550 on
+    // GB300; three divergent branches ran three sines and cosines one after
+    // another): each lane selects its own numerator and denominator
     double ts = 0.0, tc = 1.0;
-    if (lane < 3) camera_trig(c, lane, &ts, &tc);
+    if (lane < 3) {
+        const double yaw = c.yaw_deg - 360.0 * floor(c.yaw_deg / 360.0);
+        const double pitch = fmin(fmax(c.pitch_deg, -kPitchLimit), kPitchLimit);
+        const double num = lane == 0 ? yaw : (lane == 1 ? pitch : c.fov_deg);
+        sincos_pi(num / (lane == 2 ? 360.0 : 180.0), &ts, &tc);
+    }
     const double sy = __shfl_sync(0xffffffffu, ts, 0), cy = __shfl_sync(0xffffffffu, tc, 0);
     const double sp = __shfl_sync(0xffffffffu, ts, 1), cp = __shfl_sync(0xffffffffu, tc, 1);
     const double sf = __shfl_sync(0xffffffffu, ts, 2), cf = __shfl_sync(0xffffffffu, tc, 2);
@@ -362,10 +371,16 @@ __global__ void __launch_bounds__(32) k_projected_grid(const wt_camera* __restri
     const bool ok = lane < 4 && any && corner_ray(f, (lane & 1) ? x1 : x0, (lane & 2) ? y1 : y0, &gx, &gz);
     const bool visible = (__ballot_sync(0xffffffffu, ok) & 0xfu) == 0xfu;
     if (lane < 16) {
-        M4 vp, yaw;
-        view_matrices(c, f, sy, cy, &vp, &yaw);
-        view->view_projection[lane] = (float)vp.m[lane >> 2][lane & 3];
-        view->view_only_yaw[lane] = (float)yaw.m[lane >> 2][lane & 3];
+        // view_matrices, one element per lane: the two factors of the
+        // view-projection in full (cheap), then this lane's element of
+        // their product in mul's order
+        const M4 P = perspective(f.ty, c.aspect, c.z_near, c.z_far), V = view_matrix(f.cam);
+        const M4 yaw = view_matrix(Basis{f.cam.pos, D3{cy, 0.0, sy}, D3{-sy, 0.0, cy}, D3{0.0, 1.0, 0.0}});
+        const int col = lane >> 2, row = lane & 3;
+        double e = 0.0;
+        for (int j = 0; j < 4; ++j) e += P.m[j][row] * V.m[col][j];
+        view->view_projection[lane] = (float)e;
+        view->view_only_yaw[lane] = (float)yaw.m[col][row];
     }
     if (lane < 3) view->camera_position[lane] = (float)c.position[lane];
     if (lane == 0) view->status = visible ? WT_VIEW_VISIBLE : WT_VIEW_EMPTY;
