@@ -109,3 +109,22 @@ def test_saving_and_stage_entry_points_reject_bad_arguments(wt, L):
         assert stage(FAKE, 1, FAKE, 1, None, FAKE, None, None, 10, 0, C.byref(bad), FAKE, 1 << 20, None) == E, field
     bad = wt.CStageOutputs(FAKE, FAKE + 4, FAKE, FAKE, FAKE)  # ndc0 needs 8-byte alignment
     assert stage(FAKE, 1, FAKE, 1, None, FAKE, None, None, 10, 0, C.byref(bad), FAKE, 1 << 20, None) == E
+
+
+def test_stage_autotuner_rejects_bad_arguments(wt, L):
+    """wt_autotune_displace_stage checks the stage arguments (view, outputs,
+    flags, alignment) before timing anything."""
+    E = wt.abi.WT_ERR_INVALID_ARG
+    so = wt.CStageOutputs(FAKE, FAKE, FAKE, FAKE, FAKE)
+    tune = L.wt_autotune_displace_stage
+    best = wt.CTuning()
+    # (patches, n, waves, nw, hm, view, pos, nrm, cap, flags, outputs, ws, bytes, reps, best, stream)
+    assert tune(FAKE, 1, FAKE, 1, None, None, None, None, 10, 0, C.byref(so), FAKE, 1 << 20, 1, C.byref(best),
+                None) == E
+    assert tune(FAKE, 1, FAKE, 1, None, FAKE, None, None, 10, 0, None, FAKE, 1 << 20, 1, C.byref(best), None) == E
+    assert tune(FAKE, 1, FAKE, 1, None, FAKE, None, None, 10, wt.WT_PHASE_FP32_NAIVE, C.byref(so), FAKE, 1 << 20, 1,
+                C.byref(best), None) == E
+    bad = wt.CStageOutputs(ODD, FAKE, FAKE, FAKE, FAKE)
+    assert tune(FAKE, 1, FAKE, 1, None, FAKE, None, None, 10, 0, C.byref(bad), FAKE, 1 << 20, 1, C.byref(best),
+                None) == E
+    assert b"clip" in L.wt_last_error()
